@@ -1,0 +1,79 @@
+"""Run the reference's own force_calc/ewald through oracle/_ref/moldy_ref_harness.
+
+TEST INFRASTRUCTURE ONLY: used to validate the C restatement and to generate
+golden fixtures where the reference sources are present.  One configuration per
+process, because force_calc and ewald keep first-call statics
+(src/force.c:1146-1149, src/ewald.c:352-355).
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import tempfile
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+
+
+def available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "moldy_ref_harness"))
+
+
+def build() -> bool:
+    """Build oracle/_ref from the reference sources if they are present."""
+    subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True,
+                   stdout=subprocess.DEVNULL)
+    return available()
+
+
+@dataclass
+class RefResult:
+    force_real: np.ndarray      # [3, N]
+    pe_real: float
+    stress_real: np.ndarray     # [3, 3] upper triangle filled
+    force_ewald: np.ndarray     # [3, N]
+    pe_ewald: float
+    stress_ewald: np.ndarray
+    pairs: Optional[np.ndarray]  # [P, 3] int32 (isite, jsite, image index 0..26)
+    stdout: str
+    t_force: Optional[float] = None
+    t_ewald: Optional[float] = None
+
+    def notes(self):
+        return [l.strip() for l in self.stdout.splitlines() if l.strip().startswith("*")]
+
+
+def run(sysm, want_pairs: bool = False, repeats: int = 1, fast: bool = False) -> RefResult:
+    from moldy_gb300.system import write_mdsys
+    exe = os.path.join(REF_DIR, "moldy_ref_harness_fast" if fast else "moldy_ref_harness")
+    n = sysm.nsites
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.mdsys"), os.path.join(td, "out.bin")
+        write_mdsys(fin, sysm, want_pairs)
+        cp = subprocess.run([exe, fin, fout, str(repeats)], capture_output=True, text=True)
+        if cp.returncode != 0:
+            raise RuntimeError(f"reference harness failed ({cp.returncode}): {cp.stdout[-2000:]}{cp.stderr[-2000:]}")
+        raw = open(fout, "rb").read()
+    d = np.frombuffer(raw, dtype="<f8", count=2 * (3 * n + 10))
+    fr = d[:3 * n].reshape(3, n).copy()
+    per = d[3 * n]
+    sr = d[3 * n + 1:3 * n + 10].reshape(3, 3).copy()
+    o = 3 * n + 10
+    fe = d[o:o + 3 * n].reshape(3, n).copy()
+    pee = d[o + 3 * n]
+    se = d[o + 3 * n + 1:o + 3 * n + 10].reshape(3, 3).copy()
+    off = 8 * 2 * (3 * n + 10)
+    npairs = int(np.frombuffer(raw, dtype="<i8", count=1, offset=off)[0])
+    pairs = None
+    if npairs >= 0:
+        pairs = np.frombuffer(raw, dtype="<i4", count=3 * npairs, offset=off + 8).reshape(-1, 3).copy()
+    tf = te = None
+    m = re.search(r"HARNESS_TIMING force_calc (\S+) ewald (\S+)", cp.stdout)
+    if m:
+        tf, te = float(m.group(1)), float(m.group(2))
+    return RefResult(fr, float(per), sr, fe, float(pee), se, pairs, cp.stdout, tf, te)
