@@ -386,3 +386,70 @@ def write_mdsys(path: str, sysm: System, want_pairs: bool = False) -> None:
         f.write(np.ascontiguousarray(sysm.site_charge, dtype="<f8").tobytes())
         f.write(np.ascontiguousarray(sysm.site, dtype="<f8").tobytes())
         f.write(np.ascontiguousarray(sysm.c_of_m, dtype="<f8").tobytes())
+
+
+def read_mdsys(path: str, name: str = "mdsys") -> System:
+    """Inverse of :func:`write_mdsys`."""
+    raw = open(path, "rb").read()
+    if raw[:6] != MDSYS_MAGIC[:6]:
+        raise ValueError(f"{path}: not an MDSYS1 file")
+    off = 8
+    nsites, nmols, nspecies, max_id, ptype, strict, molpbc, _ = struct.unpack_from("<8i", raw, off)
+    off += 32
+    cutoff, subcell, alpha, k_cutoff = struct.unpack_from("<4d", raw, off)
+    off += 32
+    h = np.frombuffer(raw, "<f8", 9, off).reshape(3, 3).copy()
+    off += 72
+    species = []
+    for s in range(nspecies):
+        ns, nm, fw, _ = struct.unpack_from("<4i", raw, off)
+        off += 16
+        ids = np.frombuffer(raw, "<i4", ns, off).copy()
+        off += 4 * ns
+        pf = np.frombuffer(raw, "<f8", 3 * ns, off).reshape(ns, 3).copy()
+        off += 24 * ns
+        species.append(Species(f"s{s}", nm, ids, pf, bool(fw)))
+    potpar = np.frombuffer(raw, "<f8", max_id * max_id * NPOTP, off).reshape(-1, NPOTP).copy()
+    off += 8 * max_id * max_id * NPOTP
+    site_charge = np.frombuffer(raw, "<f8", max_id, off).copy()
+    off += 8 * max_id
+    site = np.frombuffer(raw, "<f8", 3 * nsites, off).reshape(3, nsites).copy()
+    off += 24 * nsites
+    c_of_m = np.frombuffer(raw, "<f8", 3 * nmols, off).reshape(nmols, 3).copy()
+    return System(h=h, species=species, ptype=ptype, potpar=potpar, site_charge=site_charge,
+                  site=site, c_of_m=c_of_m,
+                  control=Control(cutoff=cutoff, alpha=alpha, k_cutoff=k_cutoff, subcell=subcell,
+                                  strict_cutoff=bool(strict), molpbc=bool(molpbc)), name=name)
+
+
+def save_npz(path: str, sysm: System, **extra) -> None:
+    """Store a System (and any extra arrays) in one compressed .npz."""
+    c = sysm.control
+    d = dict(h=sysm.h, ptype=sysm.ptype, potpar=sysm.potpar, site_charge=sysm.site_charge,
+             site=sysm.site, c_of_m=sysm.c_of_m, name=sysm.name,
+             control=np.array([c.cutoff, c.alpha, c.k_cutoff, c.subcell, float(c.strict_cutoff),
+                               float(c.molpbc)]),
+             spec_nmols=np.array([s.nmols for s in sysm.species]),
+             spec_nsites=np.array([s.nsites for s in sysm.species]),
+             spec_fw=np.array([int(s.framework) for s in sysm.species]),
+             spec_ids=np.concatenate([s.site_id for s in sysm.species]),
+             spec_pf=np.concatenate([s.p_f_sites for s in sysm.species]))
+    d.update(extra)
+    np.savez_compressed(path, **d)
+
+
+def load_npz(path: str):
+    """Returns (System, dict of all arrays in the file)."""
+    z = dict(np.load(path, allow_pickle=False))
+    species, o = [], 0
+    for k, (nm, ns, fw) in enumerate(zip(z["spec_nmols"], z["spec_nsites"], z["spec_fw"])):
+        species.append(Species(f"s{k}", int(nm), z["spec_ids"][o:o + ns].astype(np.int32),
+                               z["spec_pf"][o:o + ns], bool(fw)))
+        o += ns
+    c = z["control"]
+    sysm = System(h=z["h"], species=species, ptype=int(z["ptype"]), potpar=z["potpar"],
+                  site_charge=z["site_charge"], site=z["site"], c_of_m=z["c_of_m"],
+                  control=Control(cutoff=float(c[0]), alpha=float(c[1]), k_cutoff=float(c[2]),
+                                  subcell=float(c[3]), strict_cutoff=bool(c[4]), molpbc=bool(c[5])),
+                  name=str(z["name"]))
+    return sysm, z

@@ -48,3 +48,5 @@ $CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_harness.c" -o "$OUT/mol
 $CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_harness.c" -o "$OUT/moldy_ref_harness_fast" \
     -L"$OUT" -lmoldyref_fast -Wl,-rpath,"$OUT" -rdynamic -ldl -lm
 echo "build_ref: built $OUT/moldy_ref_harness and $OUT/moldy_ref_harness_fast"
+$CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_examples.c" -o "$OUT/moldy_ref_examples" \
+    -L"$OUT" -lmoldyref -Wl,-rpath,"$OUT" -ldl -lm
