@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 force path on the large rigid-water workload.
+
+A step is one force evaluation of the configuration: link-cell real-space
+forces (force_calc) plus the reciprocal-space Ewald sum (ewald), i.e. the
+work the reference's time step hands to force_calc/ewald.  Workload: rigid
+4-site TIP4P-like water, 32,768 molecules = 131,072 sites in a 99.34 Å cubic
+box at 1.0 g/cm^3, Ewald alpha 0.3 /Å, cutoff 9 Å, k-cutoff for 1e-5 accuracy
+(69,876 k-vectors); seeded lattice positions and uniform random orientations
+(synthetic: there is no dataset).
+
+Default arm (--impl gb300):
+  value      steps/s of the FP32-mixed form, inputs resident in HBM, per-step
+             CUDA events on the launching stream (L2 flushed between steps);
+  fp64       the same for the plain FP64 GPU form, and their ratio;
+  e2e        steps/s through the C ABI with pinned host buffers: the H2D copy
+             of the site co-ordinates and the D2H copy of forces, energies and
+             stress inside every timed step;
+  roofline   the dominant kernel's algorithmic FLOP/s (reference op counts)
+             against the FP32 FMA peak measured on this GPU;
+  cpu_baseline  the reference algorithm's C restatement (oracle/port),
+             -O2 -ffast-math, on all host cores, on a bounded sample.
+--impl reference: the CPU restatement alone (the reference is serial C with no
+GPU code), on this workload, each step a bounded sample extrapolated to one
+full step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "MD steps/s: FP32-mixed vs FP64 GPU forces at <=1e-5 rel RMS force err"
+WORKLOAD = ("rigid 4-site water (TIP4P-like), 32768 molecules / 131072 sites, cubic box 99.34 A "
+            "at 1.0 g/cm^3, LJ O-O + Ewald alpha=0.3/A, rc=9 A, kc=2.0358/A (1e-5), lazy link cells")
+# Algorithmic work per unit (reference op counts; a sqrt/exp/divide is 1 flop,
+# an FMA 2): k-space per (site, k): lz combination 6 + structure-factor adds 2
+# (src/ewald.c:124-141,528-533) in the structure-factor pass, force 9
+# (src/ewald.c:557-566) in the force pass; real space per evaluated pair:
+# mk_r_sqr 11 + kernel (LJ + erfc) 45 + mk_forces 9 (src/force.c:700-743,
+# src/kernel.c:188-211).
+FLOPS_SFAC_PER_SITE_K = 8
+FLOPS_FORCE_PER_SITE_K = 9
+FLOPS_PAIR_LJ_ERFC = 65
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_workload(seed=7):
+    from moldy_gb300 import system as S
+    return S.water(nside=32, seed=seed, alpha=0.3, cutoff=9.0)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        rows = self.rows
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[3:]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(sysm, threads=None, k_fraction=0.125, fast=True):
+    """The reference algorithm (C restatement, -O2 -ffast-math) on the host:
+    full real-space pass plus a contiguous block of the k-vector list,
+    extrapolated to the whole list.  Returns (seconds per step, details)."""
+    from oracle import port
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r = port.force_calc(sysm, nthreads=threads, fast=fast)
+    t_rs = time.perf_counter() - t0
+    nk_probe = port.ewald(sysm, nthreads=1, k_first=0, k_last=0, fast=fast).info.nkvec
+    k_last = max(threads, int(nk_probe * k_fraction))
+    t0 = time.perf_counter()
+    e = port.ewald(sysm, nthreads=threads, k_first=0, k_last=k_last, fast=fast)
+    t_ew_sample = time.perf_counter() - t0
+    t_setup, t_k = e.info.t_setup, e.info.t_kloop
+    t_ew = t_setup + t_k * (e.info.nkvec / k_last)
+    details = {"t_real_s": t_rs, "t_ewald_sample_s": t_ew_sample, "t_ewald_est_s": t_ew,
+               "k_sample": k_last, "nkvec": e.info.nkvec, "pairs": int(r.info.npairs), "threads": threads}
+    return t_rs + t_ew, details
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sysm = make_workload()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(sysm, threads, k_fraction=0.03)
+    times, det = [], None
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t, det = cpu_baseline(sysm, threads, k_fraction=0.03)
+        times.append(t)
+    wall = time.perf_counter() - t_all
+    sec = sum(times) / len(times)
+    sample = (f"each step: full real-space pass ({det['pairs']} pairs) + k-vectors "
+              f"[0, {det['k_sample']}) of {det['nkvec']}, extrapolated to the full list")
+    line = {"metric": METRIC, "value": 1.0 / sec, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded lattice water, random orientations)",
+            "config": {"workload": WORKLOAD, "parallelism": "host threads"},
+            "impl": "reference",
+            "cpu_baseline": {"value": 1.0 / sec, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": 1.0 / sec, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+def traffic_from_profiles():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return {}
+    return {}
+
+
+def run_gpu(args):
+    import torch
+    from moldy_gb300 import _lib
+    from moldy_gb300.forcefield import ForceField
+    import ctypes as C
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    sysA = make_workload(seed=7)
+    sysB = make_workload(seed=8)          # alternate configurations step to step
+    n = sysA.nsites
+    # a dedicated (non-default) stream: the library launches on it and the
+    # CUDA events below are recorded on it
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ff = ForceField(sysA, precision="mixed", device=local)
+    ff.set_stream(stream.cuda_stream)
+    d_site = [torch.from_numpy(np.ascontiguousarray(s.site)).to(dev) for s in (sysA, sysB)]
+    d_force = torch.empty((3, n), dtype=torch.float64, device=dev)
+    d_pe = torch.zeros(2, dtype=torch.float64, device=dev)
+    d_st = torch.zeros(9, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(i):
+        ff.forces_device(d_site[i % 2].data_ptr(), d_force.data_ptr(), d_pe.data_ptr(), d_st.data_ptr())
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def timed(nsteps, warm):
+        for i in range(warm):
+            step(i)
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(nsteps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(nsteps)]
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(nsteps):
+            flush.zero_()                      # L2 flush between timed steps
+            starts[i].record(stream)
+            step(i)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        wall = time.perf_counter() - t0
+        ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        return sum(ms) / nsteps, wall
+
+    # ---- mixed form: the headline -------------------------------------
+    sampler = ClockSampler(local)
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    launches0 = ff.info()["launches"]
+    sampler.start()
+    time.sleep(0.3)
+    ms_mixed, wall_mixed = timed(args.steps, 0)
+    clocks = sampler.stop()
+    launches_timed = ff.info()["launches"] - launches0
+    ms_t = torch.tensor([ms_mixed], device=dev)
+    if dist is not None:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_mixed = float(ms_t.item())
+    f_mixed = d_force.clone()
+    step(0)
+    torch.cuda.synchronize()
+    f_mixed = d_force.clone()
+    pe_mixed = d_pe.clone()
+
+    # ---- phase timing of one evaluation (CUDA events inside the library) --
+    ff.set_phase_timing(True)
+    phases = None
+    for i in range(3):
+        flush.zero_()
+        step(i)
+        ph = ff.phase_times()
+        phases = ph if phases is None else {k: min(phases[k], ph[k]) for k in ph}
+    ff.set_phase_timing(False)
+
+    # ---- FP64 form ---------------------------------------------------------
+    ff.set_precision("fp64")
+    ms_fp64, _ = timed(max(1, args.fp64_steps), 1)
+    step(0)
+    torch.cuda.synchronize()
+    f64 = d_force.clone()
+    pe64 = d_pe.clone()
+    ferr = float(torch.sqrt(((f_mixed - f64) ** 2).sum() / (f64 ** 2).sum()).item())
+    e_err = float((pe_mixed.sum() - pe64.sum()).abs().item() / pe64.sum().abs().item())
+    ff.set_precision("mixed")
+
+    # ---- end to end through the C ABI, pinned host buffers -------------------
+    h_site = [torch.from_numpy(np.ascontiguousarray(s.site)).pin_memory() for s in (sysA, sysB)]
+    h_force = torch.empty((3, n), dtype=torch.float64).pin_memory()
+    cm = np.ascontiguousarray(sysA.c_of_m)
+    L = _lib.load()
+    hh = np.ascontiguousarray(sysA.h, np.float64).reshape(9)
+    pe_h = np.zeros(2)
+    st_h = np.zeros(9)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    ff.set_stream(0)  # the context's own stream for the host-buffer calls
+
+    def e2e_step(i):
+        st = L.mdgpu_forces(ff.ctx, dp(hh), C.cast(h_site[i % 2].data_ptr(), C.POINTER(C.c_double)),
+                            dp(cm), C.cast(h_force.data_ptr(), C.POINTER(C.c_double)), dp(pe_h), dp(st_h))
+        if st != 0:
+            raise RuntimeError(L.mdgpu_last_error(ff.ctx).decode())
+
+    for i in range(args.warmup):
+        e2e_step(i)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        e2e_step(i)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_t = torch.tensor([e2e_s], device=dev)
+    if dist is not None:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_s = float(e2e_t.item())
+    info = ff.info()
+
+    # ---- roofline of the dominant kernel ---------------------------------------
+    tf32 = C.c_double()
+    tf64 = C.c_double()
+    L.mdgpu_fma_peak(local, 0, C.byref(tf32))
+    L.mdgpu_fma_peak(local, 1, C.byref(tf64))
+    nk = info["nkvec"]
+    work = {"kforce": FLOPS_FORCE_PER_SITE_K * n * nk, "sfac": FLOPS_SFAC_PER_SITE_K * n * nk,
+            "pairs": FLOPS_PAIR_LJ_ERFC * info["npairs"]}
+    dom = max(work, key=lambda k: phases.get(k, 0.0))
+    achieved = work[dom] / (phases[dom] * 1e-3) / 1e12
+    traffic = traffic_from_profiles().get(dom)
+    kernel_names = {"kforce": "k_force32", "sfac": "k_sfac32", "pairs": "k_pairs<LJ,erfc,mixed>"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        log("timing the CPU baseline (reference algorithm restated in C) ...")
+        sec, det = cpu_baseline(sysA)
+        cpu = {"value": 1.0 / sec, "unit": "steps/s", "cores": det["threads"], "kind": "port",
+               "sample": (f"full real-space pass ({det['pairs']} pairs, {det['t_real_s']:.2f} s) + "
+                          f"k-vectors [0,{det['k_sample']}) of {det['nkvec']} "
+                          f"({det['t_ewald_sample_s']:.2f} s), Ewald extrapolated to "
+                          f"{det['t_ewald_est_s']:.2f} s; -O2 -ffast-math, {det['threads']} threads")}
+
+    value = world * 1e3 / ms_mixed
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 accumulation)",
+        "data": "synthetic (seeded lattice water, uniform random orientations)",
+        "config": {"workload": WORKLOAD, "nsites": n, "nkvec": nk, "pairs_per_step": info["npairs"],
+                   "l2": "flushed between timed steps (256 MiB write); per-step CUDA events summed",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": world * 1e3 / ms_fp64, "unit": "steps/s", "ms_per_step": ms_fp64,
+                 "steps": max(1, args.fp64_steps)},
+        "mixed_over_fp64": ms_fp64 / ms_mixed,
+        "accuracy": {"force_rel_rms_mixed_vs_fp64": ferr, "energy_rel_mixed_vs_fp64": e_err},
+        "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 3 * n * 8,
+                "d2h_bytes_per_step": 3 * n * 8 + 11 * 8 + 512},
+        "gpu_launches": int(launches_timed),
+        "phases_ms": phases,
+        "roofline": {"kernel": kernel_names[dom], "bound": "fp32", "achieved": achieved,
+                     "peak": tf32.value, "unit": "TFLOP/s", "frac": achieved / tf32.value,
+                     "traffic": traffic,
+                     "peak_source": "measured FP32 FMA throughput on this GPU (mdgpu_fma_peak), "
+                                    "MEASURED_PEAKS.json carries only HBM and bf16",
+                     "fp64_peak": tf64.value},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "wall_s_mixed_timed": wall_mixed,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ff.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * moldy_gb300.h -- extended C ABI of the GB300 force path (libmoldy_gb300.so).
+ *
+ * The library evaluates Moldy's real-space link-cell forces (force_calc,
+ * src/force.c:1108) and reciprocal-space Ewald forces (ewald,
+ * src/ewald.c:280) with hand-written sm_103a CUDA kernels.  This header is
+ * the status-returning interface: no reference structs, plain pointers and
+ * sizes, every call returns an mdgpu_status.  The drop-in entry points with
+ * the reference's own signatures are declared in moldy_ref_abi.h.
+ *
+ * Units are Moldy's program units (src/defs.h:213-236).  Site arrays are
+ * structure-of-arrays: site[0..2] (or one contiguous [3][nsites] block).
+ * h is the 3x3 cell matrix, row-major (h[i][j] at h[3*i+j]), upper
+ * triangular as ewald() presumes (src/ewald.c:439).
+ */
+#ifndef MOLDY_GB300_H
+#define MOLDY_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mdgpu_ctx mdgpu_ctx;
+
+typedef enum {
+   MDGPU_OK = 0,
+   MDGPU_E_ARG = 1,          /* invalid argument or call order                   */
+   MDGPU_E_CUDA = 2,         /* a CUDA runtime call failed                       */
+   MDGPU_E_UNSUPPORTED = 3,  /* option outside the implemented path (frameworks,
+                                non-upper-triangular h)                          */
+   MDGPU_E_CUTOFF = 4,       /* neighbour cells beyond one image: the reference's
+                                FATAL CUTOFF (src/force.c:203-206)               */
+   MDGPU_E_RANGE = 5,        /* site co-ordinate outside the cell when binning
+                                (src/force.c:126-135)                            */
+   MDGPU_E_PTYPE = 6,        /* unknown potential type (UNKPTY, src/kernel.c:183)*/
+   MDGPU_E_CAPACITY = 7,     /* an output buffer or internal limit is too small  */
+   MDGPU_E_NOMEM = 8         /* device allocation failed                         */
+} mdgpu_status;
+
+typedef enum {
+   MDGPU_FP64 = 0,           /* all arithmetic in FP64                           */
+   MDGPU_MIXED = 1           /* FP32 pair and k-space arithmetic, FP64
+                                accumulation of forces, energies and stress      */
+} mdgpu_precision;
+
+/* One molecular species (the fields of spec_mt the force path reads,
+ * src/structs.h:121-145).  Species are listed in the reference's order. */
+typedef struct {
+   int nsites;                  /* sites per molecule                         */
+   int nmols;                   /* molecules of this species                  */
+   int framework;               /* nonzero: framework species (unsupported)   */
+   const int *site_id;          /* [nsites] site identifiers (1..max_id-1)    */
+   const double *p_f_sites;     /* [nsites][3] principal-frame co-ordinates   */
+} mdgpu_species;
+
+/* Everything about the system that does not change from step to step. */
+typedef struct {
+   int nspecies;
+   const mdgpu_species *species;
+   int max_id;                  /* dimension of the potential table           */
+   int ptype;                   /* potential type, src/kernel.c:61-68 order   */
+   const double *potpar;        /* [max_id*max_id][8], [id_i*max_id + id_j]   */
+   const double *chg;           /* [nsites] site charges (src/accel.c:480-484)*/
+} mdgpu_system;
+
+/* The control-file keys on the path (src/startup.c:143-202). */
+typedef struct {
+   double cutoff;               /* real-space cutoff, Å                       */
+   double subcell;              /* link-cell side, 0 = cutoff/5               */
+   double alpha;                /* Ewald alpha; <= 1e-7 disables k-space      */
+   double k_cutoff;             /* k-space cutoff, Å^-1                       */
+   int strict_cutoff;           /* strict-cutoff keyword                      */
+   int molpbc;                  /* molecular-cutoff keyword                   */
+} mdgpu_control;
+
+/* Counters and constants of the last call (mirrors the reference's notes). */
+typedef struct {
+   int nx, ny, nz;              /* subcells                                   */
+   int n_nabors;                /* half neighbour-cell list (reference prints
+                                   twice this, src/force.c:219-221)           */
+   int nkvec, hmax, kmax, lmax;
+   double eintra;               /* intramolecular correction (program units)  */
+   double self_energy, sheet_energy;
+   int64_t npairs;              /* evaluated site pairs (reference count)     */
+   int64_t n_too_close;         /* pairs closer than 0.5 Å in different mols  */
+   int32_t too_close[16][2];    /* the first of them, canonical orientation   */
+   int64_t launches;            /* kernels launched by this context so far    */
+} mdgpu_info;
+
+/* Phases of one evaluation, for mdgpu_phase_times. */
+enum {
+   MDGPU_PH_CELLS = 0,          /* binning, cell sort, per-slot records       */
+   MDGPU_PH_PAIRS = 1,          /* real-space pair kernel and its reduction   */
+   MDGPU_PH_KPREP = 2,          /* per-site fixed-point phases                */
+   MDGPU_PH_SFAC = 3,           /* structure factor partial sums              */
+   MDGPU_PH_KREDUCE = 4,        /* per-k energy, stress, force coefficients   */
+   MDGPU_PH_KFORCE = 5,         /* reciprocal-space site forces               */
+   MDGPU_PH_FINAL = 6,          /* force partial sums, energy/stress record   */
+   MDGPU_NPHASES = 7
+};
+
+/* Context on one CUDA device.  Not thread-safe: one host thread per context. */
+mdgpu_status mdgpu_create(mdgpu_ctx **ctx, int device, mdgpu_precision precision);
+void mdgpu_destroy(mdgpu_ctx *ctx);
+const char *mdgpu_last_error(const mdgpu_ctx *ctx);
+mdgpu_status mdgpu_set_precision(mdgpu_ctx *ctx, mdgpu_precision precision);
+/* Runs every kernel on `stream` (a cudaStream_t) from now on; NULL restores
+ * the context's own stream. */
+mdgpu_status mdgpu_set_stream(mdgpu_ctx *ctx, void *stream);
+mdgpu_status mdgpu_get_stream(mdgpu_ctx *ctx, void **stream);
+
+/* Describe the system.  Copies what it needs; the first force call after
+ * this recomputes the first-call constants (intramolecular correction,
+ * Ewald self energy), as a fresh reference run would. */
+mdgpu_status mdgpu_set_system(mdgpu_ctx *ctx, const mdgpu_system *sys);
+mdgpu_status mdgpu_set_control(mdgpu_ctx *ctx, const mdgpu_control *ctl);
+
+/* Real-space part with force_calc's semantics (src/force.c:1108-1320): adds
+ * into site_force[3][nsites], *pe and the stress upper triangle.  site and
+ * site_force are host arrays; c_of_m ([nmols][3] fractional) is read only in
+ * molecular-cutoff mode and may be NULL otherwise. */
+mdgpu_status mdgpu_force_calc(mdgpu_ctx *ctx, const double *h, double *const site[3],
+                              double *const site_force[3], const double *c_of_m,
+                              double *pe, double *stress);
+
+/* Reciprocal-space part with ewald's semantics (src/ewald.c:280-589). */
+mdgpu_status mdgpu_ewald(mdgpu_ctx *ctx, const double *h, double *const site[3],
+                         double *const site_force[3], double *pe, double *stress);
+
+/* Both parts in one call on host arrays: site_soa [3][nsites] in, force_out
+ * [3][nsites] overwritten with the total site force, pe_out[2] = real-space
+ * and reciprocal-space energy, stress_out[9] the upper-triangular virial
+ * (lower triangle zero).  c_of_m as for mdgpu_force_calc. */
+mdgpu_status mdgpu_forces(mdgpu_ctx *ctx, const double *h, const double *site_soa,
+                          const double *c_of_m, double *force_out, double *pe_out,
+                          double *stress_out);
+
+/* As mdgpu_forces with every array already in device memory.  Asynchronous
+ * on the context's stream; nothing is copied to or from the host.  Returns
+ * MDGPU_E_RANGE/MDGPU_E_CUTOFF only on the next synchronising call. */
+mdgpu_status mdgpu_forces_device(mdgpu_ctx *ctx, const double *h, const double *d_site_soa,
+                                 const double *d_c_of_m, double *d_force_out,
+                                 double *d_pe_out, double *d_stress_out);
+
+/* Waits for the context's stream and reports device-side errors of earlier
+ * asynchronous calls (binning range, too-close pairs are counted in info). */
+mdgpu_status mdgpu_synchronize(mdgpu_ctx *ctx);
+
+mdgpu_status mdgpu_get_info(mdgpu_ctx *ctx, mdgpu_info *info);
+
+/* Diagnostic phase timing.  While enabled, every evaluation records CUDA
+ * events between its phases on the context's stream; mdgpu_phase_times waits
+ * for the last evaluation and returns the milliseconds of each phase
+ * (MDGPU_NPHASES values; phases that did not run read 0). */
+mdgpu_status mdgpu_set_phase_timing(mdgpu_ctx *ctx, int enable);
+mdgpu_status mdgpu_phase_times(mdgpu_ctx *ctx, double *ms);
+
+/* Diagnostic: the evaluated real-space pair set of the given configuration
+ * as canonical keys (i << 37 | j << 5 | image, i <= j, image as
+ * moldy_gb300/pairset.py), unsorted.  *count receives the number of pairs;
+ * MDGPU_E_CAPACITY if it exceeds cap (keys then holds the first cap). */
+mdgpu_status mdgpu_pair_keys(mdgpu_ctx *ctx, const double *h, const double *site_soa,
+                             const double *c_of_m, uint64_t *keys, int64_t cap,
+                             int64_t *count);
+
+/* Measures the device's dense FMA throughput (TFLOP/s, FMA = 2 flops) in
+ * FP32 (fp64 = 0) or FP64: the roofline denominators of the force kernels,
+ * whose bound is the FMA pipe.  No counterpart in the reference. */
+mdgpu_status mdgpu_fma_peak(int device, int fp64, double *tflops);
+
+/* Potential at one distance (poteval, src/force.c:632-650): reference-site
+ * charge 1, neighbour charge chgsq, Ewald alpha as given. */
+double mdgpu_poteval(const double *potpar, double r, int ptype, double chgsq, double alpha);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

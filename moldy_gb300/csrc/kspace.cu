@@ -1,0 +1,598 @@
+// Reciprocal-space Ewald sum on the GPU (the work of ewald(),
+// src/ewald.c:280-589).
+//
+// Phases.  With s = h^-1 r the fractional co-ordinate of a site, the phase of
+// k-vector (h,k,l) is k.r = 2 pi (h s_x + k s_y + l s_z) (the reference's
+// trig tables, src/ewald.c:148-193, are cos/sin of 2 pi s per axis).  Each
+// site's s is converted once to 64-bit fixed point u = frac(s) 2^64, so the
+// phase of any k-vector, in revolutions, is the exact integer
+// h u_x + k u_y + l u_z mod 2^64.  Work items are runs of up to KI
+// consecutive l values of one (h,k) column of the reference's k-list: each
+// item seeds exp(i k.r) from the exact integer phase and walks l by complex
+// multiplication with exp(2 pi i s_z) -- the reference's addition-formula
+// recurrence, re-seeded exactly every KI k-vectors so its drift stays
+// bounded.  FP64 form: 64-bit phases, sincospi seeds, FP64 recurrence.
+// Mixed form: phases rounded to 32 bits, FP32 seeds and recurrence, FP32
+// partial sums folded into FP64.
+//
+// Passes:
+//   k_prep     per site: fixed-point phases, q, exp(2 pi i s_z);
+//   k_sfac     S(k) = sum_i q_i exp(i k.r_i): one thread per item, the sites
+//              of one chunk streamed through shared memory; partial sums per
+//              (chunk, k) written out (no atomics);
+//   k_kreduce  per k: S(k) over chunks (FP64, fixed order), energy
+//              1/2 coeff |S|^2, stress, and A = coeff Re S, B = coeff Im S
+//              (src/ewald.c:525-553);
+//   k_force    per site: F_i = q_i sum_k k (sin_i A_k - cos_i B_k)
+//              (src/ewald.c:557-566), the k-list split over blockIdx.y,
+//              per-split FP64 partials;
+//   k_fsum     partial forces summed in fixed order into the output.
+#include <cstring>
+
+#include "mdgpu_internal.h"
+
+namespace mdgpu {
+
+__device__ __forceinline__ unsigned long long to_fixed64(double s)
+{
+   // frac(s) * 2^64 for |s| < 2: s * 2^62 is exact in range, rounded to an
+   // integer, then scaled by 4 with wrap-around.
+   long long t = __double2ll_rn(s * 4611686018427387904.0);
+   return (unsigned long long)t << 2;
+}
+
+__device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c);
+__device__ __forceinline__ void sincos_poly(unsigned int p, float *s, float *c);
+
+__global__ void k_prep(int N, const double *__restrict__ site, const double *__restrict__ chg,
+                       double hi0, double hi1, double hi2, double hi3, double hi4, double hi5,
+                       double hi6, double hi7, double hi8, int mixed, int4 *__restrict__ ph32,
+                       float2 *__restrict__ z32, float2 *__restrict__ zp32,
+                       ulonglong2 *__restrict__ ph64a, ulonglong2 *__restrict__ ph64b,
+                       double2 *__restrict__ z64)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= N) return;
+   double x = site[i], y = site[N + i], z = site[2 * N + i];
+   double s0 = hi0 * x + hi1 * y + hi2 * z;
+   double s1 = hi3 * x + hi4 * y + hi5 * z;
+   double s2 = hi6 * x + hi7 * y + hi8 * z;
+   unsigned long long ux = to_fixed64(s0), uy = to_fixed64(s1), uz = to_fixed64(s2);
+   double q = chg[i];
+   double sz, cz;
+   sincospi(2.0 * ((double)(long long)uz * 5.421010862427522e-20), &sz, &cz);   // 2^-64
+   if (mixed) {
+      // round the 64-bit phases to 32 bits
+      unsigned int ux32 = (unsigned int)((ux + 0x80000000ull) >> 32);
+      unsigned int uy32 = (unsigned int)((uy + 0x80000000ull) >> 32);
+      unsigned int uz32 = (unsigned int)((uz + 0x80000000ull) >> 32);
+      ph32[i] = make_int4((int)ux32, (int)uy32, (int)uz32, __float_as_int((float)q));
+      z32[i] = make_float2((float)cz, (float)sz);
+      // exp(2 pi i t s_z), t = 0..KI-1, each from its exact integer phase
+      for (int t = 0; t < KI; t++) {
+         float st, ct;
+         sincos_rev32((unsigned int)t * uz32, &st, &ct);
+         zp32[(size_t)i * KI + t] = make_float2(ct, st);
+      }
+   } else {
+      ph64a[i] = make_ulonglong2(ux, uy);
+      ph64b[i] = make_ulonglong2(uz, (unsigned long long)__double_as_longlong(q));
+      z64[i] = make_double2(cz, sz);
+   }
+}
+
+// exp(2 pi i p / 2^32) for a 32-bit phase p, to about 1 FP32 ulp: the top 24
+// bits go exactly into sincospif, the low 8 bits (< 2^-23 revolution) are
+// added to first order.
+__device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c)
+{
+   float s0, c0;
+   sincospif((float)(int)(p & 0xFFFFFF00u) * 4.656612873077393e-10f, &s0, &c0);   // 2^-31
+   const float d = (float)(p & 0xFFu) * 1.4629180792671596e-09f;                  // 2 pi / 2^32
+   *c = fmaf(-s0, d, c0);
+   *s = fmaf(c0, d, s0);
+}
+
+// exp(2 pi i p / 2^32) by quadrant reduction of the integer phase and
+// polynomials in the reduced phase x in [-1/8, 1/8) revolution:
+// sin(2 pi x) = x P(x^2) (degree 9), cos(2 pi x) = Q(x^2) (degree 8), with
+// coefficients fitted by (weighted) least squares on Chebyshev nodes and
+// rounded to FP32; max abs error about 1e-7 over the interval.
+__device__ __forceinline__ void sincos_poly(unsigned int p, float *s, float *c)
+{
+   const unsigned int qd = (p + 0x20000000u) >> 30;
+   const int r = (int)(p - (qd << 30));
+   const float x = (float)r * 2.3283064365386963e-10f;   // 2^-32
+   const float x2 = x * x;
+   float ps = fmaf(fmaf(fmaf(fmaf(41.46983337402344f, x2, -76.69776916503906f), x2, 81.6052017211914f),
+                        x2, -41.34170150756836f), x2, 6.2831854820251465f);
+   float sn = ps * x;
+   float cs = fmaf(fmaf(fmaf(fmaf(59.22028732299805f, x2, -85.4428482055664f), x2, 64.93931579589844f),
+                        x2, -19.739208221435547f), x2, 1.0f);
+   if (qd & 1u) {
+      const float t = sn;
+      sn = cs;
+      cs = -t;
+   }
+   if (qd & 2u) {
+      sn = -sn;
+      cs = -cs;
+   }
+   *s = sn;
+   *c = cs;
+}
+
+// ---------------------------------------------------------------- S(k)
+constexpr int SF_TILE = 128;
+
+// Each site's k-vectors of one item are seed * zp[t] with zp[t] =
+// exp(2 pi i t s_z) from the per-site table (k_prep): every term is at most
+// two roundings from its exact phase, so no error accumulates along l.  The
+// structure factor of a crystal is a near-cancelling sum, and its force
+// error grows with the per-site phase error.
+__global__ void __launch_bounds__(128)
+k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nitems,
+         const int4 *__restrict__ ph, const float2 *__restrict__ zp, int N, int chunk, int nk,
+         float2 *__restrict__ part)
+{
+   __shared__ int4 sph[SF_TILE];
+   __shared__ float2 szp[SF_TILE * KI];
+   const int it = blockIdx.x * blockDim.x + threadIdx.x;
+   const int4 hd = it < nitems ? item[it] : make_int4(0, 0, 0, 0);
+   const int s0 = blockIdx.y * chunk, s1 = min(N, s0 + chunk);
+   float ac[KI], as[KI];
+#pragma unroll
+   for (int t = 0; t < KI; t++) ac[t] = as[t] = 0.f;
+   const unsigned int H = (unsigned int)hd.x, K = (unsigned int)hd.y, L = (unsigned int)hd.z;
+   for (int tb = s0; tb < s1; tb += SF_TILE) {
+      const int nt = min(SF_TILE, s1 - tb);
+      __syncthreads();
+      for (int q = threadIdx.x; q < nt; q += blockDim.x) sph[q] = ph[tb + q];
+      for (int q = threadIdx.x; q < nt * KI; q += blockDim.x) szp[q] = zp[(size_t)tb * KI + q];
+      __syncthreads();
+      for (int q = 0; q < nt; q++) {
+         const int4 v = sph[q];
+         const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
+         float sn, cs;
+         sincos_poly(p, &sn, &cs);
+         const float qv = __int_as_float(v.w);
+         cs *= qv;
+         sn *= qv;
+         const float2 *z = szp + q * KI;
+#pragma unroll
+         for (int t = 0; t < KI; t++) {
+            if (t < hd.w) {
+               const float2 zt = z[t];
+               ac[t] = fmaf(cs, zt.x, fmaf(-sn, zt.y, ac[t]));
+               as[t] = fmaf(sn, zt.x, fmaf(cs, zt.y, as[t]));
+            }
+         }
+      }
+   }
+   if (it < nitems) {
+      const int k0 = item_k0[it];
+      float2 *dst = part + (size_t)blockIdx.y * nk + k0;
+#pragma unroll
+      for (int t = 0; t < KI; t++)
+         if (t < hd.w) dst[t] = make_float2(ac[t], as[t]);
+   }
+}
+
+__global__ void __launch_bounds__(128)
+k_sfac64(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nitems,
+         const ulonglong2 *__restrict__ pha, const ulonglong2 *__restrict__ phb,
+         const double2 *__restrict__ zz, int N, int chunk, int nk, double2 *__restrict__ part)
+{
+   __shared__ ulonglong2 sa[SF_TILE / 2], sb[SF_TILE / 2];
+   __shared__ double2 sz[SF_TILE / 2];
+   const int it = blockIdx.x * blockDim.x + threadIdx.x;
+   const int4 hd = it < nitems ? item[it] : make_int4(0, 0, 0, 0);
+   const int s0 = blockIdx.y * chunk, s1 = min(N, s0 + chunk);
+   double ac[KI], as[KI];
+#pragma unroll
+   for (int t = 0; t < KI; t++) ac[t] = as[t] = 0.0;
+   const unsigned long long H = (unsigned long long)(long long)hd.x,
+                            K = (unsigned long long)(long long)hd.y,
+                            L = (unsigned long long)(long long)hd.z;
+   for (int tb = s0; tb < s1; tb += SF_TILE / 2) {
+      const int nt = min(SF_TILE / 2, s1 - tb);
+      for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+         sa[q] = pha[tb + q];
+         sb[q] = phb[tb + q];
+         sz[q] = zz[tb + q];
+      }
+      __syncthreads();
+      for (int q = 0; q < nt; q++) {
+         const ulonglong2 a = sa[q], b = sb[q];
+         const double2 z = sz[q];
+         const unsigned long long p = H * a.x + K * a.y + L * b.x;
+         double sn, cs;
+         sincospi(2.0 * ((double)(long long)p * 5.421010862427522e-20), &sn, &cs);
+         const double qv = __longlong_as_double((long long)b.y);
+         cs *= qv;
+         sn *= qv;
+#pragma unroll
+         for (int t = 0; t < KI; t++) {
+            if (t < hd.w) {
+               ac[t] += cs;
+               as[t] += sn;
+            }
+            const double nc = cs * z.x - sn * z.y;
+            sn = sn * z.x + cs * z.y;
+            cs = nc;
+         }
+      }
+      __syncthreads();
+   }
+   if (it < nitems) {
+      const int k0 = item_k0[it];
+      double2 *dst = part + (size_t)blockIdx.y * nk + k0;
+#pragma unroll
+      for (int t = 0; t < KI; t++)
+         if (t < hd.w) dst[t] = make_double2(ac[t], as[t]);
+   }
+}
+
+// ------------------------------------------------- per-k energy and stress
+__device__ __forceinline__ double bsum(double v, double *sh)
+{
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+   __syncthreads();
+   if (lane == 0) sh[w] = v;
+   __syncthreads();
+   double s = 0.0;
+   if (threadIdx.x == 0)
+      for (int i = 0; i < nw; i++) s += sh[i];
+   return s;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256)
+k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__restrict__ p64,
+          const double *__restrict__ kvec /*[3][nk]*/, const double *__restrict__ coeff,
+          const double *__restrict__ coeff2, float4 *__restrict__ kd32, double4 *__restrict__ kd64,
+          double *__restrict__ blk)
+{
+   __shared__ double red[32];
+   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+   double pek = 0, st[6] = {0, 0, 0, 0, 0, 0};
+   if (k < nk) {
+      double C = 0.0, S = 0.0;
+      for (int c = 0; c < nchunks; c++) {
+         if (MIXED) {
+            const float2 v = p32[(size_t)c * nk + k];
+            C += (double)v.x;
+            S += (double)v.y;
+         } else {
+            const double2 v = p64[(size_t)c * nk + k];
+            C += v.x;
+            S += v.y;
+         }
+      }
+      const double kx = kvec[k], ky = kvec[nk + k], kz = kvec[2 * nk + k];
+      const double cf = coeff[k], cf2 = coeff2[k];
+      pek = 0.5 * cf * (C * C + S * S);
+      st[0] = pek - pek * cf2 * kx * kx;
+      st[1] = -(pek * cf2 * kx * ky);
+      st[2] = -(pek * cf2 * kx * kz);
+      st[3] = pek - pek * cf2 * ky * ky;
+      st[4] = -(pek * cf2 * ky * kz);
+      st[5] = pek - pek * cf2 * kz * kz;
+      const double A = cf * C, B = cf * S;
+      if (MIXED)
+         kd32[k] = make_float4((float)A, (float)B, (float)kz, 0.f);
+      else
+         kd64[k] = make_double4(A, B, kz, 0.0);
+   }
+   double s = bsum(pek, red);
+   if (threadIdx.x == 0) blk[blockIdx.x * 8] = s;
+   for (int i = 0; i < 6; i++) {
+      s = bsum(st[i], red);
+      if (threadIdx.x == 0) blk[blockIdx.x * 8 + 1 + i] = s;
+   }
+}
+
+__global__ void k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *out)
+{
+   int k = threadIdx.x;
+   if (k >= 7) return;
+   double s = 0.0;
+   for (int b = 0; b < nblocks; b++) s += blk[b * 8 + k];
+   if (k == 0) out->pe_k = s; else out->st_k[k - 1] = s;
+}
+
+// ---------------------------------------------------------------- forces
+constexpr int FT_ITEMS = 64;
+
+__global__ void __launch_bounds__(256)
+k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
+          const float2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
+          const float4 *__restrict__ kd, const int4 *__restrict__ ph, const float2 *__restrict__ zz,
+          const double *__restrict__ chg, int N, double *__restrict__ fpart)
+{
+   __shared__ int4 s_it[FT_ITEMS];
+   __shared__ float2 s_kxy[FT_ITEMS];
+   __shared__ int s_k0[FT_ITEMS];
+   __shared__ float4 s_kd[FT_ITEMS * KI];
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const bool live = i < N;
+   const int4 v = live ? ph[i] : make_int4(0, 0, 0, 0);
+   (void)zz;
+   // exp(2 pi i t s_z), t = 0..KI-1, each from its exact integer phase: the
+   // k-vectors of an item are seed * zp[t], so per-site phase errors do not
+   // accumulate along l (the force multiplies them by |S(k)|, which is of
+   // order N q at the Bragg peaks of a crystal).
+   float zc[KI], zs[KI];
+#pragma unroll
+   for (int t = 0; t < KI; t++) {
+      const float2 zt = zz[(size_t)i * KI + t];
+      zc[t] = live ? zt.x : 1.f;
+      zs[t] = live ? zt.y : 0.f;
+   }
+   const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
+   float fx = 0.f, fy = 0.f, fz = 0.f;
+   double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+   int nfold = 0;
+   for (int tb = a; tb < b; tb += FT_ITEMS) {
+      const int nt = min(FT_ITEMS, b - tb);
+      const int kb = item_k0[tb];
+      const int ke = (tb + nt < nitems) ? item_k0[tb + nt] : nk;
+      __syncthreads();
+      for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+         s_it[q] = item[tb + q];
+         s_kxy[q] = item_kxy[tb + q];
+         s_k0[q] = item_k0[tb + q] - kb;
+      }
+      for (int q = threadIdx.x; q < ke - kb; q += blockDim.x) s_kd[q] = kd[kb + q];
+      __syncthreads();
+      for (int q = 0; q < nt; q++) {
+         const int4 hd = s_it[q];
+         const unsigned int p = (unsigned int)hd.x * (unsigned int)v.x +
+                                (unsigned int)hd.y * (unsigned int)v.y +
+                                (unsigned int)hd.z * (unsigned int)v.z;
+         float s0, c0;
+         sincos_poly(p, &s0, &c0);
+         float sf = 0.f, skz = 0.f;
+         const float4 *kq = s_kd + s_k0[q];
+#pragma unroll
+         for (int t = 0; t < KI; t++) {
+            if (t < hd.w) {
+               const float4 k4 = kq[t];
+               const float cs = c0 * zc[t] - s0 * zs[t];
+               const float sn = fmaf(s0, zc[t], c0 * zs[t]);
+               const float f = fmaf(sn, k4.x, -cs * k4.y);
+               sf += f;
+               skz = fmaf(k4.z, f, skz);
+            }
+         }
+         const float2 kxy = s_kxy[q];
+         fx = fmaf(kxy.x, sf, fx);
+         fy = fmaf(kxy.y, sf, fy);
+         fz += skz;
+         if (++nfold == 32) {
+            Fx += fx; Fy += fy; Fz += fz;
+            fx = fy = fz = 0.f;
+            nfold = 0;
+         }
+      }
+   }
+   if (live) {
+      Fx += fx; Fy += fy; Fz += fz;
+      const double q = chg[i];
+      double *dst = fpart + (size_t)blockIdx.y * 3 * N;
+      dst[i] = q * Fx;
+      dst[N + i] = q * Fy;
+      dst[2 * N + i] = q * Fz;
+   }
+}
+
+__global__ void __launch_bounds__(256)
+k_force64(const int4 *__restrict__ item, const int *__restrict__ item_k0,
+          const double2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
+          const double4 *__restrict__ kd, const ulonglong2 *__restrict__ pha,
+          const ulonglong2 *__restrict__ phb, const double2 *__restrict__ zz,
+          const double *__restrict__ chg, int N, double *__restrict__ fpart)
+{
+   __shared__ int4 s_it[FT_ITEMS];
+   __shared__ double2 s_kxy[FT_ITEMS];
+   __shared__ int s_k0[FT_ITEMS];
+   __shared__ double4 s_kd[FT_ITEMS * KI];
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const bool live = i < N;
+   const ulonglong2 ua = live ? pha[i] : make_ulonglong2(0, 0);
+   const ulonglong2 ub = live ? phb[i] : make_ulonglong2(0, 0);
+   const double2 z = live ? zz[i] : make_double2(1.0, 0.0);
+   const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
+   double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+   for (int tb = a; tb < b; tb += FT_ITEMS) {
+      const int nt = min(FT_ITEMS, b - tb);
+      const int kb = item_k0[tb];
+      const int ke = (tb + nt < nitems) ? item_k0[tb + nt] : nk;
+      __syncthreads();
+      for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+         s_it[q] = item[tb + q];
+         s_kxy[q] = item_kxy[tb + q];
+         s_k0[q] = item_k0[tb + q] - kb;
+      }
+      for (int q = threadIdx.x; q < ke - kb; q += blockDim.x) s_kd[q] = kd[kb + q];
+      __syncthreads();
+      for (int q = 0; q < nt; q++) {
+         const int4 hd = s_it[q];
+         const unsigned long long p = (unsigned long long)(long long)hd.x * ua.x +
+                                      (unsigned long long)(long long)hd.y * ua.y +
+                                      (unsigned long long)(long long)hd.z * ub.x;
+         double sn, cs;
+         sincospi(2.0 * ((double)(long long)p * 5.421010862427522e-20), &sn, &cs);
+         double sf = 0.0, skz = 0.0;
+         const double4 *kq = s_kd + s_k0[q];
+         for (int t = 0; t < hd.w; t++) {
+            const double4 k4 = kq[t];
+            const double f = sn * k4.x - cs * k4.y;
+            sf += f;
+            skz += k4.z * f;
+            const double nc = cs * z.x - sn * z.y;
+            sn = sn * z.x + cs * z.y;
+            cs = nc;
+         }
+         const double2 kxy = s_kxy[q];
+         Fx += kxy.x * sf;
+         Fy += kxy.y * sf;
+         Fz += skz;
+      }
+   }
+   if (live) {
+      const double q = chg[i];
+      double *dst = fpart + (size_t)blockIdx.y * 3 * N;
+      dst[i] = q * Fx;
+      dst[N + i] = q * Fy;
+      dst[2 * N + i] = q * Fz;
+   }
+}
+
+__global__ void k_fsum(int n3, int nsplit, const double *__restrict__ fpart, double *__restrict__ force,
+                       int accumulate)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n3) return;
+   double s = 0.0;
+   for (int k = 0; k < nsplit; k++) s += fpart[(size_t)k * n3 + i];
+   force[i] = accumulate ? force[i] + s : s;
+}
+
+// -------------------------------------------------------------- host side
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+
+mdgpu_status ks_prepare(mdgpu_ctx *c)
+{
+   KsDev &d = c->kd;
+   const KList &kl = c->kl;
+   cudaStream_t st = c->stream;
+   const int N = c->nsites;
+   if (!c->kl_uploaded) {
+      const int nk = kl.nk, ni = kl.nitems;
+      CK(d.item.ensure(ni));
+      CK(d.item_k0.ensure(ni + 1));
+      CK(d.item_kxy64.ensure(ni));
+      CK(d.item_kxy32.ensure(ni));
+      CK(d.kz64.ensure(3 * (size_t)nk));
+      CK(d.coeff.ensure(nk));
+      CK(d.coeff2.ensure(nk));
+      CK(d.kdat32.ensure(nk));
+      CK(d.kdat64.ensure(nk));
+      std::vector<float2> kxy32(ni);
+      for (int i = 0; i < ni; i++) kxy32[i] = make_float2((float)kl.item_kxy[i].x, (float)kl.item_kxy[i].y);
+      std::vector<double> kv(3 * (size_t)nk);
+      for (int i = 0; i < ni; i++)
+         for (int t = 0; t < kl.item[i].w; t++) {
+            int k = kl.item_k0[i] + t;
+            kv[k] = kl.item_kxy[i].x;
+            kv[nk + k] = kl.item_kxy[i].y;
+            kv[2 * (size_t)nk + k] = kl.kz[k];
+         }
+      CK(cudaMemcpyAsync(d.item.p, kl.item.data(), ni * sizeof(int4), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.item_k0.p, kl.item_k0.data(), ni * sizeof(int), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.item_kxy64.p, kl.item_kxy.data(), ni * sizeof(double2), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.item_kxy32.p, kxy32.data(), ni * sizeof(float2), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.kz64.p, kv.data(), kv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.coeff.p, kl.coeff.data(), nk * sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.coeff2.p, kl.coeff2.data(), nk * sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+      c->kl_uploaded = true;
+   }
+   CK(d.ph32.ensure(N));
+   CK(d.z32.ensure(N));
+   CK(d.zp32.ensure((size_t)N * KI));
+   CK(d.ph64a.ensure(N));
+   CK(d.ph64b.ensure(N));
+   CK(d.z64.ensure(N));
+   return MDGPU_OK;
+}
+
+struct KsShape {
+   int chunks, chunk, splits, per_split;
+};
+
+static KsShape ks_shape(int N, int nitems)
+{
+   KsShape s;
+   const long long target = 152LL * 2048;          // resident threads on a full GB300
+   long long ch = target / (nitems > 0 ? nitems : 1);
+   long long max_ch = (N + 63) / 64;
+   if (ch < 1) ch = 1;
+   if (ch > max_ch) ch = max_ch;
+   s.chunk = (int)(((N + ch - 1) / ch + 31) / 32 * 32);
+   s.chunks = (N + s.chunk - 1) / s.chunk;
+   long long sp = (2 * target) / (N > 0 ? N : 1);
+   long long max_sp = (nitems + 7) / 8;
+   if (sp < 1) sp = 1;
+   if (sp > max_sp) sp = max_sp;
+   if (sp < 1) sp = 1;
+   s.per_split = (int)((nitems + sp - 1) / sp);
+   s.splits = (nitems + s.per_split - 1) / s.per_split;
+   if (s.splits < 1) s.splits = 1;
+   return s;
+}
+
+mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate)
+{
+   KsDev &d = c->kd;
+   const KList &kl = c->kl;
+   cudaStream_t st = c->stream;
+   const int N = c->nsites, nk = kl.nk, ni = kl.nitems;
+   const bool mixed = c->prec == MDGPU_MIXED;
+   DevOut *out = c->out.p;
+   if (nk == 0) {
+      if (!accumulate) CK(cudaMemsetAsync(d_force, 0, 3 * (size_t)N * sizeof(double), st));
+      return MDGPU_OK;
+   }
+   double hinv[9];
+   memcpy(hinv, kl.hinv, sizeof hinv);
+   phase_mark(c, MDGPU_PH_KPREP);
+   k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, d_site, c->rd.chg.p, hinv[0], hinv[1], hinv[2], hinv[3],
+                                           hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], mixed ? 1 : 0,
+                                           d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
+   CK(cudaGetLastError());
+   KsShape sh = ks_shape(N, ni);
+   phase_mark(c, MDGPU_PH_SFAC);
+   if (mixed) {
+      CK(d.part32.ensure((size_t)sh.chunks * nk));
+      dim3 g((ni + 127) / 128, sh.chunks);
+      k_sfac32<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, N, sh.chunk, nk, d.part32.p);
+   } else {
+      CK(d.part64.ensure((size_t)sh.chunks * nk));
+      dim3 g((ni + 127) / 128, sh.chunks);
+      k_sfac64<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, d.ph64b.p, d.z64.p, N, sh.chunk,
+                                  nk, d.part64.p);
+   }
+   CK(cudaGetLastError());
+   const int nbk = (nk + 255) / 256;
+   CK(d.blk.ensure((size_t)nbk * 8));
+   phase_mark(c, MDGPU_PH_KREDUCE);
+   if (mixed)
+      k_kreduce<true><<<nbk, 256, 0, st>>>(nk, sh.chunks, d.part32.p, nullptr, d.kz64.p, d.coeff.p,
+                                           d.coeff2.p, d.kdat32.p, nullptr, d.blk.p);
+   else
+      k_kreduce<false><<<nbk, 256, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
+                                            d.coeff2.p, nullptr, d.kdat64.p, d.blk.p);
+   k_kfinal<<<1, 32, 0, st>>>(d.blk.p, nbk, out);
+   CK(cudaGetLastError());
+   CK(d.fpart.ensure((size_t)sh.splits * 3 * N));
+   phase_mark(c, MDGPU_PH_KFORCE);
+   dim3 gf((N + 255) / 256, sh.splits);
+   if (mixed)
+      k_force32<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
+                                    d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, N, d.fpart.p);
+   else
+      k_force64<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, sh.per_split,
+                                    d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, N, d.fpart.p);
+   CK(cudaGetLastError());
+   phase_mark(c, MDGPU_PH_FINAL);
+   k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, sh.splits, d.fpart.p, d_force, accumulate ? 1 : 0);
+   CK(cudaGetLastError());
+   c->launches += 6;
+   return MDGPU_OK;
+}
+
+}  // namespace mdgpu

@@ -1,0 +1,206 @@
+// Internal declarations of libmoldy_gb300: the context, the host-side
+// geometry (link-cell stencil, k-vector list) and the launch functions of
+// the real-space (realspace.cu) and reciprocal-space (kspace.cu) kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/moldy_gb300.h"
+
+namespace mdgpu {
+
+constexpr int NPOTP = 8;          // parameters per potential (src/defs.h:144)
+constexpr int KI = 16;            // k-vectors per k-space work item
+constexpr double PI = 3.14159265358979323846;
+constexpr double ALPHAMIN = 1e-7; // src/defs.h:181
+constexpr double TOO_CLOSE = 0.25;// r^2 warning threshold, src/force.c:89
+constexpr int MAX_TOO_CLOSE_REC = 16;
+
+// ---- host-side geometry of one real-space call -------------------------
+struct RsGeom {
+   int nx = 0, ny = 0, nz = 0, ncells = 0;
+   int n_half = 0;                 // half-space stencil (reference list)
+   std::vector<int> half;          // 3 ints per offset, reference order
+   std::vector<int4> full;         // (dx,dy,dz,is_zero) both half-spaces
+   std::vector<float4> off_hi, off_lo;  // h.(d/n) as float hi + lo parts
+   double h[9];
+   double hinv[9];                 // src/matrix.c invert() of h
+   double reloc[27][3];            // image translations, src/force.c:1282-1293
+   double origin_step[9];          // h / n (column j scaled by 1/n_j)
+   double cut2 = 0, cut100 = 0;
+   double key[12];                 // h, cutoff, subcell, strict: cache key
+};
+
+// Builds the stencil and cell geometry; returns MDGPU_E_CUTOFF as the
+// reference's FATAL CUTOFF would fire.
+mdgpu_status build_rs_geom(const double *h, const mdgpu_control &ctl, RsGeom &g);
+
+// ---- host-side k-vector list ---------------------------------------------
+struct KList {
+   int hmax = 0, kmax = 0, lmax = 0, nk = 0, nitems = 0;
+   std::vector<int4> item;         // (h, k, l0, count)
+   std::vector<int> item_k0;       // index of the item's first k-vector
+   std::vector<double2> item_kxy;  // (kx, ky) of the item's (h,k) column
+   std::vector<double> kz;         // per k-vector
+   std::vector<double> coeff, coeff2;  // src/ewald.c:510-511
+   double key[12];                 // h, k_cutoff, alpha
+   double vol = 0;
+   double hinv[9];
+};
+
+mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl);
+
+// ---- first-call constants (host, FP64, reference arithmetic) -------------
+double host_poteval(const double *potpar, double r, int ptype, double chgsq, double alpha);
+double intramolecular_energy(const std::vector<mdgpu_species> &spec,
+                             const std::vector<int> &spec_ids, const std::vector<double> &spec_pf,
+                             const double *potpar, int max_id, int ptype,
+                             const std::vector<double> &chg, double alpha);
+void ewald_self_sheet(const std::vector<mdgpu_species> &spec, const std::vector<double> &spec_pf,
+                      const std::vector<double> &chg, double alpha, double *self,
+                      double *sheet, int *nsitesxf);
+double det3(const double *a);
+void inv3(const double *a, double *b);
+
+// ---- device buffers ----------------------------------------------------------
+template <typename T>
+struct DBuf {
+   T *p = nullptr;
+   size_t n = 0;
+   cudaError_t ensure(size_t want) {
+      if (want <= n && p) return cudaSuccess;
+      if (p) cudaFree(p);
+      p = nullptr;
+      n = 0;
+      cudaError_t e = cudaMalloc(&p, (want ? want : 1) * sizeof(T));
+      if (e == cudaSuccess) n = want;
+      return e;
+   }
+   void release() {
+      if (p) cudaFree(p);
+      p = nullptr;
+      n = 0;
+   }
+};
+
+// Device-resident outputs of one evaluation (all FP64).
+struct DevOut {
+   double pe_rs;          // sum of pair energies (before eintra)
+   double vir_rs[6];      // xx xy xz yy yz zz
+   double pe_k;           // sum of k-space energies (before self/sheet)
+   double st_k[6];
+   double vir_in[6];      // sum x_i (x) f_in_i, reference-semantics calls only
+   int err;               // bit 0: co-ordinate out of range
+   int n_too_close;
+   int64_t npairs2;       // full-list pair evaluations (2x reference count)
+   int too_close[MAX_TOO_CLOSE_REC][2];
+};
+
+struct RsDev {
+   DBuf<int> cell_of, cell_count, cell_start, slot_cell, sorted, blocksum;
+   DBuf<double4> pos64;    // sorted: x, y, z, q
+   DBuf<float4> pos32;     // sorted: x - cell origin (x, y, z), q
+   DBuf<int2> tag;         // sorted: site id, molecule
+   DBuf<int> molmap, siteid, ent_mol;
+   DBuf<double> chg, cofm;
+   DBuf<int4> full;
+   DBuf<float4> off_hi, off_lo;
+   DBuf<double> pot64;
+   DBuf<float> pot32;
+   DBuf<double> part;      // per-block partial energies/virials
+   DBuf<unsigned long long> keys;
+};
+
+struct KsDev {
+   DBuf<int4> item;
+   DBuf<int> item_k0;
+   DBuf<double2> item_kxy64;
+   DBuf<float2> item_kxy32;
+   DBuf<double> kz64, coeff, coeff2;
+   DBuf<float4> kdat32;    // per k: (A_k, B_k, kz, 0)
+   DBuf<double4> kdat64;
+   DBuf<int4> ph32;        // per site: fixed-point phases (32-bit) + q bits
+   DBuf<float2> z32;       // per site: exp(2 pi i s_z)
+   DBuf<float2> zp32;      // per site: exp(2 pi i t s_z), t = 0..KI-1
+   DBuf<ulonglong2> ph64a; // per site: (ux, uy) 64-bit phases
+   DBuf<ulonglong2> ph64b; // per site: (uz, q bits)
+   DBuf<double2> z64;
+   DBuf<float2> part32;    // [chunks][nk] structure-factor partials
+   DBuf<double2> part64;
+   DBuf<double> fpart;     // [splits][3][N] force partials
+   DBuf<double> blk;       // per-block energy/stress partials
+};
+
+}  // namespace mdgpu
+
+struct mdgpu_ctx {
+   int device = 0;
+   cudaStream_t own_stream = nullptr, stream = nullptr;
+   mdgpu_precision prec = MDGPU_MIXED;
+   std::string err;
+
+   // system
+   bool have_system = false, have_control = false;
+   int nsites = 0, nmols = 0, max_id = 0, ptype = 0;
+   std::vector<mdgpu_species> spec;
+   std::vector<int> spec_ids;       // concatenated per-species site ids
+   std::vector<double> spec_pf;     // concatenated principal-frame sites
+   std::vector<int> site_id, molmap, mol_first, mol_nsites;
+   std::vector<double> chg, potpar;
+   mdgpu_control ctl{};
+   bool sys_dirty = true;           // device copies out of date
+
+   // first-call constants (recomputed after set_system)
+   bool have_eintra = false, have_self = false;
+   double eintra = 0, self_energy = 0, sheet_energy = 0;
+   int nsitesxf = 0;
+
+   // cached geometry
+   mdgpu::RsGeom rs;
+   bool rs_valid = false, rs_uploaded = false;
+   mdgpu::KList kl;
+   bool kl_valid = false, kl_uploaded = false;
+
+   mdgpu::RsDev rd;
+   mdgpu::KsDev kd;
+   mdgpu::DBuf<double> site, force, force_in, cofm_in, small;
+   const double *cur_site = nullptr;   // site array of the launch in progress
+   mdgpu::DBuf<mdgpu::DevOut> out;
+   mdgpu::DevOut *h_out = nullptr;  // pinned mirror
+   double *h_stage = nullptr;       // pinned staging for 6*nsites doubles
+   size_t h_stage_n = 0;
+
+   mdgpu_info info{};
+   int64_t launches = 0;
+   bool timing = false;
+   cudaEvent_t ev[MDGPU_NPHASES + 1] = {};
+   bool ev_marked[MDGPU_NPHASES + 1] = {};
+   bool have_nabor_note = false;
+   int note_nx = 0, note_ny = 0, note_nz = 0, note_nabors = 0;
+};
+
+namespace mdgpu {
+// realspace.cu
+mdgpu_status rs_prepare(mdgpu_ctx *c);   // upload geometry/system tables
+mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
+                       double *d_force, bool accumulate, unsigned long long *d_keys,
+                       int64_t key_cap, int64_t *d_keycount);
+// kspace.cu
+mdgpu_status ks_prepare(mdgpu_ctx *c);
+mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate);
+// api.cu
+mdgpu_status fail(mdgpu_ctx *c, mdgpu_status s, const std::string &msg);
+mdgpu_status cuda_check(mdgpu_ctx *c, cudaError_t e, const char *what);
+
+// Marks the boundary before phase `i` (MDGPU_NPHASES marks the end).
+inline void phase_mark(mdgpu_ctx *c, int i)
+{
+   if (!c->timing) return;
+   if (!c->ev[i]) cudaEventCreate(&c->ev[i]);
+   cudaEventRecord(c->ev[i], c->stream);
+   c->ev_marked[i] = true;
+}
+}  // namespace mdgpu

@@ -1,0 +1,690 @@
+// Real-space link-cell forces on the GPU (the work of force_calc,
+// src/force.c:1108-1320, and kernel(), src/kernel.c:157-463).
+//
+// Pipeline, all on one stream:
+//   1. k_bin        FP64 binning of every site (or molecule centre of mass in
+//                   molecular-cutoff mode) with the reference's arithmetic and
+//                   edge fix-ups (cellbin, src/force.c:119-137);
+//   2. scan         cell counts -> cell starts (3-kernel block scan);
+//   3. k_scatter +  sites placed cell by cell, then each cell's members put
+//      k_cellsort   in ascending site order (deterministic layout);
+//   4. k_gather     per-slot records: FP64 (x,y,z,q), or FP32 co-ordinates
+//                   relative to the cell origin plus q, and (site id, molecule);
+//   5. k_pairs      one thread per site walks the full neighbour-cell stencil
+//                   (the reference's half-space list and its mirror) and
+//                   evaluates every candidate pair the reference evaluates,
+//                   accumulating the force on its own site only; energy and
+//                   virial take half of each evaluation.  No atomics on forces.
+//   6. k_reduce_rs  per-block energy/virial partials summed in fixed order.
+//
+// The pair set is the reference's exactly: every site pair of a cell and of
+// each stencil cell, with no per-pair cutoff in lazy mode and r^2 clamped to
+// 1e4 rc^2 in strict mode (src/force.c:951-954).  In FP64 form r and r^2 are
+// formed with the reference's operation order and no fused multiply-adds, so
+// the clamp and the too-close test decide exactly as the reference does.  In
+// mixed form r is formed in FP32 from cell-relative co-ordinates and an
+// (hi, lo) pair of the exact cell-offset vector; decisions within a narrow
+// band of the threshold are re-made in FP64 from the original co-ordinates.
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+
+#include "mdgpu_internal.h"
+
+namespace mdgpu {
+
+struct RsParams {
+   int nsites, nent, nx, ny, nz, ncells, nfull, max_id, molpbc, strict, ptype, pot_in_smem;
+   double hinv[9];
+   double h[9];
+   double reloc[27][3];
+   double cut2, cut100, alpha, norm;
+   float cut2f, bandf, alphaf, normf;
+};
+
+// ---------------------------------------------------------------- binning
+__device__ __forceinline__ int cellbin_dev(double s, int n, double fn, int *bad)
+{
+   const double eps = 8.0 * 2.220446049250313e-16;   // 8 * precision(), force.c:437
+   if (s < -0.5 + eps || s >= 0.5 - eps) {
+      if (s < -0.5 + eps && s >= -0.5 - eps)
+         s = -0.5;
+      else if (s >= 0.5 - eps && s <= 0.5 + eps)
+         s = 0.5 - eps;
+      else
+         *bad = 1;
+   }
+   int ib = (int)floor(__dmul_rn(__dadd_rn(s, 0.5), fn));
+   if (ib >= n || ib < 0) {
+      *bad = 1;
+      ib = ib < 0 ? 0 : n - 1;
+   }
+   return ib;
+}
+
+// s = hinv . x with mat_vec_mul's order (src/matrix.c:54-56), no FMA.
+__device__ __forceinline__ double hrow(const double *m, double a0, double a1, double a2)
+{
+   return __dadd_rn(__dadd_rn(__dmul_rn(m[0], a0), __dmul_rn(m[1], a1)), __dmul_rn(m[2], a2));
+}
+
+__global__ void k_bin(RsParams P, const double *__restrict__ site, const double *__restrict__ cofm,
+                      const int *__restrict__ mol_first, const int *__restrict__ mol_n,
+                      int *__restrict__ cell_of, int *__restrict__ cell_count, DevOut *out)
+{
+   int e = blockIdx.x * blockDim.x + threadIdx.x;
+   if (e >= P.nent) return;
+   int bad = 0;
+   double s0, s1, s2;
+   if (!P.molpbc) {
+      const int N = P.nsites;
+      double x = site[e], y = site[N + e], z = site[2 * N + e];
+      s0 = hrow(P.hinv, x, y, z);
+      s1 = hrow(P.hinv + 3, x, y, z);
+      s2 = hrow(P.hinv + 6, x, y, z);
+   } else {
+      s0 = cofm[3 * e];
+      s1 = cofm[3 * e + 1];
+      s2 = cofm[3 * e + 2];
+   }
+   int cx = cellbin_dev(s0, P.nx, (double)P.nx, &bad);
+   int cy = cellbin_dev(s1, P.ny, (double)P.ny, &bad);
+   int cz = cellbin_dev(s2, P.nz, (double)P.nz, &bad);
+   int c = cz + P.nz * (cy + P.ny * cx);
+   if (bad) atomicOr(&out->err, 1);
+   if (!P.molpbc) {
+      cell_of[e] = c;
+      atomicAdd(&cell_count[c], 1);
+   } else {
+      int f = mol_first[e], n = mol_n[e];
+      for (int s = 0; s < n; s++) cell_of[f + s] = c;
+      atomicAdd(&cell_count[c], n);
+   }
+}
+
+// ---------------------------------------------------------- exclusive scan
+__device__ __forceinline__ int warp_incl_scan(int v)
+{
+   const int lane = threadIdx.x & 31;
+#pragma unroll
+   for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+   }
+   return v;
+}
+
+// Block-wide exclusive scan of 1024 values.
+__device__ void block_excl_scan(int v, int *out_excl)
+{
+   __shared__ int wsum[32];
+   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+   int inc = warp_incl_scan(v);
+   if (lane == 31) wsum[w] = inc;
+   __syncthreads();
+   if (w == 0) {
+      int s = wsum[lane];
+      int si = warp_incl_scan(s);
+      wsum[lane] = si - s;
+   }
+   __syncthreads();
+   *out_excl = inc - v + wsum[w];
+   __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(const int *__restrict__ in, int *__restrict__ out,
+                                                      int *__restrict__ bsum, int n)
+{
+   int i = blockIdx.x * 1024 + threadIdx.x;
+   int v = i < n ? in[i] : 0, ex;
+   __shared__ int last;
+   block_excl_scan(v, &ex);
+   if (threadIdx.x == 1023) last = ex + v;
+   __syncthreads();
+   if (i < n) out[i] = ex;
+   if (threadIdx.x == 0) bsum[blockIdx.x] = last;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(int *__restrict__ bsum, int nb, int *__restrict__ total)
+{
+   __shared__ int carry_s;
+   if (threadIdx.x == 0) carry_s = 0;
+   __syncthreads();
+   for (int b0 = 0; b0 < nb; b0 += 1024) {
+      int i = b0 + threadIdx.x;
+      int v = i < nb ? bsum[i] : 0, ex;
+      __shared__ int last;
+      block_excl_scan(v, &ex);
+      if (threadIdx.x == 1023) last = ex + v;
+      __syncthreads();
+      int carry = carry_s;
+      if (i < nb) bsum[i] = ex + carry;
+      __syncthreads();
+      if (threadIdx.x == 0) carry_s = carry + last;
+      __syncthreads();
+   }
+   if (threadIdx.x == 0) *total = carry_s;
+}
+
+__global__ void k_scan_add(int *__restrict__ out, const int *__restrict__ bsum, int n)
+{
+   int i = blockIdx.x * 1024 + threadIdx.x;
+   if (i < n) out[i] += bsum[blockIdx.x];
+}
+
+// ------------------------------------------------------ placement by cell
+__global__ void k_scatter(int n, const int *__restrict__ cell_of, const int *__restrict__ cell_start,
+                          int *__restrict__ cursor, int *__restrict__ sorted)
+{
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) return;
+   int c = cell_of[i];
+   sorted[cell_start[c] + atomicAdd(&cursor[c], 1)] = i;
+}
+
+__global__ void k_cellsort(int ncells, const int *__restrict__ cell_start, int *__restrict__ sorted)
+{
+   int c = blockIdx.x * blockDim.x + threadIdx.x;
+   if (c >= ncells) return;
+   int a = cell_start[c], b = cell_start[c + 1];
+   for (int i = a + 1; i < b; i++) {
+      int v = sorted[i], j = i - 1;
+      while (j >= a && sorted[j] > v) {
+         sorted[j + 1] = sorted[j];
+         j--;
+      }
+      sorted[j + 1] = v;
+   }
+}
+
+__global__ void k_gather(RsParams P, const double *__restrict__ site, const double *__restrict__ chg,
+                         const int *__restrict__ siteid, const int *__restrict__ molmap,
+                         const int *__restrict__ sorted, const int *__restrict__ cell_of,
+                         double4 *__restrict__ pos64, float4 *__restrict__ pos32,
+                         int2 *__restrict__ tag, int *__restrict__ slot_cell)
+{
+   int p = blockIdx.x * blockDim.x + threadIdx.x;
+   const int N = P.nsites;
+   if (p >= N) return;
+   int i = sorted[p], c = cell_of[i];
+   double x = site[i], y = site[N + i], z = site[2 * N + i], q = chg[i];
+   tag[p] = make_int2(siteid[i], molmap[i]);
+   slot_cell[p] = c;
+   if (pos64) pos64[p] = make_double4(x, y, z, q);
+   if (pos32) {
+      int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
+      double s0 = (double)cx / P.nx - 0.5, s1 = (double)cy / P.ny - 0.5, s2 = (double)cz / P.nz - 0.5;
+      double ox = P.h[0] * s0 + P.h[1] * s1 + P.h[2] * s2;
+      double oy = P.h[3] * s0 + P.h[4] * s1 + P.h[5] * s2;
+      double oz = P.h[6] * s0 + P.h[7] * s1 + P.h[8] * s2;
+      pos32[p] = make_float4((float)(x - ox), (float)(y - oy), (float)(z - oz), (float)q);
+   }
+}
+
+// ---------------------------------------------------------- pair potential
+#define AS1 0.254829592
+#define AS2 -0.284496736
+#define AS3 1.421413741
+#define AS4 -1.453152027
+#define AS5 1.061405429
+#define ASP 0.3275911
+
+template <typename R> __device__ __forceinline__ R dsqrt(R x);
+template <> __device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+template <typename R> __device__ __forceinline__ R dexp(R x);
+template <> __device__ __forceinline__ double dexp<double>(double x) { return exp(x); }
+template <> __device__ __forceinline__ float dexp<float>(float x) { return expf(x); }
+
+template <int PT> struct NPar { static constexpr int v = 8; };
+template <> struct NPar<0> { static constexpr int v = 2; };
+template <> struct NPar<1> { static constexpr int v = 3; };
+template <> struct NPar<2> { static constexpr int v = 4; };
+template <> struct NPar<3> { static constexpr int v = 6; };
+template <> struct NPar<4> { static constexpr int v = 3; };
+template <> struct NPar<6> { static constexpr int v = 7; };
+
+// One pair of kernel(): f = -U'(r)/r and U, with the erfc real-space Ewald
+// term by the A&S polynomial when EW (src/kernel.c:182-353 / 355-460).
+template <int PT, bool EW, typename R>
+__device__ __forceinline__ void pair_fu(R r2, R qq, const R *p, R alpha, R norm, R &f, R &u)
+{
+   R t = R(0), ef = R(0), r = R(0), r_r = R(0), rs_r;
+   if (EW || PT != 0) {
+      r = dsqrt<R>(r2);
+      r_r = R(1) / r;
+      rs_r = r_r * r_r;
+   } else {
+      rs_r = R(1) / r2;
+   }
+   if (EW) {
+      R ar = alpha * r;
+      t = R(1) / (R(1) + R(ASP) * ar);
+      ef = qq * dexp<R>(-(ar * ar));
+      t = (t * (R(AS1) + t * (R(AS2) + t * (R(AS3) + t * (R(AS4) + t * R(AS5)))))) * ef * r_r;
+      ef = t + norm * ef;
+   }
+   if (PT == 0) {
+      R r6 = (p[1] * p[1]) * rs_r;
+      r6 = r6 * r6 * r6;
+      R r12 = r6 * r6;
+      u = t + p[0] * (r12 - r6);
+      f = rs_r * (R(6) * p[0] * (R(2) * r12 - r6) + ef);
+   } else if (PT == 1) {
+      R e1 = p[1] * dexp<R>(-p[2] * r);
+      R r6 = p[0] * (rs_r * rs_r * rs_r);
+      u = t - r6 + e1;
+      f = rs_r * (R(-6) * r6 + ef) + p[2] * e1 * r_r;
+   } else if (PT == 2) {
+      R e1 = p[0] * dexp<R>(-p[1] * r);
+      R e2 = -p[2] * dexp<R>(-p[3] * r);
+      u = t + e1 + e2;
+      f = (p[1] * e1 + p[3] * e2) * r_r + ef * rs_r;
+   } else if (PT == 3) {
+      R e1 = p[0] * dexp<R>(-p[1] * r);
+      R r4 = rs_r * rs_r;
+      R r6 = rs_r * r4;
+      R r8 = p[5] * (r4 * r4);
+      R r12 = p[2] * (r6 * r6);
+      r4 *= p[3];
+      r6 *= p[4];
+      u = t + e1 + r12 - r4 - r6 - r8;
+      f = rs_r * (R(12) * r12 - R(4) * r4 - R(6) * r6 - R(8) * r8 + ef) + p[1] * e1 * r_r;
+   } else if (PT == 4) {
+      R r4 = rs_r * rs_r;
+      R r6 = rs_r * r4;
+      R r12 = p[2] * (r6 * r6);
+      r6 *= p[1];
+      r4 *= p[0];
+      u = t + r4 + r6 + r12;
+      f = rs_r * (R(4) * r4 + R(6) * r6 + R(12) * r12 + ef);
+   } else {  // Morse (PT == 6)
+      R e1 = p[0] * dexp<R>((p[1] - r) * p[2]);
+      R r6 = p[3] * (rs_r * rs_r * rs_r);
+      R e2 = p[4] * dexp<R>(R(-2) * p[5] * (r - p[6]));
+      R e3 = -p[4] * R(2) * dexp<R>(-p[5] * (r - p[6]));
+      u = t + e1 - r6 + e2 + e3;
+      f = rs_r * (R(-6) * r6 + ef) + r_r * (p[2] * e1 + (R(2) * p[5]) * e2 + p[5] * e3);
+   }
+}
+
+// --------------------------------------------------------------- pair loop
+__device__ __forceinline__ void note_too_close(DevOut *out, int a, int b)
+{
+   int k = atomicAdd(&out->n_too_close, 1);
+   if (k < MAX_TOO_CLOSE_REC) {
+      out->too_close[k][0] = a;
+      out->too_close[k][1] = b;
+   }
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double *sh)
+{
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+   __syncthreads();
+   if (lane == 0) sh[w] = v;
+   __syncthreads();
+   double s = 0.0;
+   if (threadIdx.x == 0)
+      for (int i = 0; i < nw; i++) s += sh[i];
+   return s;   // valid in thread 0
+}
+
+// MODE 0: forces/energy/virial; MODE 1: emit canonical pair keys only.
+template <int PT, bool EW, bool MIXED, int MODE>
+__global__ void __launch_bounds__(128)
+k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ slot_cell,
+        const int4 *__restrict__ full, const float4 *__restrict__ off_hi,
+        const float4 *__restrict__ off_lo, const double4 *__restrict__ pos64,
+        const float4 *__restrict__ pos32, const int2 *__restrict__ tag,
+        const int *__restrict__ sorted, const double *__restrict__ site,
+        const double *__restrict__ potg64, const float *__restrict__ potg32,
+        const double *__restrict__ chg64,
+        double *__restrict__ force, double *__restrict__ part, DevOut *out,
+        unsigned long long *__restrict__ keys, long long key_cap)
+{
+   typedef typename std::conditional<MIXED, float, double>::type R;
+   constexpr int NP = NPar<PT>::v;
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   R *pot_s = reinterpret_cast<R *>(smem_raw);
+   const int npot = P.max_id * P.max_id;
+   const R *potg = MIXED ? (const R *)(const void *)potg32 : (const R *)(const void *)potg64;
+   if (P.pot_in_smem)
+      for (int q = threadIdx.x; q < npot * NPOTP; q += blockDim.x) pot_s[q] = potg[q];
+   __syncthreads();
+   const R *pot = P.pot_in_smem ? pot_s : potg;
+
+   const int N = P.nsites;
+   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   const bool live = p < N;
+   double Fx = 0, Fy = 0, Fz = 0, Pe = 0, V[6] = {0, 0, 0, 0, 0, 0};
+   long long nev = 0;
+   if (live) {
+      const int c = slot_cell[p];
+      const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
+      const int2 ti = tag[p];
+      const R *prow = pot + (size_t)ti.x * P.max_id * NPOTP;
+      double4 xi64 = make_double4(0, 0, 0, 0);
+      float4 xi32 = make_float4(0, 0, 0, 0);
+      if (MIXED) xi32 = pos32[p]; else xi64 = pos64[p];
+      const R qi = MIXED ? (R)xi32.w : (R)xi64.w;
+      const R alpha = MIXED ? (R)P.alphaf : (R)P.alpha, norm = MIXED ? (R)P.normf : (R)P.norm;
+      // partial sums (FP32 in mixed form, folded into FP64 every 64 stencil cells)
+      R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+      for (int e = 0; e < P.nfull; e++) {
+         const int4 d = __ldg(&full[e]);
+         int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
+         const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
+         const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
+         const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
+         bx -= ix * P.nx;
+         by -= iy * P.ny;
+         bz -= iz * P.nz;
+         const int cb = bz + P.nz * (by + P.ny * bx);
+         const int kimg = 9 * (ix + 1) + 3 * (iy + 1) + (iz + 1);
+         const int j0 = __ldg(&cell_start[cb]), j1 = __ldg(&cell_start[cb + 1]);
+         float4 oh = make_float4(0, 0, 0, 0), ol = oh;
+         if (MIXED && j1 > j0) {
+            oh = __ldg(&off_hi[e]);
+            ol = __ldg(&off_lo[e]);
+         }
+         for (int j = j0; j < j1; j++) {
+            if (d.w && j == p) continue;
+            R rx, ry, rz, r2, qj;
+            int2 tj = __ldg(&tag[j]);
+            if (MIXED) {
+               const float4 xj = __ldg(&pos32[j]);
+               rx = (oh.x + (xj.x - xi32.x)) + ol.x;
+               ry = (oh.y + (xj.y - xi32.y)) + ol.y;
+               rz = (oh.z + (xj.z - xi32.z)) + ol.z;
+               r2 = rx * rx + ry * ry + rz * rz;
+               qj = xj.w;
+            } else {
+               const double4 xj = pos64[j];
+               const double *rl = P.reloc[kimg];
+               rx = __dadd_rn(__dsub_rn(xj.x, xi64.x), rl[0]);
+               ry = __dadd_rn(__dsub_rn(xj.y, xi64.y), rl[1]);
+               rz = __dadd_rn(__dsub_rn(xj.z, xi64.z), rl[2]);
+               r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+               qj = xj.w;
+            }
+            if (MODE == 1) {
+               const long long oi = sorted[p], oj = sorted[j];
+               if (oi < oj || (oi == oj && kimg < 13)) {
+                  unsigned long long key = ((unsigned long long)oi << 37) |
+                                           ((unsigned long long)oj << 5) | (unsigned long long)kimg;
+                  unsigned long long slot = atomicAdd((unsigned long long *)&out->npairs2, 1ull);
+                  if ((long long)slot < key_cap) keys[slot] = key;
+               }
+               continue;
+            }
+            // FP64 re-check of decisions near a threshold (mixed form only)
+            double r2x = (double)r2;
+            if (MIXED) {
+               const bool near_clip = P.strict && !P.molpbc && fabsf((float)r2 - P.cut2f) < P.bandf * P.cut2f;
+               const bool near_close = fabsf((float)r2 - (float)TOO_CLOSE) < 1e-3f;
+               if (near_clip || near_close) {
+                  const int oi = sorted[p], oj = sorted[j];
+                  const double *rl = P.reloc[kimg];
+                  double ax = __dadd_rn(__dsub_rn(site[oj], site[oi]), rl[0]);
+                  double ay = __dadd_rn(__dsub_rn(site[N + oj], site[N + oi]), rl[1]);
+                  double az = __dadd_rn(__dsub_rn(site[2 * N + oj], site[2 * N + oi]), rl[2]);
+                  r2x = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az));
+               }
+            }
+            const bool intra = ti.y == tj.y;
+            if (r2x < TOO_CLOSE && !intra) {
+               const int oi = sorted[p], oj = sorted[j];
+               if (oi < oj) note_too_close(out, oi, oj);
+            }
+            const bool clip = P.strict && !P.molpbc && r2x > P.cut2;
+            const R r2a = r2;
+            if (clip) r2 = (R)P.cut100;
+            R pp[NP];
+            const R *pj = prow + (size_t)tj.x * NPOTP;
+#pragma unroll
+            for (int k = 0; k < NP; k++) pp[k] = pj[k];
+            R f, u;
+            pair_fu<PT, EW, R>(r2, qj * qi, pp, alpha, norm, f, u);
+            if (MIXED && intra) {
+               // Mixed form: an intramolecular pair's energy is exactly what
+               // the intramolecular correction subtracts again, so it is left
+               // out of both (the FP32 roundings of identical molecules would
+               // add up coherently instead of cancelling).  A clamped pair
+               // keeps the difference between its clamped and true energies.
+               R fa, ua = R(0);
+               if (clip) pair_fu<PT, EW, R>(r2a, qj * qi, pp, alpha, norm, fa, ua);
+               u = clip ? u - ua : R(0);
+            }
+            const R hf = R(0.5) * f;
+            fx -= f * rx;
+            fy -= f * ry;
+            fz -= f * rz;
+            pe += R(0.5) * u;
+            v0 += hf * rx * rx;
+            v1 += hf * rx * ry;
+            v2 += hf * rx * rz;
+            v3 += hf * ry * ry;
+            v4 += hf * ry * rz;
+            v5 += hf * rz * rz;
+            nev++;
+         }
+         // fold the FP32 partial sums into FP64 at warp-uniform points: every
+         // thread walks the same stencil entries, so the (slow) FP64 adds
+         // never run under divergence
+         if (MIXED && (e & 63) == 63) {
+            Fx += fx; Fy += fy; Fz += fz; Pe += pe;
+            V[0] += v0; V[1] += v1; V[2] += v2; V[3] += v3; V[4] += v4; V[5] += v5;
+            fx = fy = fz = pe = v0 = v1 = v2 = v3 = v4 = v5 = 0;
+         }
+      }
+      Fx += fx; Fy += fy; Fz += fz; Pe += pe;
+      V[0] += v0; V[1] += v1; V[2] += v2; V[3] += v3; V[4] += v4; V[5] += v5;
+      if (MODE == 0) {
+         const int oi = sorted[p];
+         force[oi] = Fx;
+         force[N + oi] = Fy;
+         force[2 * N + oi] = Fz;
+      }
+   }
+   if (MODE == 1) return;
+   __shared__ double red[32];
+   double s;
+   s = block_sum_d(Pe, red);
+   if (threadIdx.x == 0) part[blockIdx.x * 8 + 0] = s;
+   for (int k = 0; k < 6; k++) {
+      s = block_sum_d(V[k], red);
+      if (threadIdx.x == 0) part[blockIdx.x * 8 + 1 + k] = s;
+   }
+   // evaluation count (integer, order-independent)
+   unsigned long long cnt = (unsigned long long)nev;
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+   if ((threadIdx.x & 31) == 0 && cnt) atomicAdd((unsigned long long *)&out->npairs2, cnt);
+}
+
+__global__ void k_reduce_rs(const double *__restrict__ part, int nblocks, DevOut *out)
+{
+   // one block of 32 threads: each component summed by one thread in block order
+   int k = threadIdx.x;
+   if (k >= 7) return;
+   double s = 0.0;
+   for (int b = 0; b < nblocks; b++) s += part[b * 8 + k];
+   if (k == 0) out->pe_rs = s; else out->vir_rs[k - 1] = s;
+}
+
+// -------------------------------------------------------------- host side
+static RsParams make_params(mdgpu_ctx *c)
+{
+   RsParams P;
+   memset(&P, 0, sizeof P);
+   const RsGeom &g = c->rs;
+   P.nsites = c->nsites;
+   P.nent = c->ctl.molpbc ? c->nmols : c->nsites;
+   P.nx = g.nx; P.ny = g.ny; P.nz = g.nz; P.ncells = g.ncells;
+   P.nfull = (int)g.full.size();
+   P.max_id = c->max_id;
+   P.molpbc = c->ctl.molpbc;
+   P.strict = c->ctl.strict_cutoff;
+   P.ptype = c->ptype;
+   for (int i = 0; i < 9; i++) P.hinv[i] = g.hinv[i];
+   for (int i = 0; i < 9; i++) P.h[i] = g.h[i];
+   for (int k = 0; k < 27; k++)
+      for (int r = 0; r < 3; r++) P.reloc[k][r] = g.reloc[k][r];
+   P.cut2 = g.cut2;
+   P.cut100 = g.cut100;
+   P.alpha = c->ctl.alpha;
+   P.norm = 2.0 * c->ctl.alpha / sqrt(PI);
+   P.cut2f = (float)g.cut2;
+   P.bandf = 1e-4f;
+   P.alphaf = (float)P.alpha;
+   P.normf = (float)P.norm;
+   return P;
+}
+
+mdgpu_status rs_prepare(mdgpu_ctx *c)
+{
+   RsDev &d = c->rd;
+   const RsGeom &g = c->rs;
+   const int N = c->nsites;
+   cudaStream_t st = c->stream;
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+   if (c->sys_dirty) {
+      CK(d.siteid.ensure(N));
+      CK(d.molmap.ensure(N));
+      CK(d.chg.ensure(N));
+      CK(d.ent_mol.ensure(2 * (size_t)c->nmols));
+      CK(cudaMemcpyAsync(d.siteid.p, c->site_id.data(), N * sizeof(int), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.molmap.p, c->molmap.data(), N * sizeof(int), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.chg.p, c->chg.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+      std::vector<int> mf(2 * (size_t)c->nmols);
+      for (int m = 0; m < c->nmols; m++) {
+         mf[m] = c->mol_first[m];
+         mf[c->nmols + m] = c->mol_nsites[m];
+      }
+      CK(cudaMemcpyAsync(d.ent_mol.p, mf.data(), mf.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+      const size_t np = (size_t)c->max_id * c->max_id * NPOTP;
+      CK(d.pot64.ensure(np));
+      CK(d.pot32.ensure(np));
+      std::vector<float> p32(np);
+      for (size_t i = 0; i < np; i++) p32[i] = (float)c->potpar[i];
+      CK(cudaMemcpyAsync(d.pot64.p, c->potpar.data(), np * sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.pot32.p, p32.data(), np * sizeof(float), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+      CK(d.cell_of.ensure(N));
+      CK(d.sorted.ensure(N));
+      CK(d.pos64.ensure(N));
+      CK(d.pos32.ensure(N));
+      CK(d.tag.ensure(N));
+      CK(d.slot_cell.ensure(N));
+   }
+   if (c->rs_valid && !c->rs_uploaded) {
+      CK(d.cell_count.ensure(g.ncells + 1));
+      CK(d.cell_start.ensure(g.ncells + 1));
+      CK(d.blocksum.ensure((g.ncells + 1 + 1023) / 1024 + 2));
+      CK(d.full.ensure(g.full.size()));
+      CK(d.off_hi.ensure(g.full.size()));
+      CK(d.off_lo.ensure(g.full.size()));
+      CK(cudaMemcpyAsync(d.full.p, g.full.data(), g.full.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.off_hi.p, g.off_hi.data(), g.off_hi.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.off_lo.p, g.off_lo.data(), g.off_lo.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+      c->rs_uploaded = true;
+   }
+   const int nb = (N + 127) / 128;
+   CK(d.part.ensure((size_t)nb * 8));
+   return MDGPU_OK;
+}
+
+template <int PT, bool EW, bool MIXED, int MODE>
+static cudaError_t launch_pairs_t(const RsParams &P, mdgpu_ctx *c, double *force, DevOut *out,
+                                  unsigned long long *keys, long long key_cap, size_t smem)
+{
+   RsDev &d = c->rd;
+   const int nb = (P.nsites + 127) / 128;
+   auto kfn = k_pairs<PT, EW, MIXED, MODE>;
+   if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+   }
+   kfn<<<nb, 128, smem, c->stream>>>(P, d.cell_start.p, d.slot_cell.p, d.full.p, d.off_hi.p, d.off_lo.p,
+                                     d.pos64.p, d.pos32.p, d.tag.p, d.sorted.p, c->cur_site,
+                                     d.pot64.p, d.pot32.p, d.chg.p, force, d.part.p, out, keys, key_cap);
+   return cudaGetLastError();
+}
+
+template <int PT>
+static cudaError_t launch_pairs_pt(const RsParams &P, mdgpu_ctx *c, bool ew, bool mixed, int mode,
+                                   double *force, DevOut *out, unsigned long long *keys,
+                                   long long key_cap, size_t smem)
+{
+   if (mode == 1) return launch_pairs_t<PT, false, false, 1>(P, c, force, out, keys, key_cap, smem);
+   if (mixed)
+      return ew ? launch_pairs_t<PT, true, true, 0>(P, c, force, out, keys, key_cap, smem)
+                : launch_pairs_t<PT, false, true, 0>(P, c, force, out, keys, key_cap, smem);
+   return ew ? launch_pairs_t<PT, true, false, 0>(P, c, force, out, keys, key_cap, smem)
+             : launch_pairs_t<PT, false, false, 0>(P, c, force, out, keys, key_cap, smem);
+}
+
+mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm, double *d_force,
+                       bool accumulate, unsigned long long *d_keys, int64_t key_cap,
+                       int64_t *unused)
+{
+   (void)accumulate;
+   (void)unused;
+   RsDev &d = c->rd;
+   const RsGeom &g = c->rs;
+   cudaStream_t st = c->stream;
+   RsParams P = make_params(c);
+   const int N = c->nsites;
+   DevOut *out = c->out.p;
+   c->cur_site = d_site;
+   phase_mark(c, MDGPU_PH_CELLS);
+   CK(cudaMemsetAsync(d.cell_count.p, 0, (g.ncells + 1) * sizeof(int), st));
+   const int nent = P.nent;
+   k_bin<<<(nent + 255) / 256, 256, 0, st>>>(P, d_site, d_cofm, d.ent_mol.p, d.ent_mol.p + c->nmols,
+                                             d.cell_of.p, d.cell_count.p, out);
+   const int n = g.ncells + 1, nbs = (n + 1023) / 1024;
+   k_scan_blocks<<<nbs, 1024, 0, st>>>(d.cell_count.p, d.cell_start.p, d.blocksum.p, n);
+   k_scan_sums<<<1, 1024, 0, st>>>(d.blocksum.p, nbs, d.blocksum.p + nbs);
+   k_scan_add<<<nbs, 1024, 0, st>>>(d.cell_start.p, d.blocksum.p, n);
+   CK(cudaMemsetAsync(d.cell_count.p, 0, (g.ncells + 1) * sizeof(int), st));
+   k_scatter<<<(N + 255) / 256, 256, 0, st>>>(N, d.cell_of.p, d.cell_start.p, d.cell_count.p, d.sorted.p);
+   k_cellsort<<<(g.ncells + 255) / 256, 256, 0, st>>>(g.ncells, d.cell_start.p, d.sorted.p);
+   const bool mixed = c->prec == MDGPU_MIXED && d_keys == nullptr;
+   k_gather<<<(N + 255) / 256, 256, 0, st>>>(P, d_site, d.chg.p, d.siteid.p, d.molmap.p, d.sorted.p,
+                                             d.cell_of.p, mixed ? nullptr : d.pos64.p,
+                                             mixed ? d.pos32.p : nullptr, d.tag.p, d.slot_cell.p);
+   CK(cudaGetLastError());
+   c->launches += 7;
+   phase_mark(c, MDGPU_PH_PAIRS);
+   const size_t potb = (size_t)c->max_id * c->max_id * NPOTP * (mixed ? sizeof(float) : sizeof(double));
+   P.pot_in_smem = potb <= 96 * 1024;
+   const size_t smem = P.pot_in_smem ? potb : 0;
+   const bool ew = c->ctl.alpha > 0.0;
+   const int mode = d_keys ? 1 : 0;
+   cudaError_t e;
+   switch (c->ptype) {
+   case 0: e = launch_pairs_pt<0>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
+   case 1: e = launch_pairs_pt<1>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
+   case 2: e = launch_pairs_pt<2>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
+   case 3: e = launch_pairs_pt<3>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
+   case 4: e = launch_pairs_pt<4>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
+   case 6: e = launch_pairs_pt<6>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
+   default: return fail(c, MDGPU_E_PTYPE, "KERNEL called with unknown potential type");
+   }
+   CK(e);
+   c->launches += 1;
+   if (mode == 0) {
+      k_reduce_rs<<<1, 32, 0, st>>>(d.part.p, (N + 127) / 128, out);
+      CK(cudaGetLastError());
+      c->launches += 1;
+   }
+   phase_mark(c, MDGPU_PH_KPREP);
+   return MDGPU_OK;
+#undef CK
+}
+
+}  // namespace mdgpu
