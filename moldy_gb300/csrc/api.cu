@@ -234,7 +234,9 @@ static mdgpu_status upload_sites(mdgpu_ctx *c, double *const site[3], const doub
       CKR(cudaMemcpyAsync(c->site.p + k * N, site[k], N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
    if (c->ctl.molpbc) {
       if (!c_of_m) return fail(c, MDGPU_E_ARG, "molecular cutoff needs the centres of mass");
-      CKR(cudaMemcpyAsync(c->cofm_in.p, c_of_m, 3 * c->nmols * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      c->last_cofm.assign(c_of_m, c_of_m + 3 * (size_t)c->nmols);
+      CKR(cudaMemcpyAsync(c->cofm_in.p, c->last_cofm.data(), 3 * c->nmols * sizeof(double),
+                          cudaMemcpyHostToDevice, c->stream));
    }
    return MDGPU_OK;
 }
@@ -493,14 +495,22 @@ mdgpu_status mdgpu_ewald(mdgpu_ctx *c, const double *h, double *const site[3],
    if (!c || !site || !site_force || !pe || !stress) return fail(c, MDGPU_E_ARG, "NULL argument");
    if (!c->have_control) return fail(c, MDGPU_E_ARG, "mdgpu_set_control has not been called");
    if (!(c->ctl.alpha > ALPHAMIN)) return MDGPU_OK;
-   mdgpu_status s = ensure_ready(c, h, false, true);
+   mdgpu_status s = ensure_ready(c, h, true, true);
    if (s) return s;
    const size_t N = c->nsites;
    for (int k = 0; k < 3; k++) {
       CKR(cudaMemcpyAsync(c->site.p + k * N, site[k], N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
       CKR(cudaMemcpyAsync(c->force.p + k * N, site_force[k], N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
    }
+   if (c->ctl.molpbc) {   // binning by molecule: the centres of mass are on the host record only
+      if (c->last_cofm.size() != 3 * (size_t)c->nmols)
+         return fail(c, MDGPU_E_ARG, "molecular cutoff needs the centres of mass (call force_calc first)");
+      CKR(cudaMemcpyAsync(c->cofm_in.p, c->last_cofm.data(), 3 * c->nmols * sizeof(double),
+                          cudaMemcpyHostToDevice, c->stream));
+   }
    CKR(cudaMemsetAsync(c->out.p, 0, sizeof(DevOut), c->stream));
+   s = rs_launch(c, c->site.p, c->cofm_in.p, c->force.p, true, nullptr, 0, nullptr);
+   if (s) return s;
    s = ks_launch(c, c->site.p, c->force.p, true);
    if (s) return s;
    for (int k = 0; k < 3; k++)

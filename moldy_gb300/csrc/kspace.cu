@@ -44,21 +44,27 @@ __device__ __forceinline__ unsigned long long to_fixed64(double s)
 __device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c);
 __device__ __forceinline__ void sincos_poly(unsigned int p, float *s, float *c);
 
-__global__ void k_prep(int N, const double *__restrict__ site, const double *__restrict__ chg,
-                       double hi0, double hi1, double hi2, double hi3, double hi4, double hi5,
-                       double hi6, double hi7, double hi8, int mixed, int4 *__restrict__ ph32,
-                       float2 *__restrict__ z32, float2 *__restrict__ zp32,
-                       ulonglong2 *__restrict__ ph64a, ulonglong2 *__restrict__ ph64b,
-                       double2 *__restrict__ z64)
+// Per-site records are written in link-cell order (slot i holds site
+// sorted[i]): the structure-factor chunks are then compact regions of the
+// cell, close to neutral, so their FP32 partial sums stay small even where
+// the full sum cancels (an ionic crystal listed species by species would
+// otherwise give chunks of a single charge sign).
+__global__ void k_prep(int N, const int *__restrict__ sorted, const double *__restrict__ site,
+                       const double *__restrict__ chg, double hi0, double hi1, double hi2,
+                       double hi3, double hi4, double hi5, double hi6, double hi7, double hi8,
+                       int mixed, int4 *__restrict__ ph32, float2 *__restrict__ z32,
+                       float2 *__restrict__ zp32, ulonglong2 *__restrict__ ph64a,
+                       ulonglong2 *__restrict__ ph64b, double2 *__restrict__ z64)
 {
-   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;   // slot
    if (i >= N) return;
-   double x = site[i], y = site[N + i], z = site[2 * N + i];
+   const int si = sorted[i];                                // site
+   double x = site[si], y = site[N + si], z = site[2 * N + si];
    double s0 = hi0 * x + hi1 * y + hi2 * z;
    double s1 = hi3 * x + hi4 * y + hi5 * z;
    double s2 = hi6 * x + hi7 * y + hi8 * z;
    unsigned long long ux = to_fixed64(s0), uy = to_fixed64(s1), uz = to_fixed64(s2);
-   double q = chg[i];
+   double q = chg[si];
    double sz, cz;
    sincospi(2.0 * ((double)(long long)uz * 5.421010862427522e-20), &sz, &cz);   // 2^-64
    if (mixed) {
@@ -306,11 +312,22 @@ __global__ void k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *ou
 // ---------------------------------------------------------------- forces
 constexpr int FT_ITEMS = 64;
 
+// s += x with the rounding error carried in c (Kahan's compensated sum;
+// s - c is the running total).
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+   const float y = x - c;
+   const float t = s + y;
+   c = (t - s) - y;
+   s = t;
+}
+
 __global__ void __launch_bounds__(256)
 k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
           const float2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
           const float4 *__restrict__ kd, const int4 *__restrict__ ph, const float2 *__restrict__ zz,
-          const double *__restrict__ chg, int N, double *__restrict__ fpart)
+          const double *__restrict__ chg, const int *__restrict__ sorted, int N,
+          double *__restrict__ fpart)
 {
    __shared__ int4 s_it[FT_ITEMS];
    __shared__ float2 s_kxy[FT_ITEMS];
@@ -332,9 +349,10 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
       zs[t] = live ? zt.y : 0.f;
    }
    const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
-   float fx = 0.f, fy = 0.f, fz = 0.f;
-   double Fx = 0.0, Fy = 0.0, Fz = 0.0;
-   int nfold = 0;
+   // compensated (Kahan) FP32 sums of the per-item force contributions: no
+   // FP64 instruction in the loop (on this part the FP64 pipe retires two
+   // lanes per clock per SM, and even a periodic FP64 fold halved the rate)
+   float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
    for (int tb = a; tb < b; tb += FT_ITEMS) {
       const int nt = min(FT_ITEMS, b - tb);
       const int kb = item_k0[tb];
@@ -368,23 +386,20 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
             }
          }
          const float2 kxy = s_kxy[q];
-         fx = fmaf(kxy.x, sf, fx);
-         fy = fmaf(kxy.y, sf, fy);
-         fz += skz;
-         if (++nfold == 32) {
-            Fx += fx; Fy += fy; Fz += fz;
-            fx = fy = fz = 0.f;
-            nfold = 0;
-         }
+         kahan_add(fx, ex, kxy.x * sf);
+         kahan_add(fy, ey, kxy.y * sf);
+         kahan_add(fz, ez, skz);
       }
    }
    if (live) {
-      Fx += fx; Fy += fy; Fz += fz;
-      const double q = chg[i];
+      const double Fx = (double)fx - (double)ex, Fy = (double)fy - (double)ey,
+                   Fz = (double)fz - (double)ez;
+      const int oi = sorted[i];   // slot i holds site oi
+      const double q = chg[oi];
       double *dst = fpart + (size_t)blockIdx.y * 3 * N;
-      dst[i] = q * Fx;
-      dst[N + i] = q * Fy;
-      dst[2 * N + i] = q * Fz;
+      dst[oi] = q * Fx;
+      dst[N + oi] = q * Fy;
+      dst[2 * N + oi] = q * Fz;
    }
 }
 
@@ -393,7 +408,8 @@ k_force64(const int4 *__restrict__ item, const int *__restrict__ item_k0,
           const double2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
           const double4 *__restrict__ kd, const ulonglong2 *__restrict__ pha,
           const ulonglong2 *__restrict__ phb, const double2 *__restrict__ zz,
-          const double *__restrict__ chg, int N, double *__restrict__ fpart)
+          const double *__restrict__ chg, const int *__restrict__ sorted, int N,
+          double *__restrict__ fpart)
 {
    __shared__ int4 s_it[FT_ITEMS];
    __shared__ double2 s_kxy[FT_ITEMS];
@@ -443,11 +459,12 @@ k_force64(const int4 *__restrict__ item, const int *__restrict__ item_k0,
       }
    }
    if (live) {
-      const double q = chg[i];
+      const int oi = sorted[i];   // slot i holds site oi
+      const double q = chg[oi];
       double *dst = fpart + (size_t)blockIdx.y * 3 * N;
-      dst[i] = q * Fx;
-      dst[N + i] = q * Fy;
-      dst[2 * N + i] = q * Fz;
+      dst[oi] = q * Fx;
+      dst[N + oi] = q * Fy;
+      dst[2 * N + oi] = q * Fz;
    }
 }
 
@@ -550,7 +567,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    double hinv[9];
    memcpy(hinv, kl.hinv, sizeof hinv);
    phase_mark(c, MDGPU_PH_KPREP);
-   k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, d_site, c->rd.chg.p, hinv[0], hinv[1], hinv[2], hinv[3],
+   k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, c->rd.sorted.p, d_site, c->rd.chg.p, hinv[0], hinv[1], hinv[2], hinv[3],
                                            hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], mixed ? 1 : 0,
                                            d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
    CK(cudaGetLastError());
@@ -583,10 +600,12 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    dim3 gf((N + 255) / 256, sh.splits);
    if (mixed)
       k_force32<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
-                                    d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, N, d.fpart.p);
+                                    d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, c->rd.sorted.p, N,
+                                    d.fpart.p);
    else
       k_force64<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, sh.per_split,
-                                    d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, N, d.fpart.p);
+                                    d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, c->rd.sorted.p, N,
+                                    d.fpart.p);
    CK(cudaGetLastError());
    phase_mark(c, MDGPU_PH_FINAL);
    k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, sh.splits, d.fpart.p, d_force, accumulate ? 1 : 0);

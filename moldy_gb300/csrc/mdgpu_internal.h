@@ -168,6 +168,7 @@ struct mdgpu_ctx {
    mdgpu::KsDev kd;
    mdgpu::DBuf<double> site, force, force_in, cofm_in, small;
    const double *cur_site = nullptr;   // site array of the launch in progress
+   std::vector<double> last_cofm;      // centres of mass of the last force_calc
    mdgpu::DBuf<mdgpu::DevOut> out;
    mdgpu::DevOut *h_out = nullptr;  // pinned mirror
    double *h_stage = nullptr;       // pinned staging for 6*nsites doubles
@@ -185,8 +186,10 @@ struct mdgpu_ctx {
 namespace mdgpu {
 // realspace.cu
 mdgpu_status rs_prepare(mdgpu_ctx *c);   // upload geometry/system tables
+// cells_only: bin and order the sites (the k-space passes stream them in
+// link-cell order) without the pair kernel.
 mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
-                       double *d_force, bool accumulate, unsigned long long *d_keys,
+                       double *d_force, bool cells_only, unsigned long long *d_keys,
                        int64_t key_cap, int64_t *d_keycount);
 // kspace.cu
 mdgpu_status ks_prepare(mdgpu_ctx *c);

@@ -309,6 +309,19 @@ __device__ __forceinline__ void pair_fu(R r2, R qq, const R *p, R alpha, R norm,
 }
 
 // --------------------------------------------------------------- pair loop
+// s += x: plain in FP64, Kahan-compensated in FP32 (s - c is the total).
+__device__ __forceinline__ void accum(double &s, double &c, double x)
+{
+   (void)c;
+   s += x;
+}
+__device__ __forceinline__ void accum(float &s, float &c, float x)
+{
+   const float y = x - c;
+   const float t = s + y;
+   c = (t - s) - y;
+   s = t;
+}
 __device__ __forceinline__ void note_too_close(DevOut *out, int a, int b)
 {
    int k = atomicAdd(&out->n_too_close, 1);
@@ -372,7 +385,10 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
       const R qi = MIXED ? (R)xi32.w : (R)xi64.w;
       const R alpha = MIXED ? (R)P.alphaf : (R)P.alpha, norm = MIXED ? (R)P.normf : (R)P.norm;
       // partial sums (FP32 in mixed form, folded into FP64 every 64 stencil cells)
+      // force and energy: compensated sums in mixed form (no FP64 in the
+      // loop; on this part FP64 retires two lanes per clock per SM)
       R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+      R cx_ = 0, cy_ = 0, cz_ = 0, cpe = 0;
       for (int e = 0; e < P.nfull; e++) {
          const int4 d = __ldg(&full[e]);
          int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
@@ -459,10 +475,10 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
                u = clip ? u - ua : R(0);
             }
             const R hf = R(0.5) * f;
-            fx -= f * rx;
-            fy -= f * ry;
-            fz -= f * rz;
-            pe += R(0.5) * u;
+            accum(fx, cx_, -f * rx);
+            accum(fy, cy_, -f * ry);
+            accum(fz, cz_, -f * rz);
+            accum(pe, cpe, R(0.5) * u);
             v0 += hf * rx * rx;
             v1 += hf * rx * ry;
             v2 += hf * rx * rz;
@@ -471,16 +487,11 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
             v5 += hf * rz * rz;
             nev++;
          }
-         // fold the FP32 partial sums into FP64 at warp-uniform points: every
-         // thread walks the same stencil entries, so the (slow) FP64 adds
-         // never run under divergence
-         if (MIXED && (e & 63) == 63) {
-            Fx += fx; Fy += fy; Fz += fz; Pe += pe;
-            V[0] += v0; V[1] += v1; V[2] += v2; V[3] += v3; V[4] += v4; V[5] += v5;
-            fx = fy = fz = pe = v0 = v1 = v2 = v3 = v4 = v5 = 0;
-         }
       }
-      Fx += fx; Fy += fy; Fz += fz; Pe += pe;
+      Fx = (double)fx - (double)cx_;
+      Fy = (double)fy - (double)cy_;
+      Fz = (double)fz - (double)cz_;
+      Pe = (double)pe - (double)cpe;
       V[0] += v0; V[1] += v1; V[2] += v2; V[3] += v3; V[4] += v4; V[5] += v5;
       if (MODE == 0) {
          const int oi = sorted[p];
@@ -629,10 +640,9 @@ static cudaError_t launch_pairs_pt(const RsParams &P, mdgpu_ctx *c, bool ew, boo
 }
 
 mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm, double *d_force,
-                       bool accumulate, unsigned long long *d_keys, int64_t key_cap,
+                       bool cells_only, unsigned long long *d_keys, int64_t key_cap,
                        int64_t *unused)
 {
-   (void)accumulate;
    (void)unused;
    RsDev &d = c->rd;
    const RsGeom &g = c->rs;
@@ -660,6 +670,7 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
    CK(cudaGetLastError());
    c->launches += 7;
    phase_mark(c, MDGPU_PH_PAIRS);
+   if (cells_only) return MDGPU_OK;
    const size_t potb = (size_t)c->max_id * c->max_id * NPOTP * (mixed ? sizeof(float) : sizeof(double));
    P.pot_in_smem = potb <= 96 * 1024;
    const size_t smem = P.pot_in_smem ? potb : 0;
