@@ -164,6 +164,31 @@ mdgpu_status mdgpu_pair_keys(mdgpu_ctx *ctx, const double *h, const double *site
                              const double *c_of_m, uint64_t *keys, int64_t cap,
                              int64_t *count);
 
+/* Reciprocal-space Ewald sum that allocates nothing.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc: code running under
+ * CUDA stream capture (allocation cannot be captured into a graph), hosts
+ * that own all device memory through their own pools, and step loops that
+ * must not take the allocator's locks or fail for lack of memory mid-run.
+ * Adds the k-space forces into d_force[3][nsites], the k-space energy
+ * (without the self and sheet terms of ewald(), src/ewald.c:367-433) into
+ * *d_pe and the stress upper triangle into d_stress[9]; every pointer is the
+ * caller's device memory, h is on the host, charges d_chg[nsites] are in
+ * program units.  FP32-mixed arithmetic.  Intermediates live in a static
+ * device array of MDGPU_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit; nsites above MDGPU_NOALLOC_MAX_SITES or more
+ * than MDGPU_NOALLOC_MAX_KVEC k-vectors return MDGPU_E_CAPACITY.  The first
+ * call on a device looks the array up (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (other streams, other host threads) race.  Runs on `stream`
+ * (a cudaStream_t, NULL for the default stream) of the current device. */
+#define MDGPU_NOALLOC_MAX_SITES 16384
+#define MDGPU_NOALLOC_MAX_KVEC 8192
+#define MDGPU_NOALLOC_SCRATCH_BYTES (6u << 20)
+mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, const double *d_site,
+                                        const double *d_chg, double alpha, double k_cutoff,
+                                        double *d_force, double *d_pe, double *d_stress,
+                                        void *stream);
+
 /* Measures the device's dense FMA throughput (TFLOP/s, FMA = 2 flops) in
  * FP32 (fp64 = 0) or FP64: the roofline denominators of the force kernels,
  * whose bound is the FMA pipe.  No counterpart in the reference. */

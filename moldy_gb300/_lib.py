@@ -22,6 +22,7 @@ EXPORTS = ["mdgpu_create", "mdgpu_destroy", "mdgpu_last_error", "mdgpu_set_preci
            "mdgpu_force_calc", "mdgpu_ewald", "mdgpu_forces", "mdgpu_forces_device",
            "mdgpu_synchronize", "mdgpu_get_info", "mdgpu_pair_keys", "mdgpu_poteval",
            "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak",
+           "mdgpu_ewald_kspace_noalloc",
            "force_calc", "ewald", "poteval"]
 
 
@@ -93,6 +94,7 @@ def load():
         "mdgpu_set_phase_timing": ([vp, ip], ip),
         "mdgpu_phase_times": ([vp, dp], ip),
         "mdgpu_fma_peak": ([ip, ip, dp], ip),
+        "mdgpu_ewald_kspace_noalloc": ([dp, ip, vp, vp, C.c_double, C.c_double, vp, vp, vp, vp], ip),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
