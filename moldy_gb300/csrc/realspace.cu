@@ -10,7 +10,7 @@
 //      k_cellsort   in ascending site order (deterministic layout);
 //   4. k_gather     per-slot records: FP64 (x,y,z,q), or FP32 co-ordinates
 //                   relative to the cell origin plus q, and (site id, molecule);
-//   5. k_pairs      one thread per site walks the full neighbour-cell stencil
+//   5. k_pairs      one warp per site walks the full neighbour-cell stencil
 //                   (the reference's half-space list and its mirror) and
 //                   evaluates every candidate pair the reference evaluates,
 //                   accumulating the force on its own site only; energy and
@@ -346,8 +346,18 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh)
 }
 
 // MODE 0: forces/energy/virial; MODE 1: emit canonical pair keys only.
+//
+// One warp per home site.  The warp walks the full stencil 32 entries at a
+// time: lane e finds the slot range of stencil cell e (a contiguous run of
+// the cell-sorted arrays), a warp prefix sum lays the ranges end to end, and
+// the candidates are then dealt out 32 at a time, each lane locating its
+// candidate's stencil entry by binary search over the scanned counts.  Every
+// lane runs the same pair arithmetic on a different candidate, so the warp
+// stays converged however unevenly the sites are spread over the cells.
+constexpr int PAIR_WARPS = 8;   // warps per block
+
 template <int PT, bool EW, bool MIXED, int MODE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(PAIR_WARPS * 32)
 k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ slot_cell,
         const int4 *__restrict__ full, const float4 *__restrict__ off_hi,
         const float4 *__restrict__ off_lo, const double4 *__restrict__ pos64,
@@ -361,6 +371,8 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
    typedef typename std::conditional<MIXED, float, double>::type R;
    constexpr int NP = NPar<PT>::v;
    extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ int s_inc[PAIR_WARPS][32], s_jb[PAIR_WARPS][32], s_info[PAIR_WARPS][32];
+   __shared__ float4 s_oh[PAIR_WARPS][32], s_ol[PAIR_WARPS][32];
    R *pot_s = reinterpret_cast<R *>(smem_raw);
    const int npot = P.max_id * P.max_id;
    const R *potg = MIXED ? (const R *)(const void *)potg32 : (const R *)(const void *)potg64;
@@ -370,11 +382,12 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
    const R *pot = P.pot_in_smem ? pot_s : potg;
 
    const int N = P.nsites;
-   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-   const bool live = p < N;
-   double Fx = 0, Fy = 0, Fz = 0, Pe = 0, V[6] = {0, 0, 0, 0, 0, 0};
+   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int p = blockIdx.x * PAIR_WARPS + w;   // home slot of this warp
+   // per-lane partial sums: few terms each, then a warp tree reduction
+   R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
    long long nev = 0;
-   if (live) {
+   if (p < N) {
       const int c = slot_cell[p];
       const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
       const int2 ti = tag[p];
@@ -384,146 +397,212 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
       if (MIXED) xi32 = pos32[p]; else xi64 = pos64[p];
       const R qi = MIXED ? (R)xi32.w : (R)xi64.w;
       const R alpha = MIXED ? (R)P.alphaf : (R)P.alpha, norm = MIXED ? (R)P.normf : (R)P.norm;
-      // partial sums (FP32 in mixed form, folded into FP64 every 64 stencil cells)
-      // force and energy: compensated sums in mixed form (no FP64 in the
-      // loop; on this part FP64 retires two lanes per clock per SM)
-      R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
-      R cx_ = 0, cy_ = 0, cz_ = 0, cpe = 0;
-      for (int e = 0; e < P.nfull; e++) {
-         const int4 d = __ldg(&full[e]);
-         int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
-         const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
-         const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
-         const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
-         bx -= ix * P.nx;
-         by -= iy * P.ny;
-         bz -= iz * P.nz;
-         const int cb = bz + P.nz * (by + P.ny * bx);
-         const int kimg = 9 * (ix + 1) + 3 * (iy + 1) + (iz + 1);
-         const int j0 = __ldg(&cell_start[cb]), j1 = __ldg(&cell_start[cb + 1]);
+      const int oi = sorted[p];
+      for (int base = 0; base < P.nfull; base += 32) {
+         // lane `lane` takes stencil entry base + lane
+         const int e = base + lane;
+         int cnt = 0, jb = 0, info = 0;
          float4 oh = make_float4(0, 0, 0, 0), ol = oh;
-         if (MIXED && j1 > j0) {
-            oh = __ldg(&off_hi[e]);
-            ol = __ldg(&off_lo[e]);
+         if (e < P.nfull) {
+            const int4 d = __ldg(&full[e]);
+            int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
+            const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
+            const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
+            const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
+            bx -= ix * P.nx;
+            by -= iy * P.ny;
+            bz -= iz * P.nz;
+            const int cb = bz + P.nz * (by + P.ny * bx);
+            const int j0 = __ldg(&cell_start[cb]);
+            cnt = __ldg(&cell_start[cb + 1]) - j0;
+            jb = j0;
+            info = (9 * (ix + 1) + 3 * (iy + 1) + (iz + 1)) | (d.w << 8);
+            if (MIXED) {
+               oh = __ldg(&off_hi[e]);
+               ol = __ldg(&off_lo[e]);
+            }
          }
-         for (int j = j0; j < j1; j++) {
-            if (d.w && j == p) continue;
-            R rx, ry, rz, r2, qj;
-            int2 tj = __ldg(&tag[j]);
-            if (MIXED) {
-               const float4 xj = __ldg(&pos32[j]);
-               rx = (oh.x + (xj.x - xi32.x)) + ol.x;
-               ry = (oh.y + (xj.y - xi32.y)) + ol.y;
-               rz = (oh.z + (xj.z - xi32.z)) + ol.z;
-               r2 = rx * rx + ry * ry + rz * rz;
-               qj = xj.w;
-            } else {
-               const double4 xj = pos64[j];
-               const double *rl = P.reloc[kimg];
-               rx = __dadd_rn(__dsub_rn(xj.x, xi64.x), rl[0]);
-               ry = __dadd_rn(__dsub_rn(xj.y, xi64.y), rl[1]);
-               rz = __dadd_rn(__dsub_rn(xj.z, xi64.z), rl[2]);
-               r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
-               qj = xj.w;
-            }
-            if (MODE == 1) {
-               const long long oi = sorted[p], oj = sorted[j];
-               if (oi < oj || (oi == oj && kimg < 13)) {
-                  unsigned long long key = ((unsigned long long)oi << 37) |
-                                           ((unsigned long long)oj << 5) | (unsigned long long)kimg;
-                  unsigned long long slot = atomicAdd((unsigned long long *)&out->npairs2, 1ull);
-                  if ((long long)slot < key_cap) keys[slot] = key;
-               }
-               continue;
-            }
-            // FP64 re-check of decisions near a threshold (mixed form only)
-            double r2x = (double)r2;
-            if (MIXED) {
-               const bool near_clip = P.strict && !P.molpbc && fabsf((float)r2 - P.cut2f) < P.bandf * P.cut2f;
-               const bool near_close = fabsf((float)r2 - (float)TOO_CLOSE) < 1e-3f;
-               if (near_clip || near_close) {
-                  const int oi = sorted[p], oj = sorted[j];
-                  const double *rl = P.reloc[kimg];
-                  double ax = __dadd_rn(__dsub_rn(site[oj], site[oi]), rl[0]);
-                  double ay = __dadd_rn(__dsub_rn(site[N + oj], site[N + oi]), rl[1]);
-                  double az = __dadd_rn(__dsub_rn(site[2 * N + oj], site[2 * N + oi]), rl[2]);
-                  r2x = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az));
-               }
-            }
-            const bool intra = ti.y == tj.y;
-            if (r2x < TOO_CLOSE && !intra) {
-               const int oi = sorted[p], oj = sorted[j];
-               if (oi < oj) note_too_close(out, oi, oj);
-            }
-            const bool clip = P.strict && !P.molpbc && r2x > P.cut2;
-            const R r2a = r2;
-            if (clip) r2 = (R)P.cut100;
-            R pp[NP];
-            const R *pj = prow + (size_t)tj.x * NPOTP;
+         const int inc = warp_incl_scan(cnt);
+         const int T = __shfl_sync(0xffffffffu, inc, 31);
+         s_inc[w][lane] = inc;
+         s_jb[w][lane] = jb - (inc - cnt);     // slot = s_jb[k] + candidate index
+         s_info[w][lane] = info;
+         if (MIXED) {
+            s_oh[w][lane] = oh;
+            s_ol[w][lane] = ol;
+         }
+         __syncwarp();
+         for (int r = 0; r < T; r += 32) {
+            const int idx = r + lane;
+            if (idx < T) {
+               int k = 0;
 #pragma unroll
-            for (int k = 0; k < NP; k++) pp[k] = pj[k];
-            R f, u;
-            pair_fu<PT, EW, R>(r2, qj * qi, pp, alpha, norm, f, u);
-            if (MIXED && intra) {
-               // Mixed form: an intramolecular pair's energy is exactly what
-               // the intramolecular correction subtracts again, so it is left
-               // out of both (the FP32 roundings of identical molecules would
-               // add up coherently instead of cancelling).  A clamped pair
-               // keeps the difference between its clamped and true energies.
-               R fa, ua = R(0);
-               if (clip) pair_fu<PT, EW, R>(r2a, qj * qi, pp, alpha, norm, fa, ua);
-               u = clip ? u - ua : R(0);
+               for (int s = 16; s >= 1; s >>= 1)
+                  if (s_inc[w][k + s - 1] <= idx) k += s;
+               const int j = s_jb[w][k] + idx;
+               const int inf = s_info[w][k];
+               const int kimg = inf & 255;
+               if (!((inf >> 8) && j == p)) {
+                  R rx, ry, rz, r2, qj;
+                  const int2 tj = __ldg(&tag[j]);
+                  if (MIXED) {
+                     const float4 xj = __ldg(&pos32[j]);
+                     const float4 h4 = s_oh[w][k], l4 = s_ol[w][k];
+                     rx = (h4.x + (xj.x - xi32.x)) + l4.x;
+                     ry = (h4.y + (xj.y - xi32.y)) + l4.y;
+                     rz = (h4.z + (xj.z - xi32.z)) + l4.z;
+                     r2 = rx * rx + ry * ry + rz * rz;
+                     qj = xj.w;
+                  } else {
+                     const double4 xj = pos64[j];
+                     const double *rl = P.reloc[kimg];
+                     rx = __dadd_rn(__dsub_rn(xj.x, xi64.x), rl[0]);
+                     ry = __dadd_rn(__dsub_rn(xj.y, xi64.y), rl[1]);
+                     rz = __dadd_rn(__dsub_rn(xj.z, xi64.z), rl[2]);
+                     r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+                     qj = xj.w;
+                  }
+                  if (MODE == 1) {
+                     const long long a = oi, bb = sorted[j];
+                     if (a < bb || (a == bb && kimg < 13)) {
+                        unsigned long long key = ((unsigned long long)a << 37) |
+                                                 ((unsigned long long)bb << 5) | (unsigned long long)kimg;
+                        unsigned long long slot = atomicAdd((unsigned long long *)&out->npairs2, 1ull);
+                        if ((long long)slot < key_cap) keys[slot] = key;
+                     }
+                  } else {
+                     // Threshold decisions (too-close warning, strict-cutoff
+                     // clamp).  FP64 form: exact, on the reference's r^2.
+                     // Mixed form: on the FP32 r^2, except within a narrow
+                     // band of either threshold, where r^2 is re-formed in
+                     // FP64 from the original co-ordinates (rare).
+                     const bool intra = ti.y == tj.y;
+                     bool too_close, clip;
+                     if (MIXED) {
+                        const float r2f = (float)r2;
+                        const bool near_clip = P.strict && !P.molpbc && fabsf(r2f - P.cut2f) < P.bandf * P.cut2f;
+                        const bool near_close = fabsf(r2f - (float)TOO_CLOSE) < 1e-3f;
+                        too_close = r2f < (float)TOO_CLOSE;
+                        clip = P.strict && !P.molpbc && r2f > P.cut2f;
+                        if (near_clip || near_close) {
+                           const int oj = sorted[j];
+                           const double *rl = P.reloc[kimg];
+                           double ax = __dadd_rn(__dsub_rn(site[oj], site[oi]), rl[0]);
+                           double ay = __dadd_rn(__dsub_rn(site[N + oj], site[N + oi]), rl[1]);
+                           double az = __dadd_rn(__dsub_rn(site[2 * N + oj], site[2 * N + oi]), rl[2]);
+                           const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)),
+                                                       __dmul_rn(az, az));
+                           too_close = d2 < TOO_CLOSE;
+                           clip = P.strict && !P.molpbc && d2 > P.cut2;
+                        }
+                     } else {
+                        too_close = (double)r2 < TOO_CLOSE;
+                        clip = P.strict && !P.molpbc && (double)r2 > P.cut2;
+                     }
+                     if (too_close && !intra) {
+                        const int oj = sorted[j];
+                        if (oi < oj) note_too_close(out, oi, oj);
+                     }
+                     const R r2a = r2;
+                     if (clip) r2 = (R)P.cut100;
+                     R pp[NP];
+                     const R *pj = prow + (size_t)tj.x * NPOTP;
+#pragma unroll
+                     for (int q = 0; q < NP; q++) pp[q] = pj[q];
+                     R f, u;
+                     pair_fu<PT, EW, R>(r2, qj * qi, pp, alpha, norm, f, u);
+                     if (MIXED && intra) {
+                        // Mixed form: an intramolecular pair's energy is
+                        // exactly what the intramolecular correction subtracts
+                        // again, so it is left out of both (FP32 roundings of
+                        // identical molecules would add up coherently instead
+                        // of cancelling); a clamped pair keeps the difference
+                        // between its clamped and true energies.
+                        R fa, ua = R(0);
+                        if (clip) pair_fu<PT, EW, R>(r2a, qj * qi, pp, alpha, norm, fa, ua);
+                        u = clip ? u - ua : R(0);
+                     }
+                     const R hf = R(0.5) * f;
+                     fx -= f * rx;
+                     fy -= f * ry;
+                     fz -= f * rz;
+                     pe += R(0.5) * u;
+                     v0 += hf * rx * rx;
+                     v1 += hf * rx * ry;
+                     v2 += hf * rx * rz;
+                     v3 += hf * ry * ry;
+                     v4 += hf * ry * rz;
+                     v5 += hf * rz * rz;
+                     nev++;
+                  }
+               }
             }
-            const R hf = R(0.5) * f;
-            accum(fx, cx_, -f * rx);
-            accum(fy, cy_, -f * ry);
-            accum(fz, cz_, -f * rz);
-            accum(pe, cpe, R(0.5) * u);
-            v0 += hf * rx * rx;
-            v1 += hf * rx * ry;
-            v2 += hf * rx * rz;
-            v3 += hf * ry * ry;
-            v4 += hf * ry * rz;
-            v5 += hf * rz * rz;
-            nev++;
          }
+         __syncwarp();
       }
-      Fx = (double)fx - (double)cx_;
-      Fy = (double)fy - (double)cy_;
-      Fz = (double)fz - (double)cz_;
-      Pe = (double)pe - (double)cpe;
-      V[0] += v0; V[1] += v1; V[2] += v2; V[3] += v3; V[4] += v4; V[5] += v5;
       if (MODE == 0) {
-         const int oi = sorted[p];
-         force[oi] = Fx;
-         force[N + oi] = Fy;
-         force[2 * N + oi] = Fz;
+         // warp tree reduction of the home site's force, in the working
+         // precision (each lane holds a sum of a few pairs)
+         R Fx = fx, Fy = fy, Fz = fz;
+#pragma unroll
+         for (int o = 16; o > 0; o >>= 1) {
+            Fx += __shfl_down_sync(0xffffffffu, Fx, o);
+            Fy += __shfl_down_sync(0xffffffffu, Fy, o);
+            Fz += __shfl_down_sync(0xffffffffu, Fz, o);
+         }
+         if (lane == 0) {
+            force[oi] = (double)Fx;
+            force[N + oi] = (double)Fy;
+            force[2 * N + oi] = (double)Fz;
+         }
       }
    }
    if (MODE == 1) return;
-   __shared__ double red[32];
-   double s;
-   s = block_sum_d(Pe, red);
-   if (threadIdx.x == 0) part[blockIdx.x * 8 + 0] = s;
-   for (int k = 0; k < 6; k++) {
-      s = block_sum_d(V[k], red);
-      if (threadIdx.x == 0) part[blockIdx.x * 8 + 1 + k] = s;
+   // energy and virial: warp trees in the working precision, then the
+   // block's warps summed in FP64 (FP64 is slow on this part: keep it to a
+   // handful of operations per block)
+   __shared__ R wred[7][PAIR_WARPS];
+   R vv[7] = {pe, v0, v1, v2, v3, v4, v5};
+#pragma unroll
+   for (int k = 0; k < 7; k++) {
+      R s = vv[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) wred[k][w] = s;
    }
-   // evaluation count (integer, order-independent)
+   __syncthreads();
+   if (threadIdx.x < 7) {
+      double s = 0.0;
+      for (int q = 0; q < PAIR_WARPS; q++) s += (double)wred[threadIdx.x][q];
+      part[blockIdx.x * 8 + threadIdx.x] = s;
+   }
    unsigned long long cnt = (unsigned long long)nev;
 #pragma unroll
    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-   if ((threadIdx.x & 31) == 0 && cnt) atomicAdd((unsigned long long *)&out->npairs2, cnt);
+   if (lane == 0 && cnt) atomicAdd((unsigned long long *)&out->npairs2, cnt);
 }
 
-__global__ void k_reduce_rs(const double *__restrict__ part, int nblocks, DevOut *out)
+// One block of 256 threads: thread t sums blocks t, t+256, ... of each
+// component, then a fixed-shape tree combines the 256 partial sums (the
+// result does not depend on timing).
+__global__ void __launch_bounds__(256) k_reduce_rs(const double *__restrict__ part, int nblocks, DevOut *out)
 {
-   // one block of 32 threads: each component summed by one thread in block order
-   int k = threadIdx.x;
-   if (k >= 7) return;
-   double s = 0.0;
-   for (int b = 0; b < nblocks; b++) s += part[b * 8 + k];
-   if (k == 0) out->pe_rs = s; else out->vir_rs[k - 1] = s;
+   __shared__ double sh[7][256];
+   const int t = threadIdx.x;
+   double s[7] = {0, 0, 0, 0, 0, 0, 0};
+   for (int b = t; b < nblocks; b += 256)
+      for (int k = 0; k < 7; k++) s[k] += part[b * 8 + k];
+   for (int k = 0; k < 7; k++) sh[k][t] = s[k];
+   __syncthreads();
+   for (int w = 128; w > 0; w >>= 1) {
+      if (t < w)
+         for (int k = 0; k < 7; k++) sh[k][t] += sh[k][t + w];
+      __syncthreads();
+   }
+   if (t == 0) {
+      out->pe_rs = sh[0][0];
+      for (int k = 0; k < 6; k++) out->vir_rs[k] = sh[k + 1][0];
+   }
 }
 
 // -------------------------------------------------------------- host side
@@ -604,7 +683,7 @@ mdgpu_status rs_prepare(mdgpu_ctx *c)
       CK(cudaStreamSynchronize(st));
       c->rs_uploaded = true;
    }
-   const int nb = (N + 127) / 128;
+   const int nb = (N + PAIR_WARPS - 1) / PAIR_WARPS;
    CK(d.part.ensure((size_t)nb * 8));
    return MDGPU_OK;
 }
@@ -614,13 +693,13 @@ static cudaError_t launch_pairs_t(const RsParams &P, mdgpu_ctx *c, double *force
                                   unsigned long long *keys, long long key_cap, size_t smem)
 {
    RsDev &d = c->rd;
-   const int nb = (P.nsites + 127) / 128;
+   const int nb = (P.nsites + PAIR_WARPS - 1) / PAIR_WARPS;
    auto kfn = k_pairs<PT, EW, MIXED, MODE>;
    if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
    }
-   kfn<<<nb, 128, smem, c->stream>>>(P, d.cell_start.p, d.slot_cell.p, d.full.p, d.off_hi.p, d.off_lo.p,
+   kfn<<<nb, PAIR_WARPS * 32, smem, c->stream>>>(P, d.cell_start.p, d.slot_cell.p, d.full.p, d.off_hi.p, d.off_lo.p,
                                      d.pos64.p, d.pos32.p, d.tag.p, d.sorted.p, c->cur_site,
                                      d.pot64.p, d.pot32.p, d.chg.p, force, d.part.p, out, keys, key_cap);
    return cudaGetLastError();
@@ -689,7 +768,7 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
    CK(e);
    c->launches += 1;
    if (mode == 0) {
-      k_reduce_rs<<<1, 32, 0, st>>>(d.part.p, (N + 127) / 128, out);
+      k_reduce_rs<<<1, 256, 0, st>>>(d.part.p, (N + PAIR_WARPS - 1) / PAIR_WARPS, out);
       CK(cudaGetLastError());
       c->launches += 1;
    }
