@@ -370,7 +370,16 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", choices=["mixed", "fp64"],
+                    help="run three untimed evaluations of the workload and exit (for ncu captures)")
     args = ap.parse_args()
+    if args.profile_case:
+        from moldy_gb300.forcefield import ForceField
+        ff = ForceField(make_workload(), precision=args.profile_case)
+        for _ in range(3):
+            _, pe, _ = ff.forces()
+        log("profile case done", pe)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
