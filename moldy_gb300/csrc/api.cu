@@ -740,6 +740,12 @@ void force_calc(real **site, real **site_force, system_mt *system, spec_mt *spec
    mdgpu_ctx *c = ref_ctx();
    double h[9];
    ref_sync(c, system, species, chg, potpar, h);
+   // force_calc also accumulates the radial distribution function on RDF
+   // steps (src/force.c:1302-1313); that part is not on the GPU path
+   if (control.rdf_interval > 0 && control.istep >= control.begin_rdf &&
+       control.istep % control.rdf_interval == 0)
+      ref_fatal("moldy_gb300: RDF accumulation is not available on the GPU force path "
+                "(set rdf-interval=0)");
    double st[9];
    for (int i = 0; i < 9; i++) st[i] = stress[i / 3][i % 3];
    mdgpu_status s = mdgpu_force_calc(c, h, site, site_force, &system->c_of_m[0][0], pe, st);

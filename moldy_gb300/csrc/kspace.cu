@@ -184,6 +184,7 @@ k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nit
    }
 }
 
+
 __global__ void __launch_bounds__(128)
 k_sfac64(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nitems,
          const ulonglong2 *__restrict__ pha, const ulonglong2 *__restrict__ phb,
@@ -322,7 +323,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
    s = t;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(FT_THREADS)
 k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
           const float2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
           const float4 *__restrict__ kd, const int4 *__restrict__ ph, const float2 *__restrict__ zz,
@@ -333,26 +334,34 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    __shared__ float2 s_kxy[FT_ITEMS];
    __shared__ int s_k0[FT_ITEMS];
    __shared__ float4 s_kd[FT_ITEMS * KI];
-   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-   const bool live = i < N;
-   const int4 v = live ? ph[i] : make_int4(0, 0, 0, 0);
-   (void)zz;
+   // two sites per thread, FT_THREADS apart: they share every load of the
+   // per-k coefficients and the item bookkeeping
+   const int i0 = blockIdx.x * (2 * FT_THREADS) + threadIdx.x, i1 = i0 + FT_THREADS;
+   const bool live0 = i0 < N, live1 = i1 < N;
+   const int4 va = live0 ? ph[i0] : make_int4(0, 0, 0, 0);
+   const int4 vb = live1 ? ph[i1] : make_int4(0, 0, 0, 0);
    // exp(2 pi i t s_z), t = 0..KI-1, each from its exact integer phase: the
    // k-vectors of an item are seed * zp[t], so per-site phase errors do not
    // accumulate along l (the force multiplies them by |S(k)|, which is of
    // order N q at the Bragg peaks of a crystal).
-   float zc[KI], zs[KI];
+   float zca[KI], zsa[KI], zcb[KI], zsb[KI];
 #pragma unroll
    for (int t = 0; t < KI; t++) {
-      const float2 zt = zz[(size_t)i * KI + t];
-      zc[t] = live ? zt.x : 1.f;
-      zs[t] = live ? zt.y : 0.f;
+      const float2 za = live0 ? zz[(size_t)i0 * KI + t] : make_float2(1.f, 0.f);
+      const float2 zb = live1 ? zz[(size_t)i1 * KI + t] : make_float2(1.f, 0.f);
+      zca[t] = za.x;
+      zsa[t] = za.y;
+      zcb[t] = zb.x;
+      zsb[t] = zb.y;
    }
    const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
-   // compensated (Kahan) FP32 sums of the per-item force contributions: no
-   // FP64 instruction in the loop (on this part the FP64 pipe retires two
-   // lanes per clock per SM, and even a periodic FP64 fold halved the rate)
-   float fx = 0.f, fy = 0.f, fz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
+   // compensated (Kahan) FP32 sums, taken every 4 items of plain FP32
+   // partials: no FP64 instruction in the loop (on this part the FP64 pipe
+   // retires two lanes per clock per SM; a periodic FP64 fold halved the rate)
+   float fxa = 0.f, fya = 0.f, fza = 0.f, exa = 0.f, eya = 0.f, eza = 0.f;
+   float fxb = 0.f, fyb = 0.f, fzb = 0.f, exb = 0.f, eyb = 0.f, ezb = 0.f;
+   float pxa = 0.f, pya = 0.f, pza = 0.f, pxb = 0.f, pyb = 0.f, pzb = 0.f;
+   int npart = 0;
    for (int tb = a; tb < b; tb += FT_ITEMS) {
       const int nt = min(FT_ITEMS, b - tb);
       const int kb = item_k0[tb];
@@ -367,39 +376,72 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
       __syncthreads();
       for (int q = 0; q < nt; q++) {
          const int4 hd = s_it[q];
-         const unsigned int p = (unsigned int)hd.x * (unsigned int)v.x +
-                                (unsigned int)hd.y * (unsigned int)v.y +
-                                (unsigned int)hd.z * (unsigned int)v.z;
-         float s0, c0;
-         sincos_poly(p, &s0, &c0);
-         float sf = 0.f, skz = 0.f;
+         const unsigned int pa = (unsigned int)hd.x * (unsigned int)va.x +
+                                 (unsigned int)hd.y * (unsigned int)va.y +
+                                 (unsigned int)hd.z * (unsigned int)va.z;
+         const unsigned int pb = (unsigned int)hd.x * (unsigned int)vb.x +
+                                 (unsigned int)hd.y * (unsigned int)vb.y +
+                                 (unsigned int)hd.z * (unsigned int)vb.z;
+         float sa0, ca0, sb0, cb0;
+         sincos_poly(pa, &sa0, &ca0);
+         sincos_poly(pb, &sb0, &cb0);
+         float sfa = 0.f, skza = 0.f, sfb = 0.f, skzb = 0.f;
          const float4 *kq = s_kd + s_k0[q];
 #pragma unroll
          for (int t = 0; t < KI; t++) {
             if (t < hd.w) {
                const float4 k4 = kq[t];
-               const float cs = c0 * zc[t] - s0 * zs[t];
-               const float sn = fmaf(s0, zc[t], c0 * zs[t]);
-               const float f = fmaf(sn, k4.x, -cs * k4.y);
-               sf += f;
-               skz = fmaf(k4.z, f, skz);
+               const float csa = ca0 * zca[t] - sa0 * zsa[t];
+               const float sna = fmaf(sa0, zca[t], ca0 * zsa[t]);
+               const float fa = fmaf(sna, k4.x, -csa * k4.y);
+               sfa += fa;
+               skza = fmaf(k4.z, fa, skza);
+               const float csb = cb0 * zcb[t] - sb0 * zsb[t];
+               const float snb = fmaf(sb0, zcb[t], cb0 * zsb[t]);
+               const float fb = fmaf(snb, k4.x, -csb * k4.y);
+               sfb += fb;
+               skzb = fmaf(k4.z, fb, skzb);
             }
          }
          const float2 kxy = s_kxy[q];
-         kahan_add(fx, ex, kxy.x * sf);
-         kahan_add(fy, ey, kxy.y * sf);
-         kahan_add(fz, ez, skz);
+         pxa = fmaf(kxy.x, sfa, pxa);
+         pya = fmaf(kxy.y, sfa, pya);
+         pza += skza;
+         pxb = fmaf(kxy.x, sfb, pxb);
+         pyb = fmaf(kxy.y, sfb, pyb);
+         pzb += skzb;
+         if (++npart == 4) {
+            kahan_add(fxa, exa, pxa);
+            kahan_add(fya, eya, pya);
+            kahan_add(fza, eza, pza);
+            kahan_add(fxb, exb, pxb);
+            kahan_add(fyb, eyb, pyb);
+            kahan_add(fzb, ezb, pzb);
+            pxa = pya = pza = pxb = pyb = pzb = 0.f;
+            npart = 0;
+         }
       }
    }
-   if (live) {
-      const double Fx = (double)fx - (double)ex, Fy = (double)fy - (double)ey,
-                   Fz = (double)fz - (double)ez;
-      const int oi = sorted[i];   // slot i holds site oi
+   kahan_add(fxa, exa, pxa);
+   kahan_add(fya, eya, pya);
+   kahan_add(fza, eza, pza);
+   kahan_add(fxb, exb, pxb);
+   kahan_add(fyb, eyb, pyb);
+   kahan_add(fzb, ezb, pzb);
+   double *dst = fpart + (size_t)blockIdx.y * 3 * N;
+   if (live0) {
+      const int oi = sorted[i0];   // slot i0 holds site oi
       const double q = chg[oi];
-      double *dst = fpart + (size_t)blockIdx.y * 3 * N;
-      dst[oi] = q * Fx;
-      dst[N + oi] = q * Fy;
-      dst[2 * N + oi] = q * Fz;
+      dst[oi] = q * ((double)fxa - (double)exa);
+      dst[N + oi] = q * ((double)fya - (double)eya);
+      dst[2 * N + oi] = q * ((double)fza - (double)eza);
+   }
+   if (live1) {
+      const int oi = sorted[i1];
+      const double q = chg[oi];
+      dst[oi] = q * ((double)fxb - (double)exb);
+      dst[N + oi] = q * ((double)fyb - (double)eyb);
+      dst[2 * N + oi] = q * ((double)fzb - (double)ezb);
    }
 }
 
@@ -531,17 +573,21 @@ struct KsShape {
    int chunks, chunk, splits, per_split;
 };
 
-static KsShape ks_shape(int N, int nitems)
+// Chunks of the structure-factor pass and k-splits of the force pass, sized
+// for about two waves of resident threads; ipt items per thread in the
+// former, spt sites per thread in the latter.
+static KsShape ks_shape(int N, int nitems, int ipt, int spt)
 {
    KsShape s;
    const long long target = 152LL * 2048;          // resident threads on a full GB300
-   long long ch = target / (nitems > 0 ? nitems : 1);
+   const long long sf_threads = (nitems + ipt - 1) / ipt, f_threads = (N + spt - 1) / spt;
+   long long ch = target / (sf_threads > 0 ? sf_threads : 1);
    long long max_ch = (N + 63) / 64;
    if (ch < 1) ch = 1;
    if (ch > max_ch) ch = max_ch;
    s.chunk = (int)(((N + ch - 1) / ch + 31) / 32 * 32);
    s.chunks = (N + s.chunk - 1) / s.chunk;
-   long long sp = (2 * target) / (N > 0 ? N : 1);
+   long long sp = (2 * target) / (f_threads > 0 ? f_threads : 1);
    long long max_sp = (nitems + 7) / 8;
    if (sp < 1) sp = 1;
    if (sp > max_sp) sp = max_sp;
@@ -571,7 +617,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
                                            hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], mixed ? 1 : 0,
                                            d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
    CK(cudaGetLastError());
-   KsShape sh = ks_shape(N, ni);
+   KsShape sh = mixed ? ks_shape(N, ni, 1, 2) : ks_shape(N, ni, 1, 1);
    phase_mark(c, MDGPU_PH_SFAC);
    if (mixed) {
       CK(d.part32.ensure((size_t)sh.chunks * nk));
@@ -599,7 +645,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    phase_mark(c, MDGPU_PH_KFORCE);
    dim3 gf((N + 255) / 256, sh.splits);
    if (mixed)
-      k_force32<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
+      k_force32<<<gf, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
                                     d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, c->rd.sorted.p, N,
                                     d.fpart.p);
    else

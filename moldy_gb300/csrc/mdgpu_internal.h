@@ -14,6 +14,7 @@ namespace mdgpu {
 
 constexpr int NPOTP = 8;          // parameters per potential (src/defs.h:144)
 constexpr int KI = 16;            // k-vectors per k-space work item
+constexpr int FT_THREADS = 128;   // k_force32: threads per block, two sites each
 constexpr double PI = 3.14159265358979323846;
 constexpr double ALPHAMIN = 1e-7; // src/defs.h:181
 constexpr double TOO_CLOSE = 0.25;// r^2 warning threshold, src/force.c:89

@@ -264,7 +264,8 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    if (splits < 1) splits = 1;
    const int per_split = (ni + splits - 1) / splits;
    splits = (ni + per_split - 1) / per_split;
-   k_force32<<<dim3((N + 255) / 256, splits), 256, 0, st>>>(item, k0, kxy, ni, nk, per_split, kdat, ph, zp,
+   k_force32<<<dim3((N + 2 * FT_THREADS - 1) / (2 * FT_THREADS), splits), FT_THREADS, 0, st>>>(
+      item, k0, kxy, ni, nk, per_split, kdat, ph, zp,
                                                            d_chg, sorted, N, fpart);
    k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, splits, fpart, d_force, 1);
    k_add_energy<<<1, 32, 0, st>>>(out, d_pe, d_stress);
