@@ -189,6 +189,53 @@ mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, const doubl
                                         double *d_force, double *d_pe, double *d_stress,
                                         void *stream);
 
+/* ---- Adjoint: parameter gradients.  No counterpart in the reference. -----
+ *
+ * The parameters are the potential table (max_id*max_id*MDGPU_NPOTP
+ * doubles, the layout of mdgpu_system.potpar), the per-site charges
+ * (nsites, program units) and the Ewald alpha; the cutoffs and the k-vector
+ * list stay fixed.  Table entry [a][b] is the one the force on a site of
+ * identifier a from a site of identifier b reads: for a symmetric table the
+ * derivative with respect to a shared parameter p_ab = p_ba (a != b) is
+ * grad[a][b][k] + grad[b][a][k].  Entries k beyond the potential type's
+ * parameter count read 0.  The energy is pe[0] + pe[1] of mdgpu_forces; the
+ * force-matching loss of reference forces f_ref is
+ *    L = weight * sum_i |F_i - f_ref_i|^2
+ * and its gradient sum_i 2 weight (F_i - f_ref_i) . dF_i/dtheta comes from
+ * Hessian-vector products through the real-space pairs (their link-cell walk
+ * recomputed, no stored pair list) and the k-space sum.  Both calls run the
+ * forward evaluation first, in the context's precision.  Limits: max_id <=
+ * MDGPU_ADJ_MAX_ID; in strict-cutoff mode no molecule may be larger than the
+ * cutoff (MDGPU_E_UNSUPPORTED otherwise). */
+#define MDGPU_NPOTP 8
+#define MDGPU_ADJ_MAX_ID 16
+typedef struct {
+   const double *potpar;        /* [max_id*max_id][8] or NULL: unchanged      */
+   const double *chg;           /* [nsites] or NULL: unchanged                */
+   double alpha;                /* > 0: new alpha; <= 0: unchanged            */
+} mdgpu_params;
+
+typedef struct {
+   double *potpar;              /* out [max_id*max_id][8], or NULL            */
+   double *chg;                 /* out [nsites], or NULL                      */
+   double alpha;                /* out                                        */
+} mdgpu_grad;
+
+/* Replaces the parameters of the system and control record. */
+mdgpu_status mdgpu_set_params(mdgpu_ctx *ctx, const mdgpu_params *params);
+
+/* Energy and its gradient at params (NULL: the current ones) for the
+ * configuration site_soa [3][nsites] (c_of_m as for mdgpu_forces). */
+mdgpu_status mdgpu_energy_grad(mdgpu_ctx *ctx, const mdgpu_params *params, const double *h,
+                               const double *site_soa, const double *c_of_m, double *energy,
+                               mdgpu_grad *grad);
+
+/* Force-matching loss against f_ref_soa [3][nsites] and its gradient. */
+mdgpu_status mdgpu_fm_loss_grad(mdgpu_ctx *ctx, const mdgpu_params *params, const double *h,
+                                const double *site_soa, const double *c_of_m,
+                                const double *f_ref_soa, double weight, double *loss,
+                                mdgpu_grad *grad);
+
 /* Measures the device's dense FMA throughput (TFLOP/s, FMA = 2 flops) in
  * FP32 (fp64 = 0) or FP64: the roofline denominators of the force kernels,
  * whose bound is the FMA pipe.  No counterpart in the reference. */

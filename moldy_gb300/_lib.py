@@ -22,7 +22,8 @@ EXPORTS = ["mdgpu_create", "mdgpu_destroy", "mdgpu_last_error", "mdgpu_set_preci
            "mdgpu_force_calc", "mdgpu_ewald", "mdgpu_forces", "mdgpu_forces_device",
            "mdgpu_synchronize", "mdgpu_get_info", "mdgpu_pair_keys", "mdgpu_poteval",
            "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak",
-           "mdgpu_ewald_kspace_noalloc",
+           "mdgpu_ewald_kspace_noalloc", "mdgpu_set_params", "mdgpu_energy_grad",
+           "mdgpu_fm_loss_grad",
            "force_calc", "ewald", "poteval"]
 
 
@@ -55,6 +56,16 @@ class Info(C.Structure):
                 ("too_close", (C.c_int32 * 2) * 16), ("launches", C.c_int64)]
 
 
+class Params(C.Structure):
+    _fields_ = [("potpar", C.POINTER(C.c_double)), ("chg", C.POINTER(C.c_double)), ("alpha", C.c_double)]
+
+
+class Grad(C.Structure):
+    _fields_ = [("potpar", C.POINTER(C.c_double)), ("chg", C.POINTER(C.c_double)), ("alpha", C.c_double)]
+
+
+NPOTP = 8
+ADJ_MAX_ID = 16
 NPHASES = 7
 PHASES = ["cells", "pairs", "kprep", "sfac", "kreduce", "kforce", "final"]
 
@@ -95,6 +106,9 @@ def load():
         "mdgpu_phase_times": ([vp, dp], ip),
         "mdgpu_fma_peak": ([ip, ip, dp], ip),
         "mdgpu_ewald_kspace_noalloc": ([dp, ip, vp, vp, C.c_double, C.c_double, vp, vp, vp, vp], ip),
+        "mdgpu_set_params": ([vp, C.POINTER(Params)], ip),
+        "mdgpu_energy_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.POINTER(Grad)], ip),
+        "mdgpu_fm_loss_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.c_double, dp, C.POINTER(Grad)], ip),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -121,7 +121,7 @@ static mdgpu_status check_h(mdgpu_ctx *c, const double *h)
 
 // Cell geometry and k-list for this h and control, rebuilt only when either
 // changed; the first-call constants on first use after set_system.
-static mdgpu_status ensure_ready(mdgpu_ctx *c, const double *h, bool need_rs, bool need_ks)
+mdgpu_status mdgpu::ensure_ready(mdgpu_ctx *c, const double *h, bool need_rs, bool need_ks)
 {
    if (!c->have_system) return fail(c, MDGPU_E_ARG, "mdgpu_set_system has not been called");
    if (!c->have_control) return fail(c, MDGPU_E_ARG, "mdgpu_set_control has not been called");
@@ -214,7 +214,7 @@ static void fill_info(mdgpu_ctx *c)
 }
 
 // Copies the device result record back and reports device-side errors.
-static mdgpu_status sync_out(mdgpu_ctx *c)
+mdgpu_status mdgpu::sync_out(mdgpu_ctx *c)
 {
    cudaError_t e = cudaMemcpyAsync(c->h_out, c->out.p, sizeof(DevOut), cudaMemcpyDeviceToHost, c->stream);
    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -287,6 +287,11 @@ void mdgpu_destroy(mdgpu_ctx *c)
    k.kz64.release(); k.coeff.release(); k.coeff2.release(); k.kdat32.release(); k.kdat64.release();
    k.ph32.release(); k.z32.release(); k.zp32.release(); k.ph64a.release(); k.ph64b.release(); k.z64.release();
    k.part32.release(); k.part64.release(); k.fpart.release(); k.blk.release();
+   AdjDev &a = c->ad;
+   a.res64.release(); a.res32.release(); a.fref.release(); a.gq.release(); a.gpart.release();
+   a.slots.release(); a.scal.release(); a.lpart.release(); a.phv32.release(); a.phv64.release();
+   a.partv32.release(); a.partv64.release(); a.kadj32.release(); a.kadj64.release(); a.kz32.release();
+   a.gkpart.release(); a.blk.release();
    c->site.release(); c->force.release(); c->force_in.release(); c->cofm_in.release(); c->out.release();
    c->small.release();
    if (c->h_out) cudaFreeHost(c->h_out);

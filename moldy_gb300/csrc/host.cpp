@@ -410,6 +410,60 @@ static double as_erf(double x)
    return -as_erf(-x);
 }
 
+// d/dx of the A&S erfc approximation t P(t) e^{-x^2}, t = 1/(1 + p x), x >= 0.
+static double as_derfc(double x)
+{
+   const double t = 1.0 / (1.0 + ASP * x);
+   const double pt = AS1 + t * (AS2 + t * (AS3 + t * (AS4 + t * AS5)));
+   const double dpt = AS2 + t * (2.0 * AS3 + t * (3.0 * AS4 + t * 4.0 * AS5));
+   return std::exp(-x * x) * (-ASP * t * t * (pt + t * dpt) - 2.0 * x * t * pt);
+}
+
+// Gradient of the energy terms ewald() adds besides the k sum,
+// -self + sheet/V (src/ewald.c:367-433): with respect to each site charge
+// (added into g_chg[nsites]) and alpha (added into *g_alpha).  The
+// intramolecular part of the self energy is taken per molecule with its own
+// charges (the reference evaluates the first molecule of each species, whose
+// charges every molecule of the species shares).
+void ewald_self_sheet_grad(const std::vector<mdgpu_species> &spec, const std::vector<double> &spec_pf,
+                           const std::vector<double> &chg, double alpha, double vol, double *g_chg,
+                           double *g_alpha)
+{
+   const double rpi = 1.0 / std::sqrt(PI);
+   double ga = 0.0, sq = 0.0;
+   size_t isite = 0, so = 0;
+   for (const auto &sp : spec) {
+      const int ns = sp.nsites;
+      const double *pf = spec_pf.data() + 3 * so;
+      for (int m = 0; m < sp.nmols; m++) {
+         const double *q = chg.data() + isite;
+         for (int a = 0; a < ns; a++) {
+            g_chg[isite + a] -= 2.0 * alpha * rpi * q[a];
+            ga -= rpi * q[a] * q[a];
+            sq += q[a];
+            for (int b = a + 1; b < ns; b++) {
+               const double *u = pf + 3 * a, *v = pf + 3 * b;
+               const double r = std::sqrt((u[0] - v[0]) * (u[0] - v[0]) + (u[1] - v[1]) * (u[1] - v[1]) +
+                                          (u[2] - v[2]) * (u[2] - v[2]));
+               const double e = as_erf(alpha * r) / r;
+               g_chg[isite + a] -= q[b] * e;
+               g_chg[isite + b] -= q[a] * e;
+               ga += q[a] * q[b] * as_derfc(alpha * r);   // d erf/dx = -d erfc/dx
+            }
+         }
+         isite += ns;
+      }
+      so += ns;
+   }
+   const double conv_q = (4.07497263794495e-14 * 1.0e-3 * 1.05482230112e-05) / 1.60217733e-19;
+   if (std::fabs(sq) * conv_q > 1.0e-5) {   // sheet = -pi (sum q)^2 / (2 alpha^2)
+      const double dq = -PI * sq / (alpha * alpha * vol);
+      for (size_t i = 0; i < isite; i++) g_chg[i] += dq;
+      ga += PI * sq * sq / (alpha * alpha * alpha * vol);
+   }
+   *g_alpha += ga;
+}
+
 // Ewald self energy and charged-system sheet correction (src/ewald.c:367-425).
 void ewald_self_sheet(const std::vector<mdgpu_species> &spec, const std::vector<double> &spec_pf,
                       const std::vector<double> &chg, double alpha, double *self, double *sheet,

@@ -30,6 +30,7 @@
 #include <cstring>
 
 #include "mdgpu_internal.h"
+#include "phase.cuh"
 
 namespace mdgpu {
 
@@ -42,7 +43,6 @@ __device__ __forceinline__ unsigned long long to_fixed64(double s)
 }
 
 __device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c);
-__device__ __forceinline__ void sincos_poly(unsigned int p, float *s, float *c);
 
 // Per-site records are written in link-cell order (slot i holds site
 // sorted[i]): the structure-factor chunks are then compact regions of the
@@ -99,34 +99,6 @@ __device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c)
    *s = fmaf(c0, d, s0);
 }
 
-// exp(2 pi i p / 2^32) by quadrant reduction of the integer phase and
-// polynomials in the reduced phase x in [-1/8, 1/8) revolution:
-// sin(2 pi x) = x P(x^2) (degree 9), cos(2 pi x) = Q(x^2) (degree 8), with
-// coefficients fitted by (weighted) least squares on Chebyshev nodes and
-// rounded to FP32; max abs error about 1e-7 over the interval.
-__device__ __forceinline__ void sincos_poly(unsigned int p, float *s, float *c)
-{
-   const unsigned int qd = (p + 0x20000000u) >> 30;
-   const int r = (int)(p - (qd << 30));
-   const float x = (float)r * 2.3283064365386963e-10f;   // 2^-32
-   const float x2 = x * x;
-   float ps = fmaf(fmaf(fmaf(fmaf(41.46983337402344f, x2, -76.69776916503906f), x2, 81.6052017211914f),
-                        x2, -41.34170150756836f), x2, 6.2831854820251465f);
-   float sn = ps * x;
-   float cs = fmaf(fmaf(fmaf(fmaf(59.22028732299805f, x2, -85.4428482055664f), x2, 64.93931579589844f),
-                        x2, -19.739208221435547f), x2, 1.0f);
-   if (qd & 1u) {
-      const float t = sn;
-      sn = cs;
-      cs = -t;
-   }
-   if (qd & 2u) {
-      sn = -sn;
-      cs = -cs;
-   }
-   *s = sn;
-   *c = cs;
-}
 
 // ---------------------------------------------------------------- S(k)
 constexpr int SF_TILE = 128;
@@ -569,14 +541,10 @@ mdgpu_status ks_prepare(mdgpu_ctx *c)
    return MDGPU_OK;
 }
 
-struct KsShape {
-   int chunks, chunk, splits, per_split;
-};
-
 // Chunks of the structure-factor pass and k-splits of the force pass, sized
 // for about two waves of resident threads; ipt items per thread in the
 // former, spt sites per thread in the latter.
-static KsShape ks_shape(int N, int nitems, int ipt, int spt)
+KsShape ks_shape(int N, int nitems, int ipt, int spt)
 {
    KsShape s;
    const long long target = 152LL * 2048;          // resident threads on a full GB300

@@ -63,6 +63,9 @@ double intramolecular_energy(const std::vector<mdgpu_species> &spec,
 void ewald_self_sheet(const std::vector<mdgpu_species> &spec, const std::vector<double> &spec_pf,
                       const std::vector<double> &chg, double alpha, double *self,
                       double *sheet, int *nsitesxf);
+void ewald_self_sheet_grad(const std::vector<mdgpu_species> &spec, const std::vector<double> &spec_pf,
+                           const std::vector<double> &chg, double alpha, double vol, double *g_chg,
+                           double *g_alpha);
 double det3(const double *a);
 void inv3(const double *a, double *b);
 
@@ -135,6 +138,27 @@ struct KsDev {
    DBuf<double> blk;       // per-block energy/stress partials
 };
 
+// Buffers of the adjoint (parameter-gradient) passes.
+struct AdjDev {
+   DBuf<double4> res64;    // per slot: residual weight v of the site (FP64 form)
+   DBuf<float4> res32;     // per slot: the same in FP32 (mixed form)
+   DBuf<double> fref;      // [3][N] reference forces
+   DBuf<double> gq;        // [2][N] dE/dq, dG/dq per site
+   DBuf<double> gpart;     // per-block real-space gradient slots
+   DBuf<double> slots;     // summed real-space slots
+   DBuf<double> scal;      // loss, k-space dE/dalpha, dG/dalpha
+   DBuf<double> lpart;     // per-block loss partials
+   DBuf<int4> phv32;       // [3][N] mixed-form phases with weight q v_a
+   DBuf<ulonglong2> phv64; // [3][N] (u_z, weight q v_a) for the FP64 form
+   DBuf<float2> partv32;   // [3][chunks][nk] weighted structure-factor partials
+   DBuf<double2> partv64;
+   DBuf<float4> kadj32;    // per k: A, B, P, Q
+   DBuf<double4> kadj64;
+   DBuf<float> kz32;       // per k: k_z
+   DBuf<double> gkpart;    // [splits][2][N] k-space charge-gradient partials
+   DBuf<double> blk;       // per-block k-space dE/dalpha, dG/dalpha
+};
+
 }  // namespace mdgpu
 
 struct mdgpu_ctx {
@@ -167,6 +191,7 @@ struct mdgpu_ctx {
 
    mdgpu::RsDev rd;
    mdgpu::KsDev kd;
+   mdgpu::AdjDev ad;
    mdgpu::DBuf<double> site, force, force_in, cofm_in, small;
    const double *cur_site = nullptr;   // site array of the launch in progress
    std::vector<double> last_cofm;      // centres of mass of the last force_calc
@@ -192,12 +217,28 @@ mdgpu_status rs_prepare(mdgpu_ctx *c);   // upload geometry/system tables
 mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
                        double *d_force, bool cells_only, unsigned long long *d_keys,
                        int64_t key_cap, int64_t *d_keycount);
+// Real-space adjoint over the slots binned by the last rs_launch: gradients
+// into c->ad.gq ([2][N], written) and c->ad.slots; residual weights from
+// c->ad.res64/res32 when loss.
+mdgpu_status rs_adjoint(mdgpu_ctx *c, bool loss);
+int pot_nparams(int ptype);     // parameters the potential type reads
 // kspace.cu
 mdgpu_status ks_prepare(mdgpu_ctx *c);
 mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate);
+struct KsShape {
+   int chunks, chunk, splits, per_split;
+};
+// Chunks of the structure-factor pass and k-splits of a per-site pass
+// (ipt items per thread, spt sites per thread).
+KsShape ks_shape(int N, int nitems, int ipt, int spt);
 // api.cu
 mdgpu_status fail(mdgpu_ctx *c, mdgpu_status s, const std::string &msg);
 mdgpu_status cuda_check(mdgpu_ctx *c, cudaError_t e, const char *what);
+// Cell geometry, k-list and first-call constants current for h and the
+// control record, device tables uploaded.
+mdgpu_status ensure_ready(mdgpu_ctx *c, const double *h, bool need_rs, bool need_ks);
+// Copies the device result record back, waits, reports device-side errors.
+mdgpu_status sync_out(mdgpu_ctx *c);
 
 // Marks the boundary before phase `i` (MDGPU_NPHASES marks the end).
 inline void phase_mark(mdgpu_ctx *c, int i)

@@ -1,0 +1,37 @@
+// Device helpers shared by the reciprocal-space kernels (kspace.cu) and
+// their adjoint (adjoint.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace mdgpu {
+
+// exp(2 pi i p / 2^32) by quadrant reduction of the integer phase and
+// polynomials in the reduced phase x in [-1/8, 1/8) revolution:
+// sin(2 pi x) = x P(x^2) (degree 9), cos(2 pi x) = Q(x^2) (degree 8), with
+// coefficients fitted by (weighted) least squares on Chebyshev nodes and
+// rounded to FP32; max abs error about 1e-7 over the interval.
+__device__ __forceinline__ void sincos_poly(unsigned int p, float *s, float *c)
+{
+   const unsigned int qd = (p + 0x20000000u) >> 30;
+   const int r = (int)(p - (qd << 30));
+   const float x = (float)r * 2.3283064365386963e-10f;   // 2^-32
+   const float x2 = x * x;
+   float ps = fmaf(fmaf(fmaf(fmaf(41.46983337402344f, x2, -76.69776916503906f), x2, 81.6052017211914f),
+                        x2, -41.34170150756836f), x2, 6.2831854820251465f);
+   float sn = ps * x;
+   float cs = fmaf(fmaf(fmaf(fmaf(59.22028732299805f, x2, -85.4428482055664f), x2, 64.93931579589844f),
+                        x2, -19.739208221435547f), x2, 1.0f);
+   if (qd & 1u) {
+      const float t = sn;
+      sn = cs;
+      cs = -t;
+   }
+   if (qd & 2u) {
+      sn = -sn;
+      cs = -cs;
+   }
+   *s = sn;
+   *c = cs;
+}
+
+}  // namespace mdgpu

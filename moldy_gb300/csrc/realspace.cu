@@ -42,6 +42,13 @@ struct RsParams {
    float cut2f, bandf, alphaf, normf;
 };
 
+// Launch parameters of the real-space adjoint.
+struct AdjParams {
+   int loss;              // nonzero: residual weights given, loss terms wanted
+   unsigned type_mask;    // bit b set: some site has identifier b
+   int nslot;             // 2 max_id^2 NP + 2 gradient slots
+};
+
 // ---------------------------------------------------------------- binning
 __device__ __forceinline__ int cellbin_dev(double s, int n, double fn, int *bad)
 {
@@ -345,6 +352,139 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh)
    return s;   // valid in thread 0
 }
 
+constexpr int PAIR_WARPS = 8;   // warps per block
+
+// Per-warp shared rows of the stencil walk.
+struct WalkRows {
+   int *inc, *jb, *info;
+   float4 *oh, *ol;
+};
+
+// Walks the full stencil of home slot p (in cell c) with one warp and calls
+// visit(j, k, kimg) for every candidate slot j, the home site itself
+// excluded: k is the lane whose stencil entry j belongs to (its cell-offset
+// vectors are rows.oh[k], rows.ol[k]) and kimg the periodic image code.
+template <bool MIXED, class Visit>
+__device__ __forceinline__ void walk_stencil(const RsParams &P, int p, int c, int lane,
+                                             const int *__restrict__ cell_start,
+                                             const int4 *__restrict__ full,
+                                             const float4 *__restrict__ off_hi,
+                                             const float4 *__restrict__ off_lo, const WalkRows &rows,
+                                             Visit &&visit)
+{
+   const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
+   for (int base = 0; base < P.nfull; base += 32) {
+      // lane `lane` takes stencil entry base + lane
+      const int e = base + lane;
+      int cnt = 0, jb = 0, info = 0;
+      float4 oh = make_float4(0, 0, 0, 0), ol = oh;
+      if (e < P.nfull) {
+         const int4 d = __ldg(&full[e]);
+         int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
+         const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
+         const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
+         const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
+         bx -= ix * P.nx;
+         by -= iy * P.ny;
+         bz -= iz * P.nz;
+         const int cb = bz + P.nz * (by + P.ny * bx);
+         const int j0 = __ldg(&cell_start[cb]);
+         cnt = __ldg(&cell_start[cb + 1]) - j0;
+         jb = j0;
+         info = (9 * (ix + 1) + 3 * (iy + 1) + (iz + 1)) | (d.w << 8);
+         if (MIXED) {
+            oh = __ldg(&off_hi[e]);
+            ol = __ldg(&off_lo[e]);
+         }
+      }
+      const int inc = warp_incl_scan(cnt);
+      const int T = __shfl_sync(0xffffffffu, inc, 31);
+      rows.inc[lane] = inc;
+      rows.jb[lane] = jb - (inc - cnt);     // slot = jb[k] + candidate index
+      rows.info[lane] = info;
+      if (MIXED) {
+         rows.oh[lane] = oh;
+         rows.ol[lane] = ol;
+      }
+      __syncwarp();
+      for (int r = 0; r < T; r += 32) {
+         const int idx = r + lane;
+         if (idx < T) {
+            int k = 0;
+#pragma unroll
+            for (int s = 16; s >= 1; s >>= 1)
+               if (rows.inc[k + s - 1] <= idx) k += s;
+            const int j = rows.jb[k] + idx;
+            const int inf = rows.info[k];
+            if (!((inf >> 8) && j == p)) visit(j, k, inf & 255);
+         }
+      }
+      __syncwarp();
+   }
+}
+
+// Separation r = x_j - x_i (+ image) from the home site to slot j, r^2 and
+// q_j.  FP64 form: the reference's operation order, no fused multiply-adds.
+// Mixed form: cell-relative FP32 co-ordinates plus the exact cell offset as
+// an FP32 (hi, lo) pair.
+template <bool MIXED, typename R>
+__device__ __forceinline__ void pair_sep(const RsParams &P, int j, int k, int kimg, const WalkRows &rows,
+                                         const float4 &xi32, const double4 &xi64,
+                                         const double4 *__restrict__ pos64,
+                                         const float4 *__restrict__ pos32, R &rx, R &ry, R &rz, R &r2,
+                                         R &qj)
+{
+   if (MIXED) {
+      const float4 xj = __ldg(&pos32[j]);
+      const float4 h4 = rows.oh[k], l4 = rows.ol[k];
+      rx = (h4.x + (xj.x - xi32.x)) + l4.x;
+      ry = (h4.y + (xj.y - xi32.y)) + l4.y;
+      rz = (h4.z + (xj.z - xi32.z)) + l4.z;
+      r2 = rx * rx + ry * ry + rz * rz;
+      qj = xj.w;
+   } else {
+      const double4 xj = pos64[j];
+      const double *rl = P.reloc[kimg];
+      rx = __dadd_rn(__dsub_rn(xj.x, xi64.x), rl[0]);
+      ry = __dadd_rn(__dsub_rn(xj.y, xi64.y), rl[1]);
+      rz = __dadd_rn(__dsub_rn(xj.z, xi64.z), rl[2]);
+      r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+      qj = xj.w;
+   }
+}
+
+// Threshold decisions (too-close warning, strict-cutoff clamp).  FP64 form:
+// exact, on the reference's r^2.  Mixed form: on the FP32 r^2, except
+// within a narrow band of either threshold, where r^2 is re-formed in FP64
+// from the original co-ordinates (rare).
+template <bool MIXED, typename R>
+__device__ __forceinline__ void pair_flags(const RsParams &P, R r2, int oi, int j, int kimg,
+                                           const int *__restrict__ sorted, const double *__restrict__ site,
+                                           bool &too_close, bool &clip)
+{
+   if (MIXED) {
+      const int N = P.nsites;
+      const float r2f = (float)r2;
+      const bool near_clip = P.strict && !P.molpbc && fabsf(r2f - P.cut2f) < P.bandf * P.cut2f;
+      const bool near_close = fabsf(r2f - (float)TOO_CLOSE) < 1e-3f;
+      too_close = r2f < (float)TOO_CLOSE;
+      clip = P.strict && !P.molpbc && r2f > P.cut2f;
+      if (near_clip || near_close) {
+         const int oj = sorted[j];
+         const double *rl = P.reloc[kimg];
+         double ax = __dadd_rn(__dsub_rn(site[oj], site[oi]), rl[0]);
+         double ay = __dadd_rn(__dsub_rn(site[N + oj], site[N + oi]), rl[1]);
+         double az = __dadd_rn(__dsub_rn(site[2 * N + oj], site[2 * N + oi]), rl[2]);
+         const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az));
+         too_close = d2 < TOO_CLOSE;
+         clip = P.strict && !P.molpbc && d2 > P.cut2;
+      }
+   } else {
+      too_close = (double)r2 < TOO_CLOSE;
+      clip = P.strict && !P.molpbc && (double)r2 > P.cut2;
+   }
+}
+
 // MODE 0: forces/energy/virial; MODE 1: emit canonical pair keys only.
 //
 // One warp per home site.  The warp walks the full stencil 32 entries at a
@@ -354,8 +494,6 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh)
 // candidate's stencil entry by binary search over the scanned counts.  Every
 // lane runs the same pair arithmetic on a different candidate, so the warp
 // stays converged however unevenly the sites are spread over the cells.
-constexpr int PAIR_WARPS = 8;   // warps per block
-
 template <int PT, bool EW, bool MIXED, int MODE>
 __global__ void __launch_bounds__(PAIR_WARPS * 32)
 k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ slot_cell,
@@ -384,12 +522,13 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
    const int N = P.nsites;
    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
    const int p = blockIdx.x * PAIR_WARPS + w;   // home slot of this warp
+   const WalkRows rows{s_inc[w], s_jb[w], s_info[w], s_oh[w], s_ol[w]};
    // per-lane partial sums: few terms each, then a warp tree reduction
    R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
-   long long nev = 0;
+   int nev = 0;                                  // evaluations by this lane
+   const R cut100 = (R)P.cut100;
    if (p < N) {
       const int c = slot_cell[p];
-      const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
       const int2 ti = tag[p];
       const R *prow = pot + (size_t)ti.x * P.max_id * NPOTP;
       double4 xi64 = make_double4(0, 0, 0, 0);
@@ -398,148 +537,58 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
       const R qi = MIXED ? (R)xi32.w : (R)xi64.w;
       const R alpha = MIXED ? (R)P.alphaf : (R)P.alpha, norm = MIXED ? (R)P.normf : (R)P.norm;
       const int oi = sorted[p];
-      for (int base = 0; base < P.nfull; base += 32) {
-         // lane `lane` takes stencil entry base + lane
-         const int e = base + lane;
-         int cnt = 0, jb = 0, info = 0;
-         float4 oh = make_float4(0, 0, 0, 0), ol = oh;
-         if (e < P.nfull) {
-            const int4 d = __ldg(&full[e]);
-            int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
-            const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
-            const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
-            const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
-            bx -= ix * P.nx;
-            by -= iy * P.ny;
-            bz -= iz * P.nz;
-            const int cb = bz + P.nz * (by + P.ny * bx);
-            const int j0 = __ldg(&cell_start[cb]);
-            cnt = __ldg(&cell_start[cb + 1]) - j0;
-            jb = j0;
-            info = (9 * (ix + 1) + 3 * (iy + 1) + (iz + 1)) | (d.w << 8);
-            if (MIXED) {
-               oh = __ldg(&off_hi[e]);
-               ol = __ldg(&off_lo[e]);
+      walk_stencil<MIXED>(P, p, c, lane, cell_start, full, off_hi, off_lo, rows, [&](int j, int k, int kimg) {
+         R rx, ry, rz, r2, qj;
+         const int2 tj = __ldg(&tag[j]);
+         pair_sep<MIXED>(P, j, k, kimg, rows, xi32, xi64, pos64, pos32, rx, ry, rz, r2, qj);
+         if (MODE == 1) {
+            const long long a = oi, bb = sorted[j];
+            if (a < bb || (a == bb && kimg < 13)) {
+               unsigned long long key = ((unsigned long long)a << 37) |
+                                        ((unsigned long long)bb << 5) | (unsigned long long)kimg;
+               unsigned long long slot = atomicAdd((unsigned long long *)&out->npairs2, 1ull);
+               if ((long long)slot < key_cap) keys[slot] = key;
             }
+            return;
          }
-         const int inc = warp_incl_scan(cnt);
-         const int T = __shfl_sync(0xffffffffu, inc, 31);
-         s_inc[w][lane] = inc;
-         s_jb[w][lane] = jb - (inc - cnt);     // slot = s_jb[k] + candidate index
-         s_info[w][lane] = info;
-         if (MIXED) {
-            s_oh[w][lane] = oh;
-            s_ol[w][lane] = ol;
+         const bool intra = ti.y == tj.y;
+         bool too_close, clip;
+         pair_flags<MIXED>(P, r2, oi, j, kimg, sorted, site, too_close, clip);
+         if (too_close && !intra) {
+            const int oj = sorted[j];
+            if (oi < oj) note_too_close(out, oi, oj);
          }
-         __syncwarp();
-         for (int r = 0; r < T; r += 32) {
-            const int idx = r + lane;
-            if (idx < T) {
-               int k = 0;
+         const R r2a = r2;
+         if (clip) r2 = cut100;
+         R pp[NP];
+         const R *pj = prow + (size_t)tj.x * NPOTP;
 #pragma unroll
-               for (int s = 16; s >= 1; s >>= 1)
-                  if (s_inc[w][k + s - 1] <= idx) k += s;
-               const int j = s_jb[w][k] + idx;
-               const int inf = s_info[w][k];
-               const int kimg = inf & 255;
-               if (!((inf >> 8) && j == p)) {
-                  R rx, ry, rz, r2, qj;
-                  const int2 tj = __ldg(&tag[j]);
-                  if (MIXED) {
-                     const float4 xj = __ldg(&pos32[j]);
-                     const float4 h4 = s_oh[w][k], l4 = s_ol[w][k];
-                     rx = (h4.x + (xj.x - xi32.x)) + l4.x;
-                     ry = (h4.y + (xj.y - xi32.y)) + l4.y;
-                     rz = (h4.z + (xj.z - xi32.z)) + l4.z;
-                     r2 = rx * rx + ry * ry + rz * rz;
-                     qj = xj.w;
-                  } else {
-                     const double4 xj = pos64[j];
-                     const double *rl = P.reloc[kimg];
-                     rx = __dadd_rn(__dsub_rn(xj.x, xi64.x), rl[0]);
-                     ry = __dadd_rn(__dsub_rn(xj.y, xi64.y), rl[1]);
-                     rz = __dadd_rn(__dsub_rn(xj.z, xi64.z), rl[2]);
-                     r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
-                     qj = xj.w;
-                  }
-                  if (MODE == 1) {
-                     const long long a = oi, bb = sorted[j];
-                     if (a < bb || (a == bb && kimg < 13)) {
-                        unsigned long long key = ((unsigned long long)a << 37) |
-                                                 ((unsigned long long)bb << 5) | (unsigned long long)kimg;
-                        unsigned long long slot = atomicAdd((unsigned long long *)&out->npairs2, 1ull);
-                        if ((long long)slot < key_cap) keys[slot] = key;
-                     }
-                  } else {
-                     // Threshold decisions (too-close warning, strict-cutoff
-                     // clamp).  FP64 form: exact, on the reference's r^2.
-                     // Mixed form: on the FP32 r^2, except within a narrow
-                     // band of either threshold, where r^2 is re-formed in
-                     // FP64 from the original co-ordinates (rare).
-                     const bool intra = ti.y == tj.y;
-                     bool too_close, clip;
-                     if (MIXED) {
-                        const float r2f = (float)r2;
-                        const bool near_clip = P.strict && !P.molpbc && fabsf(r2f - P.cut2f) < P.bandf * P.cut2f;
-                        const bool near_close = fabsf(r2f - (float)TOO_CLOSE) < 1e-3f;
-                        too_close = r2f < (float)TOO_CLOSE;
-                        clip = P.strict && !P.molpbc && r2f > P.cut2f;
-                        if (near_clip || near_close) {
-                           const int oj = sorted[j];
-                           const double *rl = P.reloc[kimg];
-                           double ax = __dadd_rn(__dsub_rn(site[oj], site[oi]), rl[0]);
-                           double ay = __dadd_rn(__dsub_rn(site[N + oj], site[N + oi]), rl[1]);
-                           double az = __dadd_rn(__dsub_rn(site[2 * N + oj], site[2 * N + oi]), rl[2]);
-                           const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)),
-                                                       __dmul_rn(az, az));
-                           too_close = d2 < TOO_CLOSE;
-                           clip = P.strict && !P.molpbc && d2 > P.cut2;
-                        }
-                     } else {
-                        too_close = (double)r2 < TOO_CLOSE;
-                        clip = P.strict && !P.molpbc && (double)r2 > P.cut2;
-                     }
-                     if (too_close && !intra) {
-                        const int oj = sorted[j];
-                        if (oi < oj) note_too_close(out, oi, oj);
-                     }
-                     const R r2a = r2;
-                     if (clip) r2 = (R)P.cut100;
-                     R pp[NP];
-                     const R *pj = prow + (size_t)tj.x * NPOTP;
-#pragma unroll
-                     for (int q = 0; q < NP; q++) pp[q] = pj[q];
-                     R f, u;
-                     pair_fu<PT, EW, R>(r2, qj * qi, pp, alpha, norm, f, u);
-                     if (MIXED && intra) {
-                        // Mixed form: an intramolecular pair's energy is
-                        // exactly what the intramolecular correction subtracts
-                        // again, so it is left out of both (FP32 roundings of
-                        // identical molecules would add up coherently instead
-                        // of cancelling); a clamped pair keeps the difference
-                        // between its clamped and true energies.
-                        R fa, ua = R(0);
-                        if (clip) pair_fu<PT, EW, R>(r2a, qj * qi, pp, alpha, norm, fa, ua);
-                        u = clip ? u - ua : R(0);
-                     }
-                     const R hf = R(0.5) * f;
-                     fx -= f * rx;
-                     fy -= f * ry;
-                     fz -= f * rz;
-                     pe += R(0.5) * u;
-                     v0 += hf * rx * rx;
-                     v1 += hf * rx * ry;
-                     v2 += hf * rx * rz;
-                     v3 += hf * ry * ry;
-                     v4 += hf * ry * rz;
-                     v5 += hf * rz * rz;
-                     nev++;
-                  }
-               }
-            }
+         for (int q = 0; q < NP; q++) pp[q] = pj[q];
+         R f, u;
+         pair_fu<PT, EW, R>(r2, qj * qi, pp, alpha, norm, f, u);
+         if (MIXED && intra) {
+            // Mixed form: an intramolecular pair's energy is exactly what
+            // the intramolecular correction subtracts again, so it is left
+            // out of both (FP32 roundings of identical molecules would add
+            // up coherently instead of cancelling); a clamped pair keeps the
+            // difference between its clamped and true energies.
+            R fa, ua = R(0);
+            if (clip) pair_fu<PT, EW, R>(r2a, qj * qi, pp, alpha, norm, fa, ua);
+            u = clip ? u - ua : R(0);
          }
-         __syncwarp();
-      }
+         const R hf = R(0.5) * f;
+         fx -= f * rx;
+         fy -= f * ry;
+         fz -= f * rz;
+         pe += R(0.5) * u;
+         v0 += hf * rx * rx;
+         v1 += hf * rx * ry;
+         v2 += hf * rx * rz;
+         v3 += hf * ry * ry;
+         v4 += hf * ry * rz;
+         v5 += hf * rz * rz;
+         nev++;
+      });
       if (MODE == 0) {
          // warp tree reduction of the home site's force, in the working
          // precision (each lane holds a sum of a few pairs)
@@ -603,6 +652,266 @@ __global__ void __launch_bounds__(256) k_reduce_rs(const double *__restrict__ pa
       out->pe_rs = sh[0][0];
       for (int k = 0; k < 6; k++) out->vir_rs[k] = sh[k + 1][0];
    }
+}
+
+// ----------------------------------------------------------------- adjoint
+// Derivatives of one pair evaluation of pair_fu (f = -U'(r)/r, U) with
+// respect to the potential parameters and the Ewald terms:
+//   du[k] = dU/dp_k, df[k] = df/dp_k               (short-range part)
+//   uc = erfc(alpha r)/r, fc = (uc + norm exp(-alpha^2 r^2))/r^2
+//                                                   (per unit q_i q_j)
+//   duc = d uc/d alpha, dfc = d fc/d alpha          (per unit q_i q_j)
+// erfc is pair_fu's A&S polynomial t P(t) exp(-x^2), t = 1/(1 + p x), and
+// is differentiated as such: these are the derivatives of the energy and
+// force the forward kernel computes.
+template <int NP, typename R>
+struct PairGrad {
+   R du[NP], df[NP];
+   R uc, fc, duc, dfc;
+};
+
+template <int PT, bool EW, typename R>
+__device__ __forceinline__ void pair_grad(R r2, const R *p, R alpha, R norm, PairGrad<NPar<PT>::v, R> &g)
+{
+   const R r = dsqrt<R>(r2), r_r = R(1) / r, rs_r = r_r * r_r;
+   g.uc = g.fc = g.duc = g.dfc = R(0);
+   if (EW) {
+      const R x = alpha * r;
+      const R t = R(1) / (R(1) + R(ASP) * x);
+      const R pt = R(AS1) + t * (R(AS2) + t * (R(AS3) + t * (R(AS4) + t * R(AS5))));
+      const R dpt = R(AS2) + t * (R(2.0 * AS3) + t * (R(3.0 * AS4) + t * R(4.0 * AS5)));
+      const R ex = dexp<R>(-(x * x));
+      // d/dx [t P(t) e^{-x^2}] with dt/dx = -p t^2
+      const R derfc = ex * (-R(ASP) * t * t * (pt + t * dpt) - R(2) * x * t * pt);
+      g.uc = t * pt * ex * r_r;
+      g.fc = rs_r * (g.uc + norm * ex);
+      g.duc = derfc;
+      g.dfc = rs_r * (derfc + R(1.1283791670955126) * ex * (R(1) - R(2) * x * x));   // 2/sqrt(pi)
+   }
+   if (PT == 0) {   // p0 ((p1/r)^12 - (p1/r)^6)
+      const R p1s = p[1] * p[1];
+      R s6 = p1s * rs_r;
+      s6 = s6 * s6 * s6;
+      const R s12 = s6 * s6;
+      const R t5 = p1s * p1s * p[1] * (rs_r * rs_r * rs_r);   // d s6 / d p1 / 6
+      g.du[0] = s12 - s6;
+      g.du[1] = R(6) * p[0] * t5 * (R(2) * s6 - R(1));
+      g.df[0] = rs_r * R(6) * (R(2) * s12 - s6);
+      g.df[1] = rs_r * R(36) * p[0] * t5 * (R(4) * s6 - R(1));
+   } else if (PT == 1) {   // -p0/r^6 + p1 exp(-p2 r)
+      const R E = dexp<R>(-p[2] * r);
+      const R r6 = rs_r * rs_r * rs_r;
+      g.du[0] = -r6;
+      g.du[1] = E;
+      g.du[2] = -r * p[1] * E;
+      g.df[0] = R(-6) * rs_r * r6;
+      g.df[1] = p[2] * E * r_r;
+      g.df[2] = p[1] * E * (r_r - p[2]);
+   } else if (PT == 2) {   // p0 exp(-p1 r) - p2 exp(-p3 r)
+      const R E1 = dexp<R>(-p[1] * r), E3 = dexp<R>(-p[3] * r);
+      const R e1 = p[0] * E1, e2 = -p[2] * E3;
+      g.du[0] = E1;
+      g.du[1] = -r * e1;
+      g.du[2] = -E3;
+      g.du[3] = -r * e2;
+      g.df[0] = p[1] * E1 * r_r;
+      g.df[1] = e1 * (r_r - p[1]);
+      g.df[2] = -p[3] * E3 * r_r;
+      g.df[3] = e2 * (r_r - p[3]);
+   } else if (PT == 3) {   // p0 exp(-p1 r) + p2/r^12 - p3/r^4 - p4/r^6 - p5/r^8
+      const R E1 = dexp<R>(-p[1] * r), e1 = p[0] * E1;
+      const R r4 = rs_r * rs_r, r6 = r4 * rs_r, r8 = r4 * r4, r12 = r6 * r6;
+      g.du[0] = E1;
+      g.du[1] = -r * e1;
+      g.du[2] = r12;
+      g.du[3] = -r4;
+      g.du[4] = -r6;
+      g.du[5] = -r8;
+      g.df[0] = p[1] * E1 * r_r;
+      g.df[1] = e1 * (r_r - p[1]);
+      g.df[2] = R(12) * rs_r * r12;
+      g.df[3] = R(-4) * rs_r * r4;
+      g.df[4] = R(-6) * rs_r * r6;
+      g.df[5] = R(-8) * rs_r * r8;
+   } else if (PT == 4) {   // p0/r^4 + p1/r^6 + p2/r^12
+      const R r4 = rs_r * rs_r, r6 = r4 * rs_r, r12 = r6 * r6;
+      g.du[0] = r4;
+      g.du[1] = r6;
+      g.du[2] = r12;
+      g.df[0] = R(4) * rs_r * r4;
+      g.df[1] = R(6) * rs_r * r6;
+      g.df[2] = R(12) * rs_r * r12;
+   } else {   // Morse: p0 e^{(p1-r)p2} - p3/r^6 + p4 (e^{-2 p5 (r-p6)} - 2 e^{-p5 (r-p6)})
+      const R E1 = dexp<R>((p[1] - r) * p[2]), e1 = p[0] * E1;
+      const R r6 = rs_r * rs_r * rs_r;
+      const R d6 = r - p[6];
+      const R E2 = dexp<R>(R(-2) * p[5] * d6), E3 = dexp<R>(-p[5] * d6);
+      const R e2 = p[4] * E2, e3 = R(-2) * p[4] * E3;
+      g.du[0] = E1;
+      g.du[1] = p[2] * e1;
+      g.du[2] = (p[1] - r) * e1;
+      g.du[3] = -r6;
+      g.du[4] = E2 - R(2) * E3;
+      g.du[5] = -d6 * (R(2) * e2 + e3);
+      g.du[6] = p[5] * (R(2) * e2 + e3);
+      g.df[0] = r_r * p[2] * E1;
+      g.df[1] = r_r * p[2] * p[2] * e1;
+      g.df[2] = r_r * e1 * (R(1) + p[2] * (p[1] - r));
+      g.df[3] = R(-6) * rs_r * r6;
+      g.df[4] = R(2) * p[5] * r_r * (E2 - E3);
+      g.df[5] = r_r * (R(2) * e2 + e3 - d6 * p[5] * (R(4) * e2 + e3));
+      g.df[6] = r_r * p[5] * p[5] * (R(4) * e2 + e3);
+   }
+}
+
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v)
+{
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+   return v;   // valid in lane 0
+}
+
+// Gradients of the real-space energy and of G = sum_i v_i . F_i (the
+// force-matching loss for residual weights v, the Hessian-vector product of
+// the loss) with respect to the potential table, the site charges and
+// alpha.  The same stencil walk as k_pairs, recomputed (no stored pair
+// list), with the walk repeated once per partner site identifier b so that
+// every lane accumulates the table entries (id_i, b, k) in registers.
+//   slots [0, T)      dE/dp(a,b,k) at (a*max_id + b)*NP + k, T = max_id^2 NP
+//   slots [T, 2T)     dG/dp(a,b,k)
+//   slots 2T, 2T+1    dE/dalpha, dG/dalpha
+//   gq[oi], gq[N+oi]  dE/dq, dG/dq of the home site (written, not added)
+// The table entry (a, b) is the one the force on a site of id a from a site
+// of id b reads; each ordered evaluation carries half the pair energy.
+// Intramolecular pairs are left out of the energy terms (the
+// intramolecular correction removes them again); the forces keep them.
+// Persistent blocks: each warp takes home slots blockIdx.x*PAIR_WARPS + w,
+// stepping by the grid; per-block slot sums are written to gpart.
+template <int PT, bool EW, bool MIXED>
+__global__ void __launch_bounds__(PAIR_WARPS * 32)
+k_pairs_adj(RsParams P, AdjParams A, const int *__restrict__ cell_start,
+            const int *__restrict__ slot_cell, const int4 *__restrict__ full,
+            const float4 *__restrict__ off_hi, const float4 *__restrict__ off_lo,
+            const double4 *__restrict__ pos64, const float4 *__restrict__ pos32,
+            const int2 *__restrict__ tag, const int *__restrict__ sorted,
+            const double *__restrict__ site, const double *__restrict__ potg64,
+            const float *__restrict__ potg32, const double4 *__restrict__ res64,
+            const float4 *__restrict__ res32, double *__restrict__ gq, double *__restrict__ gpart)
+{
+   typedef typename std::conditional<MIXED, float, double>::type R;
+   constexpr int NP = NPar<PT>::v;
+   extern __shared__ double s_acc[];
+   __shared__ int s_inc[PAIR_WARPS][32], s_jb[PAIR_WARPS][32], s_info[PAIR_WARPS][32];
+   __shared__ float4 s_oh[PAIR_WARPS][32], s_ol[PAIR_WARPS][32];
+   for (int q = threadIdx.x; q < A.nslot; q += blockDim.x) s_acc[q] = 0.0;
+   __syncthreads();
+   const R *pot = MIXED ? (const R *)(const void *)potg32 : (const R *)(const void *)potg64;
+   const int N = P.nsites, T = P.max_id * P.max_id * NP;
+   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const WalkRows rows{s_inc[w], s_jb[w], s_info[w], s_oh[w], s_ol[w]};
+   const R alpha = MIXED ? (R)P.alphaf : (R)P.alpha, norm = MIXED ? (R)P.normf : (R)P.norm;
+   const R cut100 = (R)P.cut100;
+   for (int p0 = blockIdx.x * PAIR_WARPS; p0 < N; p0 += gridDim.x * PAIR_WARPS) {
+      const int p = p0 + w;
+      if (p >= N) break;
+      const int c = slot_cell[p];
+      const int2 ti = tag[p];
+      double4 xi64 = make_double4(0, 0, 0, 0);
+      float4 xi32 = make_float4(0, 0, 0, 0);
+      if (MIXED) xi32 = pos32[p]; else xi64 = pos64[p];
+      const R qi = MIXED ? (R)xi32.w : (R)xi64.w;
+      R vix = 0, viy = 0, viz = 0;
+      if (A.loss) {
+         if (MIXED) {
+            const float4 v = res32[p];
+            vix = v.x; viy = v.y; viz = v.z;
+         } else {
+            const double4 v = res64[p];
+            vix = v.x; viy = v.y; viz = v.z;
+         }
+      }
+      const int oi = sorted[p];
+      R gqe = 0, gql = 0, gae = 0, gal = 0;
+      for (int b = 0; b < P.max_id; b++) {
+         if (!((A.type_mask >> b) & 1u)) continue;
+         R pp[NP], ge[NP], gl[NP];
+         const R *pj = pot + ((size_t)ti.x * P.max_id + b) * NPOTP;
+#pragma unroll
+         for (int q = 0; q < NP; q++) {
+            pp[q] = pj[q];
+            ge[q] = gl[q] = R(0);
+         }
+         walk_stencil<MIXED>(P, p, c, lane, cell_start, full, off_hi, off_lo, rows, [&](int j, int k, int kimg) {
+            const int2 tj = __ldg(&tag[j]);
+            if (tj.x != b) return;
+            R rx, ry, rz, r2, qj;
+            pair_sep<MIXED>(P, j, k, kimg, rows, xi32, xi64, pos64, pos32, rx, ry, rz, r2, qj);
+            bool too_close, clip;
+            pair_flags<MIXED>(P, r2, oi, j, kimg, sorted, site, too_close, clip);
+            if (clip) r2 = cut100;
+            PairGrad<NP, R> g;
+            pair_grad<PT, EW, R>(r2, pp, alpha, norm, g);
+            if (ti.y != tj.y) {
+#pragma unroll
+               for (int q = 0; q < NP; q++) ge[q] += g.du[q];
+               gqe += qj * g.uc;
+               gae += qj * g.duc;
+            }
+            if (A.loss) {
+               R vjx, vjy, vjz;
+               if (MIXED) {
+                  const float4 v = __ldg(&res32[j]);
+                  vjx = v.x; vjy = v.y; vjz = v.z;
+               } else {
+                  const double4 v = res64[j];
+                  vjx = v.x; vjy = v.y; vjz = v.z;
+               }
+               const R wi = vix * rx + viy * ry + viz * rz;            // v_i . r
+               const R ws = wi - (vjx * rx + vjy * ry + vjz * rz);      // (v_i - v_j) . r
+#pragma unroll
+               for (int q = 0; q < NP; q++) gl[q] -= g.df[q] * wi;
+               gql -= qj * g.fc * ws;
+               gal -= qj * g.dfc * wi;
+            }
+         });
+         double *se = s_acc + ((size_t)ti.x * P.max_id + b) * NP;
+#pragma unroll
+         for (int q = 0; q < NP; q++) {
+            const R s = warp_sum(ge[q]);
+            if (lane == 0) atomicAdd(se + q, 0.5 * (double)s);
+         }
+         if (A.loss) {
+#pragma unroll
+            for (int q = 0; q < NP; q++) {
+               const R s = warp_sum(gl[q]);
+               if (lane == 0) atomicAdd(se + T + q, (double)s);
+            }
+         }
+      }
+      gqe = warp_sum(gqe);
+      gql = warp_sum(gql);
+      gae = warp_sum(gae);
+      gal = warp_sum(gal);
+      if (lane == 0) {
+         gq[oi] = (double)gqe;
+         gq[N + oi] = (double)gql;
+         atomicAdd(s_acc + 2 * T, 0.5 * (double)qi * (double)gae);
+         atomicAdd(s_acc + 2 * T + 1, (double)qi * (double)gal);
+      }
+   }
+   __syncthreads();
+   for (int q = threadIdx.x; q < A.nslot; q += blockDim.x) gpart[(size_t)blockIdx.x * A.nslot + q] = s_acc[q];
+}
+
+// Slot sums over blocks, in block order.
+__global__ void k_adj_slots(const double *__restrict__ gpart, int nblocks, int nslot, double *__restrict__ slots)
+{
+   const int q = blockIdx.x * blockDim.x + threadIdx.x;
+   if (q >= nslot) return;
+   double s = 0.0;
+   for (int b = 0; b < nblocks; b++) s += gpart[(size_t)b * nslot + q];
+   slots[q] = s;
 }
 
 // -------------------------------------------------------------- host side
@@ -716,6 +1025,75 @@ static cudaError_t launch_pairs_pt(const RsParams &P, mdgpu_ctx *c, bool ew, boo
                 : launch_pairs_t<PT, false, true, 0>(P, c, force, out, keys, key_cap, smem);
    return ew ? launch_pairs_t<PT, true, false, 0>(P, c, force, out, keys, key_cap, smem)
              : launch_pairs_t<PT, false, false, 0>(P, c, force, out, keys, key_cap, smem);
+}
+
+template <int PT, bool EW, bool MIXED>
+static cudaError_t launch_adj_t(const RsParams &P, const AdjParams &A, mdgpu_ctx *c, int nblk)
+{
+   RsDev &d = c->rd;
+   AdjDev &a = c->ad;
+   k_pairs_adj<PT, EW, MIXED><<<nblk, PAIR_WARPS * 32, A.nslot * sizeof(double), c->stream>>>(
+      P, A, d.cell_start.p, d.slot_cell.p, d.full.p, d.off_hi.p, d.off_lo.p, d.pos64.p, d.pos32.p, d.tag.p,
+      d.sorted.p, c->cur_site, d.pot64.p, d.pot32.p, a.res64.p, a.res32.p, a.gq.p, a.gpart.p);
+   return cudaGetLastError();
+}
+
+template <int PT>
+static cudaError_t launch_adj_pt(const RsParams &P, const AdjParams &A, mdgpu_ctx *c, bool ew, bool mixed,
+                                 int nblk)
+{
+   if (mixed)
+      return ew ? launch_adj_t<PT, true, true>(P, A, c, nblk) : launch_adj_t<PT, false, true>(P, A, c, nblk);
+   return ew ? launch_adj_t<PT, true, false>(P, A, c, nblk) : launch_adj_t<PT, false, false>(P, A, c, nblk);
+}
+
+int pot_nparams(int ptype)
+{
+   switch (ptype) {
+   case 0: return NPar<0>::v;
+   case 1: return NPar<1>::v;
+   case 2: return NPar<2>::v;
+   case 3: return NPar<3>::v;
+   case 4: return NPar<4>::v;
+   case 6: return NPar<6>::v;
+   default: return 0;
+   }
+}
+
+mdgpu_status rs_adjoint(mdgpu_ctx *c, bool loss)
+{
+   AdjDev &a = c->ad;
+   cudaStream_t st = c->stream;
+   RsParams P = make_params(c);
+   const int N = c->nsites;
+   const bool mixed = c->prec == MDGPU_MIXED;
+   const int np = pot_nparams(c->ptype);
+   AdjParams A;
+   A.loss = loss ? 1 : 0;
+   A.type_mask = 0;
+   for (int id : c->site_id) A.type_mask |= 1u << id;
+   A.nslot = 2 * c->max_id * c->max_id * np + 2;
+   int nblk = (N + PAIR_WARPS - 1) / PAIR_WARPS;
+   if (nblk > 4 * 152) nblk = 4 * 152;
+   CK(a.gq.ensure(2 * (size_t)N));
+   CK(a.gpart.ensure((size_t)nblk * A.nslot));
+   CK(a.slots.ensure((size_t)A.nslot));
+   const bool ew = c->ctl.alpha > 0.0;
+   cudaError_t e;
+   switch (c->ptype) {
+   case 0: e = launch_adj_pt<0>(P, A, c, ew, mixed, nblk); break;
+   case 1: e = launch_adj_pt<1>(P, A, c, ew, mixed, nblk); break;
+   case 2: e = launch_adj_pt<2>(P, A, c, ew, mixed, nblk); break;
+   case 3: e = launch_adj_pt<3>(P, A, c, ew, mixed, nblk); break;
+   case 4: e = launch_adj_pt<4>(P, A, c, ew, mixed, nblk); break;
+   case 6: e = launch_adj_pt<6>(P, A, c, ew, mixed, nblk); break;
+   default: return fail(c, MDGPU_E_PTYPE, "KERNEL called with unknown potential type");
+   }
+   CK(e);
+   k_adj_slots<<<(A.nslot + 255) / 256, 256, 0, st>>>(a.gpart.p, nblk, A.nslot, a.slots.p);
+   CK(cudaGetLastError());
+   c->launches += 2;
+   return MDGPU_OK;
 }
 
 mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm, double *d_force,

@@ -162,6 +162,60 @@ class ForceField:
         self._check(st)
         return np.sort(keys[:cnt.value])
 
+    # -- adjoint -------------------------------------------------------------
+    def _params(self, potpar, chg, alpha):
+        keep = []
+        P = _lib.Params(None, None, float(alpha) if alpha is not None else 0.0)
+        if potpar is not None:
+            a = np.ascontiguousarray(potpar, np.float64).reshape(-1)
+            if a.size != self.sysm.max_id ** 2 * _lib.NPOTP:
+                raise ValueError("potpar must hold max_id*max_id*8 values")
+            keep.append(a)
+            P.potpar = _dp(a)
+        if chg is not None:
+            a = np.ascontiguousarray(chg, np.float64).reshape(-1)
+            if a.size != self.sysm.nsites:
+                raise ValueError("chg must hold one charge per site")
+            keep.append(a)
+            P.chg = _dp(a)
+        return P, keep
+
+    def set_params(self, potpar=None, chg=None, alpha=None):
+        """Replace the potential table, the site charges and/or alpha (None
+        keeps the current value); the cutoffs and the k-vector list stay."""
+        P, keep = self._params(potpar, chg, alpha)
+        self._check(self.L.mdgpu_set_params(self.ctx, C.byref(P)))
+
+    def _grad_call(self, loss: bool, site, c_of_m, f_ref=None, weight=1.0):
+        site = np.ascontiguousarray(self.sysm.site if site is None else site, np.float64)
+        cm = np.ascontiguousarray(self.sysm.c_of_m if c_of_m is None else c_of_m, np.float64)
+        M, N = self.sysm.max_id, site.shape[1]
+        gp = np.zeros(M * M * _lib.NPOTP)
+        gq = np.zeros(N)
+        G = _lib.Grad(_dp(gp), _dp(gq), 0.0)
+        val = np.zeros(1)
+        if loss:
+            fr = np.ascontiguousarray(f_ref, np.float64)
+            self._check(self.L.mdgpu_fm_loss_grad(self.ctx, None, _dp(self._h()), _dp(site), _dp(cm), _dp(fr),
+                                                  float(weight), _dp(val), C.byref(G)))
+        else:
+            self._check(self.L.mdgpu_energy_grad(self.ctx, None, _dp(self._h()), _dp(site), _dp(cm), _dp(val),
+                                                 C.byref(G)))
+        return float(val[0]), {"potpar": gp.reshape(M, M, _lib.NPOTP), "chg": gq, "alpha": float(G.alpha)}
+
+    def energy_grad(self, site: Optional[np.ndarray] = None, c_of_m: Optional[np.ndarray] = None):
+        """Potential energy pe[0] + pe[1] and its gradient with respect to
+        the potential table ([max_id, max_id, 8]; entry [a, b] as the force
+        on a site of id a from one of id b reads it), the site charges and
+        alpha, at the current parameters."""
+        return self._grad_call(False, site, c_of_m)
+
+    def fm_loss_grad(self, f_ref: np.ndarray, weight: float = 1.0, site: Optional[np.ndarray] = None,
+                     c_of_m: Optional[np.ndarray] = None):
+        """Force-matching loss weight * sum |F - f_ref|^2 and its gradient
+        (same layout as energy_grad)."""
+        return self._grad_call(True, site, c_of_m, f_ref, weight)
+
     def info(self) -> dict:
         i = _lib.Info()
         self._check(self.L.mdgpu_get_info(self.ctx, C.byref(i)))
