@@ -236,6 +236,45 @@ mdgpu_status mdgpu_fm_loss_grad(mdgpu_ctx *ctx, const mdgpu_params *params, cons
                                 const double *f_ref_soa, double weight, double *loss,
                                 mdgpu_grad *grad);
 
+/* ---- Rigid-molecule dynamics on the GPU.  No counterpart in the reference
+ * as an entry point: the constant-energy step of do_step (src/accel.c:626-827,
+ * thermostat and barostat off) with this library's forces, every step on
+ * the device.  Per step: half drift of centres of mass (fractional
+ * co-ordinates, periodic wrap) and quaternions (the reference's symplectic
+ * rotational splitting, src/leapfrog.c:246-392), site co-ordinates, forces,
+ * molecular forces and principal-frame torques, two half kicks with the
+ * kinetic energy between them, half drift.  State layout is the
+ * reference's: c_of_m and mom [nmols][3] (fractional centres of mass and
+ * scaled momenta h^T h m ds/dt), quat and amom [nmols_r][4] for the
+ * molecules of rotating species in species order (amom[0] unused, [1..3]
+ * principal angular momenta).  Framework species, thermostats and barostats
+ * are not supported. */
+typedef struct {
+   const double *mass;          /* [nspecies] molecular mass, amu             */
+   const double *inertia;       /* [nspecies][3] principal moments of inertia */
+   const int *rdof;             /* [nspecies] rotational degrees of freedom   */
+   double step;                 /* timestep, ps                               */
+   int nosymmetric_rot;         /* the nosymmetric-rot control key            */
+} mdgpu_dynamics;
+
+/* Loads the dynamic state (h as for mdgpu_forces; quat/amom may be NULL
+ * when no species rotates). */
+mdgpu_status mdgpu_md_init(mdgpu_ctx *ctx, const mdgpu_dynamics *dyn, const double *h,
+                           const double *c_of_m, const double *mom, const double *quat,
+                           const double *amom);
+
+/* Advances nsteps steps.  energies ([nsteps][4], or NULL) receives per step
+ * the real-space energy with the distant-potential correction (pe[0] of
+ * eval_forces), the reciprocal-space energy (pe[1]) and the translational
+ * and rotational kinetic energies at the half kick (the point where do_step
+ * evaluates its conserved quantity).  MDGPU_E_RANGE if a site left the
+ * cell or a quaternion lost its normalisation (QNORM2). */
+mdgpu_status mdgpu_md_run(mdgpu_ctx *ctx, int nsteps, double *energies);
+
+/* Copies the current state back (any pointer may be NULL). */
+mdgpu_status mdgpu_md_get_state(mdgpu_ctx *ctx, double *c_of_m, double *mom, double *quat,
+                                double *amom);
+
 /* Measures the device's dense FMA throughput (TFLOP/s, FMA = 2 flops) in
  * FP32 (fp64 = 0) or FP64: the roofline denominators of the force kernels,
  * whose bound is the FMA pipe.  No counterpart in the reference. */

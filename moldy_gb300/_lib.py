@@ -23,7 +23,7 @@ EXPORTS = ["mdgpu_create", "mdgpu_destroy", "mdgpu_last_error", "mdgpu_set_preci
            "mdgpu_synchronize", "mdgpu_get_info", "mdgpu_pair_keys", "mdgpu_poteval",
            "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak",
            "mdgpu_ewald_kspace_noalloc", "mdgpu_set_params", "mdgpu_energy_grad",
-           "mdgpu_fm_loss_grad",
+           "mdgpu_fm_loss_grad", "mdgpu_md_init", "mdgpu_md_run", "mdgpu_md_get_state",
            "force_calc", "ewald", "poteval"]
 
 
@@ -62,6 +62,11 @@ class Params(C.Structure):
 
 class Grad(C.Structure):
     _fields_ = [("potpar", C.POINTER(C.c_double)), ("chg", C.POINTER(C.c_double)), ("alpha", C.c_double)]
+
+
+class Dynamics(C.Structure):
+    _fields_ = [("mass", C.POINTER(C.c_double)), ("inertia", C.POINTER(C.c_double)),
+                ("rdof", C.POINTER(C.c_int)), ("step", C.c_double), ("nosymmetric_rot", C.c_int)]
 
 
 NPOTP = 8
@@ -107,6 +112,9 @@ def load():
         "mdgpu_fma_peak": ([ip, ip, dp], ip),
         "mdgpu_ewald_kspace_noalloc": ([dp, ip, vp, vp, C.c_double, C.c_double, vp, vp, vp, vp], ip),
         "mdgpu_set_params": ([vp, C.POINTER(Params)], ip),
+        "mdgpu_md_init": ([vp, C.POINTER(Dynamics), dp, dp, dp, dp, dp], ip),
+        "mdgpu_md_run": ([vp, ip, dp], ip),
+        "mdgpu_md_get_state": ([vp, dp, dp, dp, dp], ip),
         "mdgpu_energy_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.POINTER(Grad)], ip),
         "mdgpu_fm_loss_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.c_double, dp, C.POINTER(Grad)], ip),
     }

@@ -504,4 +504,61 @@ void ewald_self_sheet(const std::vector<mdgpu_species> &spec, const std::vector<
    *nsitesxf = (int)nxf;
 }
 
+
+// -int_rc^inf r^2 U(r) dr of the short-range part (dist_pot, src/kernel.c:103-150)
+static double dist_pot(const double *p, double rc, int ptype)
+{
+   const double tol = 1.0e-7;   // BPAR_TOL, src/kernel.c:97
+   const double rc3 = rc * rc * rc;
+   switch (ptype) {
+   case 0:
+      {
+      const double t = p[1] * p[1] / rc;
+      return p[0] * (t * t * t) / 3.0;
+   }
+   case 1:
+      if (p[2] > tol)
+         return p[0] / (3.0 * rc3) -
+                p[1] * std::exp(-p[2] * rc) * (rc * rc / p[2] + 2 * rc / (p[2] * p[2]) + 2.0 / (p[2] * p[2] * p[2]));
+      return p[0] / (3.0 * rc3);
+   case 2:
+      if (p[3] > tol)
+         return p[2] * (rc * rc / p[3] + 2 * rc / (p[3] * p[3]) + 2.0 / (p[3] * p[3] * p[3])) * std::exp(-p[3] * rc);
+      return 0.0;
+   case 3: {
+      const double tail = -p[2] / (9.0 * rc3 * rc3 * rc3) + p[3] / rc + p[4] / (3.0 * rc3) + p[5] / (5.0 * rc * rc * rc3);
+      if (p[1] > tol)
+         return -p[0] * std::exp(-p[1] * rc) * (rc * rc / p[1] + 2 * rc / (p[1] * p[1]) + 2.0 / (p[1] * p[1] * p[1])) +
+                tail;
+      return tail;
+   }
+   case 6:
+      if (p[5] != 0.0)
+         return p[3] / (3.0 * rc3) + 2.0 * p[4] * (rc * rc / p[5] + 2 * rc / (p[5] * p[5]) + 2.0 / (p[5] * p[5] * p[5])) *
+                                        std::exp(-p[5] * (rc - p[6]));
+      return p[3] / (3.0 * rc3);
+   case 4:
+      return -p[0] / rc - p[1] / rc3 / 3.0 - p[2] / (rc3 * rc3 * rc3) / 9.0;
+   default:
+      return 0.0;
+   }
+}
+
+double distant_const(const mdgpu_ctx *c)
+{
+   const int M = c->max_id;
+   std::vector<long long> count(M, 0);
+   size_t so = 0;
+   for (const auto &sp : c->spec) {
+      for (int k = 0; k < sp.nsites; k++) count[c->spec_ids[so + k]] += sp.nmols;
+      so += sp.nsites;
+   }
+   double cst = 0.0;
+   for (int id = 1; id < M; id++)
+      for (int jd = 1; jd < M; jd++)
+         cst -= 2 * PI * (double)count[id] * (double)count[jd] *
+                dist_pot(c->potpar.data() + ((size_t)id + (size_t)M * jd) * NPOTP, c->ctl.cutoff, c->ptype);
+   return cst;
+}
+
 }  // namespace mdgpu

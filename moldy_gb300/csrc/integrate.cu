@@ -1,0 +1,500 @@
+// Constant-energy rigid-molecule dynamics on the GPU: the step of do_step
+// (src/accel.c:626-827) without thermostat or barostat, all in FP64 and all
+// on the device, so a run of many steps moves no per-step data to the host.
+//
+// One step (the symplectic leapfrog of src/leapfrog.c):
+//   k_md_drift   half-step of the centres of mass (leapf_com,
+//                src/leapfrog.c:133-146, with the periodic wrap of escape(),
+//                src/leapfrog.c:117-128) and of the quaternions and principal
+//                angular momenta (leapf_quat, src/leapfrog.c:246-392: the
+//                Dullweber-Leimkuhler-McLachlan rotational splitting,
+//                symmetric-top variant unless nosymmetric_rot)
+//   k_md_sites   site co-ordinates from centres of mass and quaternions
+//                (make_sites, src/algorith.c:169-215)
+//   forces       the force path of this library (real space + k space)
+//   k_md_kick    molecular forces and principal-frame torques (mol_force,
+//                mol_torque, src/algorith.c:111-160), two half kicks of the
+//                momenta (leapf_mom, leapf_amom, src/leapfrog.c:149-157,
+//                395-406), the kinetic energy between them -- where do_step
+//                evaluates its conserved quantity (src/accel.c:718-727)
+//   k_md_record  per-step energies (potential with the distant-potential
+//                correction of eval_forces, src/accel.c:608-611; kinetic)
+//   k_md_drift   second half-step of the co-ordinates.
+// Matrix-vector products and axpy updates keep the reference's operation
+// order without fused multiply-adds (src/matrix.c mat_vec_mul, mvaxpy).
+#include <cmath>
+#include <cstring>
+
+#include "mdgpu_internal.h"
+
+namespace mdgpu {
+
+constexpr double INERTIA_MIN = 1.0e-14;   // src/defs.h:298
+constexpr double AMOM_EPS = 8.0e-37;      // 8 * DBL_MIN as src/leapfrog.c:88-90 defines it
+constexpr double QNORM_TOL = 1.0e-4;      // TOLERANCE, src/leapfrog.c:78
+
+#define DM(a, b) __dmul_rn(a, b)
+#define DA(a, b) __dadd_rn(a, b)
+#define DS(a, b) __dsub_rn(a, b)
+
+struct MdStepParams {
+   int nmols, nsites, molpbc, nosym, saxis, o1, o2;
+   double h[9], hinv[9];
+   double kick[9];      // 0.5 dt h^T (leapf_mom's scaled transpose)
+   double half;         // 0.5 dt
+};
+
+// q <- p * q-style products of src/quaterns.c:38-127 (r may alias p or q)
+__device__ __forceinline__ void qmul(const double *p, const double *q, double *r)
+{
+   const double p0 = p[0], p1 = p[1], p2 = p[2], p3 = p[3];
+   const double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+   r[0] = DS(DS(DS(DM(p0, q0), DM(p1, q1)), DM(p2, q2)), DM(p3, q3));
+   r[1] = DA(DS(DA(DM(p1, q0), DM(p0, q1)), DM(p3, q2)), DM(p2, q3));
+   r[2] = DS(DA(DA(DM(p2, q0), DM(p3, q1)), DM(p0, q2)), DM(p1, q3));
+   r[3] = DA(DA(DS(DM(p3, q0), DM(p2, q1)), DM(p1, q2)), DM(p0, q3));
+}
+__device__ __forceinline__ void qconjmul(const double *p, const double *q, double *r)
+{
+   const double pc[4] = {p[0], -p[1], -p[2], -p[3]};
+   qmul(pc, q, r);
+}
+
+// rot = (cos a, sin a along `axis`), a = 0.5 step rinertia amom[axis+1]
+// (make_rot, src/leapfrog.c:206-219), then amom <- rot^-1 amom rot,
+// quat <- quat rot (rot_substep, src/leapfrog.c:236-243).
+__device__ __forceinline__ void rot_axis(double step, int axis, double rin, double *amom, double *quat)
+{
+   const double angle = DM(DM(DM(0.5, step), rin), amom[axis + 1]);
+   double sa, ca;
+   sincos(angle, &sa, &ca);
+   double rot[4] = {ca, 0.0, 0.0, 0.0};
+   rot[axis + 1] = sa;
+   qconjmul(rot, amom, amom);
+   qmul(amom, rot, amom);
+   qmul(quat, rot, quat);
+}
+
+// Rotation about the angular momentum by 0.5 step rinertia |L|
+// (make_rot_amom, src/leapfrog.c:222-235), applied to the quaternion only.
+__device__ __forceinline__ void rot_amom(double step, double rin, const double *amom, double *quat)
+{
+   const double samom = sqrt(DA(DA(DM(amom[1], amom[1]), DM(amom[2], amom[2])), DM(amom[3], amom[3])));
+   const double ramom = 1.0 / DA(samom, AMOM_EPS);
+   const double angle = DM(DM(DM(0.5, step), rin), samom);
+   double sa, ca;
+   sincos(angle, &sa, &ca);
+   const double rot[4] = {ca, DM(DM(sa, ramom), amom[1]), DM(DM(sa, ramom), amom[2]), DM(DM(sa, ramom), amom[3])};
+   qmul(quat, rot, quat);
+}
+
+__global__ void k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict__ mol_spec,
+                           const int *__restrict__ mol_q, double *__restrict__ cofm,
+                           const double *__restrict__ mom, double *__restrict__ quat, double *__restrict__ amom,
+                           int *__restrict__ err)
+{
+   const int m = blockIdx.x * blockDim.x + threadIdx.x;
+   if (m >= P.nmols) return;
+   const MdSpec &S = spec[mol_spec[m]];
+   // leapf_com: c += (step/mass) G^-1 mom, then the periodic wrap
+   const double *a = S.gdrift;
+   double *c = cofm + 3 * (size_t)m;
+   const double x0 = mom[3 * (size_t)m], x1 = mom[3 * (size_t)m + 1], x2 = mom[3 * (size_t)m + 2];
+   const double y0 = DA(DA(DA(c[0], DM(a[0], x0)), DM(a[1], x1)), DM(a[2], x2));
+   const double y1 = DA(DA(DA(c[1], DM(a[3], x0)), DM(a[4], x1)), DM(a[5], x2));
+   const double y2 = DA(DA(DA(c[2], DM(a[6], x0)), DM(a[7], x1)), DM(a[8], x2));
+   c[0] = DS(y0, floor(DA(y0, 0.5)));
+   c[1] = DS(y1, floor(DA(y1, 0.5)));
+   c[2] = DS(y2, floor(DA(y2, 0.5)));
+   const int qi = mol_q[m];
+   if (qi < 0) return;
+   double q[4], L[4];
+   for (int k = 0; k < 4; k++) {
+      q[k] = quat[4 * (size_t)qi + k];
+      L[k] = amom[4 * (size_t)qi + k];
+   }
+   const double st = P.half;
+   const double *ri = S.rinertia;
+   if (P.nosym) {   // leapf_quat_a, src/leapfrog.c:338-392
+      rot_axis(0.5 * st, 0, ri[0], L, q);
+      rot_axis(0.5 * st, 1, ri[1], L, q);
+      rot_axis(st, 2, ri[2], L, q);
+      rot_axis(0.5 * st, 1, ri[1], L, q);
+      rot_axis(0.5 * st, 0, ri[0], L, q);
+   } else {         // leapf_quat_b, src/leapfrog.c:253-333
+      const int sx = P.saxis, o1 = P.o1, o2 = P.o2;
+      rot_axis(0.5 * st, o1, DS(ri[o1], ri[o2]), L, q);
+      rot_axis(st, sx, DS(ri[sx], ri[o2]), L, q);
+      rot_amom(st, ri[o2], L, q);
+      rot_axis(0.5 * st, o1, DS(ri[o1], ri[o2]), L, q);
+   }
+   // normalise, src/leapfrog.c:99-114
+   double norm = 0.0;
+   for (int k = 0; k < 4; k++) norm = DA(norm, DM(q[k], q[k]));
+   norm = sqrt(norm);
+   if (fabs(norm - 1.0) > QNORM_TOL) atomicOr(err, 2);
+   for (int k = 0; k < 4; k++) {
+      quat[4 * (size_t)qi + k] = q[k] / norm;
+      amom[4 * (size_t)qi + k] = L[k];
+   }
+}
+
+// Rotation matrix of a quaternion (q_to_rot, src/quaterns.c:129-160).
+__device__ __forceinline__ void q_to_rot(const double *q, double *r)
+{
+   const double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+   const double a01 = DM(DM(2.0, q0), q1), a02 = DM(DM(2.0, q0), q2), a03 = DM(DM(2.0, q0), q3);
+   const double a12 = DM(DM(2.0, q1), q2), a13 = DM(DM(2.0, q1), q3), a23 = DM(DM(2.0, q2), q3);
+   r[1] = DS(a12, a03);
+   r[2] = DA(a13, a02);
+   r[3] = DA(a12, a03);
+   r[5] = DS(a23, a01);
+   r[6] = DS(a13, a02);
+   r[7] = DA(a23, a01);
+   const double s0 = DM(q0, q0), s1 = DM(q1, q1), s2 = DM(q2, q2), s3 = DM(q3, q3);
+   r[0] = DS(DS(DA(s0, s1), s2), s3);
+   r[4] = DS(DA(DS(s0, s1), s2), s3);
+   r[8] = DA(DS(DS(s0, s1), s2), s3);
+}
+
+__device__ __forceinline__ void matvec(const double *m, double a0, double a1, double a2, double *o)
+{
+   o[0] = DA(DA(DM(m[0], a0), DM(m[1], a1)), DM(m[2], a2));
+   o[1] = DA(DA(DM(m[3], a0), DM(m[4], a1)), DM(m[5], a2));
+   o[2] = DA(DA(DM(m[6], a0), DM(m[7], a1)), DM(m[8], a2));
+}
+
+// One thread per site: site = R(q) p + h s (make_sites), wrapped into the
+// cell unless molecular cutoffs are in use.
+__global__ void k_md_sites(MdStepParams P, const int *__restrict__ site_mol, const int *__restrict__ site_pf,
+                           const double *__restrict__ pf, const int *__restrict__ mol_q,
+                           const double *__restrict__ cofm, const double *__restrict__ quat,
+                           double *__restrict__ site)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const int N = P.nsites;
+   if (i >= N) return;
+   const int m = site_mol[i];
+   double c[3], r[3];
+   matvec(P.h, cofm[3 * (size_t)m], cofm[3 * (size_t)m + 1], cofm[3 * (size_t)m + 2], c);
+   const double *p = pf + 3 * (size_t)site_pf[i];
+   const int qi = mol_q[m];
+   if (qi >= 0) {
+      double R[9];
+      q_to_rot(quat + 4 * (size_t)qi, R);
+      matvec(R, p[0], p[1], p[2], r);
+   } else {
+      r[0] = p[0];
+      r[1] = p[1];
+      r[2] = p[2];
+   }
+   double x = DA(r[0], c[0]), y = DA(r[1], c[1]), z = DA(r[2], c[2]);
+   if (!P.molpbc) {
+      const double *hi = P.hinv, *h = P.h;
+      const double tx = floor(DA(DA(DA(DM(hi[0], x), DM(hi[1], y)), DM(hi[2], z)), 0.5));
+      const double ty = floor(DA(DA(DA(DM(hi[3], x), DM(hi[4], y)), DM(hi[5], z)), 0.5));
+      const double tz = floor(DA(DA(DA(DM(hi[6], x), DM(hi[7], y)), DM(hi[8], z)), 0.5));
+      x = DS(x, DA(DA(DM(h[0], tx), DM(h[1], ty)), DM(h[2], tz)));
+      y = DS(y, DA(DA(DM(h[3], tx), DM(h[4], ty)), DM(h[5], tz)));
+      z = DS(z, DA(DA(DM(h[6], tx), DM(h[7], ty)), DM(h[8], tz)));
+   }
+   site[i] = x;
+   site[N + i] = y;
+   site[2 * N + i] = z;
+}
+
+// One thread per molecule: force and principal-frame torque from the site
+// forces, two half kicks, and the kinetic energy between them (block sums
+// of the translational and rotational parts in kpart).
+__global__ void __launch_bounds__(256)
+k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict__ mol_spec,
+          const int *__restrict__ mol_q, const int *__restrict__ mol_site0, const double *__restrict__ pf,
+          const double *__restrict__ force, const double *__restrict__ quat, double *__restrict__ mom,
+          double *__restrict__ amom, double *__restrict__ kpart)
+{
+   __shared__ double sh[2][256];
+   const int m = blockIdx.x * blockDim.x + threadIdx.x;
+   const int N = P.nsites;
+   double ket = 0.0, ker = 0.0;
+   if (m < P.nmols) {
+      const MdSpec &S = spec[mol_spec[m]];
+      const int s0 = mol_site0[m];
+      double F[3] = {0.0, 0.0, 0.0};
+      for (int k = 0; k < 3; k++)
+         for (int s = 0; s < S.nsites; s++) F[k] = DA(F[k], force[(size_t)k * N + s0 + s]);
+      const int qi = mol_q[m];
+      double T[3] = {0.0, 0.0, 0.0};
+      if (qi >= 0) {
+         double R[9], Rt[9];
+         q_to_rot(quat + 4 * (size_t)qi, R);
+         for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) Rt[3 * a + b] = R[3 * b + a];
+         const double *p = pf + 3 * (size_t)S.pf0;
+         for (int i = 0, j = 1, k = 2; i < 3; i++, j = (j + 1) % 3, k = (k + 1) % 3) {
+            double t = 0.0;
+            for (int s = 0; s < S.nsites; s++) {
+               double f[3];
+               matvec(Rt, force[s0 + s], force[(size_t)N + s0 + s], force[2 * (size_t)N + s0 + s], f);
+               t = DA(t, DS(DM(p[3 * s + j], f[k]), DM(p[3 * s + k], f[j])));
+            }
+            T[i] = t;
+         }
+      }
+      const double *a = P.kick;
+      double *pm = mom + 3 * (size_t)m;
+      double x[3] = {pm[0], pm[1], pm[2]};
+      for (int half = 0; half < 2; half++) {
+         const double y0 = DA(DA(DA(x[0], DM(a[0], F[0])), DM(a[1], F[1])), DM(a[2], F[2]));
+         const double y1 = DA(DA(DA(x[1], DM(a[3], F[0])), DM(a[4], F[1])), DM(a[5], F[2]));
+         const double y2 = DA(DA(DA(x[2], DM(a[6], F[0])), DM(a[7], F[1])), DM(a[8], F[2]));
+         x[0] = y0;
+         x[1] = y1;
+         x[2] = y2;
+         double L[3] = {0.0, 0.0, 0.0};
+         if (qi >= 0) {
+            double *am = amom + 4 * (size_t)qi;
+            for (int k = 0; k < 3; k++) {
+               am[k + 1] = DA(am[k + 1], DM(P.half, T[k]));
+               L[k] = am[k + 1];
+            }
+         }
+         if (half == 0) {
+            // trans_ke, rot_ke (src/algorith.c:221-258) at the half kick
+            double v[3];
+            const double *hi = P.hinv;
+            v[0] = DA(DA(DM(hi[0], x[0]), DM(hi[3], x[1])), DM(hi[6], x[2]));
+            v[1] = DA(DA(DM(hi[1], x[0]), DM(hi[4], x[1])), DM(hi[7], x[2]));
+            v[2] = DA(DA(DM(hi[2], x[0]), DM(hi[5], x[1])), DM(hi[8], x[2]));
+            ket = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / (2.0 * S.mass);
+            if (qi >= 0)
+               for (int k = 0; k < 3; k++)
+                  if (S.inertia[k] > INERTIA_MIN) ker += 0.5 * L[k] * L[k] / S.inertia[k];
+         }
+      }
+      pm[0] = x[0];
+      pm[1] = x[1];
+      pm[2] = x[2];
+   }
+   // fixed-shape block sums
+   sh[0][threadIdx.x] = ket;
+   sh[1][threadIdx.x] = ker;
+   __syncthreads();
+   for (int w = 128; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) {
+         sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+         sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+      }
+      __syncthreads();
+   }
+   if (threadIdx.x == 0) {
+      kpart[2 * blockIdx.x] = sh[0][0];
+      kpart[2 * blockIdx.x + 1] = sh[1][0];
+   }
+}
+
+__global__ void k_md_record(int step, const double *__restrict__ pe, const double *__restrict__ kpart, int nb,
+                            double dist_v, const DevOut *__restrict__ out, double *__restrict__ energies,
+                            int *__restrict__ err)
+{
+   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+   double kt = 0.0, kr = 0.0;
+   for (int b = 0; b < nb; b++) {
+      kt += kpart[2 * b];
+      kr += kpart[2 * b + 1];
+   }
+   double *e = energies + 4 * (size_t)step;
+   e[0] = pe[0] + dist_v;
+   e[1] = pe[1];
+   e[2] = kt;
+   e[3] = kr;
+   if (out->err & 1) *err |= 1;
+}
+
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+
+static void step_params(const mdgpu_ctx *c, MdStepParams &P)
+{
+   const MdHost &H = c->mdh;
+   std::memset(&P, 0, sizeof P);
+   P.nmols = c->nmols;
+   P.nsites = c->nsites;
+   P.molpbc = c->ctl.molpbc;
+   P.nosym = H.nosym;
+   P.saxis = H.saxis;
+   P.o1 = (H.saxis + 1) % 3;
+   P.o2 = (H.saxis + 2) % 3;
+   std::memcpy(P.h, H.h, sizeof P.h);
+   inv3(H.h, P.hinv);
+   // leapf_mom: step * h^T, step = dt/2 (each of the two half kicks)
+   for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) P.kick[3 * i + j] = H.half * H.h[3 * j + i];
+   P.half = H.half;
+}
+
+}  // namespace mdgpu
+
+using namespace mdgpu;
+
+extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, const double *h,
+                                      const double *c_of_m, const double *mom, const double *quat,
+                                      const double *amom)
+{
+   if (!c || !dyn || !h || !c_of_m || !mom || !dyn->mass || !dyn->inertia || !dyn->rdof)
+      return fail(c, MDGPU_E_ARG, "NULL argument");
+   if (!c->have_system || !c->have_control)
+      return fail(c, MDGPU_E_ARG, "mdgpu_set_system and mdgpu_set_control come first");
+   if (!(dyn->step > 0.0)) return fail(c, MDGPU_E_ARG, "the timestep must be positive");
+   mdgpu_status s = ensure_ready(c, h, true, true);
+   if (s) return s;
+   MdHost &H = c->mdh;
+   const int nsp = (int)c->spec.size();
+   H.spec.assign(nsp, MdSpec{});
+   std::vector<int> mol_spec(c->nmols), mol_q(c->nmols), mol_site0(c->nmols), site_mol(c->nsites),
+      site_pf(c->nsites);
+   std::memcpy(H.h, h, sizeof H.h);
+   H.half = 0.5 * dyn->step;
+   H.nosym = dyn->nosymmetric_rot ? 1 : 0;
+   // leapf_com's matrix (step/(mass s)) G^-1 with G = h^T h (src/leapfrog.c:133-143)
+   double ht[9], G[9], Gi[9];
+   for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) ht[3 * i + j] = h[3 * j + i];
+   for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+         G[3 * i + j] = ht[3 * i] * h[j] + ht[3 * i + 1] * h[3 + j] + ht[3 * i + 2] * h[6 + j];
+   inv3(G, Gi);
+   int nq = 0, m = 0, site = 0, pf0 = 0;
+   H.saxis = -1;
+   for (int k = 0; k < nsp; k++) {
+      MdSpec &S = H.spec[k];
+      const mdgpu_species &sp = c->spec[k];
+      S.mass = dyn->mass[k];
+      if (!(S.mass > 0.0)) return fail(c, MDGPU_E_ARG, "species mass must be positive");
+      for (int i = 0; i < 3; i++) S.inertia[i] = dyn->inertia[3 * k + i];
+      for (int i = 0; i < 3; i++) {
+         const double *I = S.inertia;
+         S.rinertia[i] = I[i] / (I[(i + 1) % 3] + I[(i + 2) % 3]) < INERTIA_MIN ? 0.0 : 1.0 / I[i];
+      }
+      S.nsites = sp.nsites;
+      S.pf0 = pf0;
+      const double sc = H.half / S.mass;
+      for (int i = 0; i < 9; i++) S.gdrift[i] = sc * Gi[i];
+      const bool rot = dyn->rdof[k] > 0;
+      if (rot && H.saxis < 0) {
+         // near-symmetry axis, chosen once from the first rotating species
+         // as leapf_quat_b's static first-call choice does (src/leapfrog.c:282-297)
+         double idmin = 1e37;
+         for (int i = 0; i < 3; i++) {
+            const double idiff = std::fabs(S.rinertia[(i + 1) % 3] - S.rinertia[(i + 2) % 3]);
+            if (idiff < idmin) {
+               idmin = idiff;
+               H.saxis = i;
+            }
+         }
+      }
+      for (int j = 0; j < sp.nmols; j++, m++) {
+         mol_spec[m] = k;
+         mol_q[m] = rot ? nq++ : -1;
+         mol_site0[m] = site;
+         for (int t = 0; t < sp.nsites; t++, site++) {
+            site_mol[site] = m;
+            site_pf[site] = pf0 + t;
+         }
+      }
+      pf0 += sp.nsites;
+   }
+   if (H.saxis < 0) H.saxis = 0;
+   if (nq > 0 && (!quat || !amom)) return fail(c, MDGPU_E_ARG, "rotating species need quaternions and angular momenta");
+   H.nmols_r = nq;
+   H.dist = distant_const(c);
+   MdDev &D = c->md;
+   cudaStream_t st = c->stream;
+   CK(D.cofm.ensure(3 * (size_t)c->nmols));
+   CK(D.mom.ensure(3 * (size_t)c->nmols));
+   CK(D.quat.ensure(4 * (size_t)nq + 4));
+   CK(D.amom.ensure(4 * (size_t)nq + 4));
+   CK(D.mol_spec.ensure(c->nmols));
+   CK(D.mol_q.ensure(c->nmols));
+   CK(D.mol_site0.ensure(c->nmols));
+   CK(D.site_mol.ensure(c->nsites));
+   CK(D.site_pf.ensure(c->nsites));
+   CK(D.pf.ensure(c->spec_pf.size()));
+   CK(D.spec.ensure(nsp));
+   CK(D.kpart.ensure(2 * (size_t)((c->nmols + 255) / 256)));
+   CK(D.err.ensure(1));
+   CK(cudaMemcpyAsync(D.cofm.p, c_of_m, 3 * (size_t)c->nmols * sizeof(double), cudaMemcpyHostToDevice, st));
+   CK(cudaMemcpyAsync(D.mom.p, mom, 3 * (size_t)c->nmols * sizeof(double), cudaMemcpyHostToDevice, st));
+   if (nq) {
+      CK(cudaMemcpyAsync(D.quat.p, quat, 4 * (size_t)nq * sizeof(double), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(D.amom.p, amom, 4 * (size_t)nq * sizeof(double), cudaMemcpyHostToDevice, st));
+   }
+   CK(cudaMemcpyAsync(D.mol_spec.p, mol_spec.data(), c->nmols * sizeof(int), cudaMemcpyHostToDevice, st));
+   CK(cudaMemcpyAsync(D.mol_q.p, mol_q.data(), c->nmols * sizeof(int), cudaMemcpyHostToDevice, st));
+   CK(cudaMemcpyAsync(D.mol_site0.p, mol_site0.data(), c->nmols * sizeof(int), cudaMemcpyHostToDevice, st));
+   CK(cudaMemcpyAsync(D.site_mol.p, site_mol.data(), c->nsites * sizeof(int), cudaMemcpyHostToDevice, st));
+   CK(cudaMemcpyAsync(D.site_pf.p, site_pf.data(), c->nsites * sizeof(int), cudaMemcpyHostToDevice, st));
+   CK(cudaMemcpyAsync(D.pf.p, c->spec_pf.data(), c->spec_pf.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+   CK(cudaMemcpyAsync(D.spec.p, H.spec.data(), nsp * sizeof(MdSpec), cudaMemcpyHostToDevice, st));
+   CK(cudaMemsetAsync(D.err.p, 0, sizeof(int), st));
+   CK(cudaStreamSynchronize(st));
+   H.ready = true;
+   return MDGPU_OK;
+}
+
+extern "C" mdgpu_status mdgpu_md_run(mdgpu_ctx *c, int nsteps, double *energies)
+{
+   if (!c || nsteps < 0) return fail(c, MDGPU_E_ARG, "invalid argument");
+   if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
+   const MdHost &H = c->mdh;
+   MdDev &D = c->md;
+   cudaStream_t st = c->stream;
+   mdgpu_status s = ensure_ready(c, H.h, true, true);
+   if (s) return s;
+   MdStepParams P;
+   step_params(c, P);
+   const int N = c->nsites, M = c->nmols;
+   const int nbm = (M + 255) / 256;
+   CK(D.energies.ensure(4 * (size_t)(nsteps > 0 ? nsteps : 1)));
+   CK(c->small.ensure(16));
+   const double dist_v = H.dist / det3(H.h);
+   for (int i = 0; i < nsteps; i++) {
+      k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
+                                                   D.amom.p, D.err.p);
+      k_md_sites<<<(N + 255) / 256, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.cofm.p,
+                                                  D.quat.p, c->site.p);
+      CK(cudaGetLastError());
+      c->launches += 2;
+      s = mdgpu_forces_device(c, H.h, c->site.p, D.cofm.p, c->force.p, c->small.p, c->small.p + 2);
+      if (s) return s;
+      k_md_kick<<<nbm, 256, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.mol_site0.p, D.pf.p, c->force.p,
+                                     D.quat.p, D.mom.p, D.amom.p, D.kpart.p);
+      k_md_record<<<1, 32, 0, st>>>(i, c->small.p, D.kpart.p, nbm, dist_v, c->out.p, D.energies.p, D.err.p);
+      k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
+                                                   D.amom.p, D.err.p);
+      CK(cudaGetLastError());
+      c->launches += 3;
+   }
+   int err = 0;
+   if (energies && nsteps > 0)
+      CK(cudaMemcpyAsync(energies, D.energies.p, 4 * (size_t)nsteps * sizeof(double), cudaMemcpyDeviceToHost, st));
+   CK(cudaMemcpyAsync(&err, D.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+   if ((s = sync_out(c)) != MDGPU_OK) return s;
+   if (err & 1) return fail(c, MDGPU_E_RANGE, "Co-ordinate out of range in BIN (fill_cells)");
+   if (err & 2) return fail(c, MDGPU_E_RANGE, "quaternion normalisation error (QNORM2)");
+   return MDGPU_OK;
+}
+
+extern "C" mdgpu_status mdgpu_md_get_state(mdgpu_ctx *c, double *c_of_m, double *mom, double *quat,
+                                           double *amom)
+{
+   if (!c) return MDGPU_E_ARG;
+   if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
+   MdDev &D = c->md;
+   cudaStream_t st = c->stream;
+   const size_t M = c->nmols, Q = c->mdh.nmols_r;
+   if (c_of_m) CK(cudaMemcpyAsync(c_of_m, D.cofm.p, 3 * M * sizeof(double), cudaMemcpyDeviceToHost, st));
+   if (mom) CK(cudaMemcpyAsync(mom, D.mom.p, 3 * M * sizeof(double), cudaMemcpyDeviceToHost, st));
+   if (quat && Q) CK(cudaMemcpyAsync(quat, D.quat.p, 4 * Q * sizeof(double), cudaMemcpyDeviceToHost, st));
+   if (amom && Q) CK(cudaMemcpyAsync(amom, D.amom.p, 4 * Q * sizeof(double), cudaMemcpyDeviceToHost, st));
+   CK(cudaStreamSynchronize(st));
+   return MDGPU_OK;
+}

@@ -66,6 +66,9 @@ void ewald_self_sheet(const std::vector<mdgpu_species> &spec, const std::vector<
 void ewald_self_sheet_grad(const std::vector<mdgpu_species> &spec, const std::vector<double> &spec_pf,
                            const std::vector<double> &chg, double alpha, double vol, double *g_chg,
                            double *g_alpha);
+// Constant of the distant-potential correction (distant_const,
+// src/accel.c:293-328 with dist_pot, src/kernel.c:103-150): energy x volume.
+double distant_const(const mdgpu_ctx *c);
 double det3(const double *a);
 void inv3(const double *a, double *b);
 
@@ -159,6 +162,32 @@ struct AdjDev {
    DBuf<double> blk;       // per-block k-space dE/dalpha, dG/dalpha
 };
 
+// Rigid-molecule dynamics (integrate.cu): one species' constants.
+struct MdSpec {
+   double mass;
+   double inertia[3], rinertia[3];   // principal moments and their inverses
+   double gdrift[9];                 // (dt/2 / mass) (h^T h)^-1, leapf_com's matrix
+   int nsites, pf0;                  // sites per molecule, first principal-frame site
+};
+
+struct MdHost {
+   bool ready = false;
+   std::vector<MdSpec> spec;
+   double h[9];
+   double half = 0;                  // dt / 2
+   double dist = 0;                  // distant-potential constant (energy x volume)
+   int nosym = 0, saxis = 0, nmols_r = 0;
+};
+
+struct MdDev {
+   DBuf<double> cofm, mom, quat, amom;   // [nmols][3], [nmols][3], [nmols_r][4] x2
+   DBuf<int> mol_spec, mol_q, mol_site0, site_mol, site_pf;
+   DBuf<double> pf;                      // principal-frame sites of every species
+   DBuf<MdSpec> spec;
+   DBuf<double> kpart, energies;
+   DBuf<int> err;
+};
+
 }  // namespace mdgpu
 
 struct mdgpu_ctx {
@@ -192,6 +221,8 @@ struct mdgpu_ctx {
    mdgpu::RsDev rd;
    mdgpu::KsDev kd;
    mdgpu::AdjDev ad;
+   mdgpu::MdHost mdh;
+   mdgpu::MdDev md;
    mdgpu::DBuf<double> site, force, force_in, cofm_in, small;
    const double *cur_site = nullptr;   // site array of the launch in progress
    std::vector<double> last_cofm;      // centres of mass of the last force_calc

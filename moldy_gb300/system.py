@@ -85,6 +85,8 @@ class System:
     c_of_m: np.ndarray           # [nmols, 3] fractional centres of mass
     control: Control
     name: str = "system"
+    site_mass: Optional[np.ndarray] = None   # [max_id] mass per site identifier, amu
+    quat: Optional[np.ndarray] = None        # [nmols_r, 4] orientations of rotating molecules
 
     @property
     def max_id(self) -> int:
@@ -219,7 +221,7 @@ def argon_fcc(ncell: int = 5, density: float = 0.0213, displacement: float = 0.1
     return System(h=h, species=[spec], ptype=LJPOT, potpar=potpar,
                   site_charge=np.zeros(max_id), site=x, c_of_m=c_of_m,
                   control=Control(cutoff=cutoff, alpha=-1.0, subcell=subcell, strict_cutoff=strict),
-                  name=f"argon{natoms}")
+                  name=f"argon{natoms}", site_mass=np.array([0.0, 39.948]))
 
 
 def tip4p_geometry():
@@ -279,7 +281,7 @@ def water(nside: int = 8, density_gcc: float = 1.0, seed: int = 2, alpha: float 
                   site=x, c_of_m=com_frac.copy(),
                   control=Control(cutoff=cutoff, alpha=alpha, k_cutoff=k_c, subcell=subcell,
                                   strict_cutoff=strict, molpbc=molpbc),
-                  name=f"water{4 * nmols}")
+                  name=f"water{4 * nmols}", site_mass=np.array([0.0, 16.0, 1.0, 0.0]), quat=q)
 
 
 def rock_salt(ncell: int = 16, a: float = 5.64, displacement: float = 0.1, seed: int = 3,
@@ -317,7 +319,7 @@ def rock_salt(ncell: int = 16, a: float = 5.64, displacement: float = 0.1, seed:
     return System(h=h, species=species, ptype=E6POT, potpar=potpar, site_charge=site_charge,
                   site=x, c_of_m=c_of_m,
                   control=Control(cutoff=cutoff, alpha=alpha, k_cutoff=k_c),
-                  name=f"rocksalt{2 * n}")
+                  name=f"rocksalt{2 * n}", site_mass=np.array([0.0, 22.98977, 35.453]))
 
 
 def generic_ions(ptype: int, n: int = 256, L: float = 20.0, seed: int = 4, alpha: float = 0.35,
@@ -434,6 +436,10 @@ def save_npz(path: str, sysm: System, **extra) -> None:
              spec_fw=np.array([int(s.framework) for s in sysm.species]),
              spec_ids=np.concatenate([s.site_id for s in sysm.species]),
              spec_pf=np.concatenate([s.p_f_sites for s in sysm.species]))
+    if sysm.site_mass is not None:
+        d["site_mass"] = sysm.site_mass
+    if sysm.quat is not None:
+        d["quat"] = sysm.quat
     d.update(extra)
     np.savez_compressed(path, **d)
 
@@ -451,5 +457,5 @@ def load_npz(path: str):
                   site_charge=z["site_charge"], site=z["site"], c_of_m=z["c_of_m"],
                   control=Control(cutoff=float(c[0]), alpha=float(c[1]), k_cutoff=float(c[2]),
                                   subcell=float(c[3]), strict_cutoff=bool(c[4]), molpbc=bool(c[5])),
-                  name=str(z["name"]))
+                  name=str(z["name"]), site_mass=z.get("site_mass"), quat=z.get("quat"))
     return sysm, z

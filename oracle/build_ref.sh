@@ -11,6 +11,8 @@
 #                         -funroll-loops on auxil.c (src/Makefile.am:75-88):
 #                         the timed CPU baseline
 #   moldy_ref_harness[_fast]  oracle/ref_harness.c linked against each
+#   moldy_ref_examples        oracle/ref_examples.c (start-up of the examples)
+#   moldy_ref_md[_fast]       oracle/ref_md.c (constant-energy do_step runs)
 # All of main.c is left out; the harness defines control/ithread/nthreads
 # (src/main.c:83-84).  version.h (normally written by a git hook) is generated
 # into oracle/_ref/.  Exits 0 without building when the sources are absent.
@@ -50,3 +52,7 @@ $CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_harness.c" -o "$OUT/mol
 echo "build_ref: built $OUT/moldy_ref_harness and $OUT/moldy_ref_harness_fast"
 $CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_examples.c" -o "$OUT/moldy_ref_examples" \
     -L"$OUT" -lmoldyref -Wl,-rpath,"$OUT" -ldl -lm
+$CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_md.c" -o "$OUT/moldy_ref_md" \
+    -L"$OUT" -lmoldyref -Wl,-rpath,"$OUT" -ldl -lm
+$CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_md.c" -o "$OUT/moldy_ref_md_fast" \
+    -L"$OUT" -lmoldyref_fast -Wl,-rpath,"$OUT" -ldl -lm

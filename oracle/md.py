@@ -1,0 +1,65 @@
+"""Runs the reference's own constant-energy dynamics (oracle/ref_md.c, do_step
+of src/accel.c:626-827 compiled from the reference sources by
+oracle/build_ref.sh) from a given state.
+
+TEST INFRASTRUCTURE ONLY: it makes the golden trajectories the GPU
+integrator is checked against (tests/golden/make_md_golden.py).  The product
+path never imports this module.
+"""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import tempfile
+from typing import Tuple
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.path.join(HERE, "_ref")
+
+
+def write_mdstate(path: str, sysm, dyn, state, nsteps: int) -> None:
+    c = sysm.control
+    with open(path, "wb") as f:
+        f.write(b"MDSTAT1\0")
+        f.write(struct.pack("<10i", sysm.nsites, sysm.nmols, len(sysm.species), sysm.max_id, sysm.ptype,
+                            int(c.strict_cutoff), int(c.molpbc), int(dyn.nosymmetric_rot), int(nsteps), 0))
+        f.write(struct.pack("<5d", c.cutoff, c.subcell, c.alpha, c.k_cutoff, dyn.step))
+        f.write(np.ascontiguousarray(sysm.h, "<f8").tobytes())
+        for k, sp in enumerate(sysm.species):
+            f.write(struct.pack("<4i", sp.nsites, sp.nmols, int(sp.framework), int(dyn.rdof[k])))
+            f.write(np.ascontiguousarray(sp.site_id, "<i4").tobytes())
+            f.write(np.ascontiguousarray(sp.p_f_sites, "<f8").tobytes())
+            f.write(struct.pack("<4d", dyn.mass[k], *dyn.inertia[k]))
+        f.write(np.ascontiguousarray(sysm.potpar, "<f8").tobytes())
+        f.write(np.ascontiguousarray(sysm.site_charge, "<f8").tobytes())
+        for a in (state.c_of_m, state.mom, state.quat, state.amom):
+            f.write(np.ascontiguousarray(a, "<f8").tobytes())
+
+
+def run(sysm, dyn, state, nsteps: int, fast: bool = False) -> Tuple[np.ndarray, object, float]:
+    """(records [nsteps, 3] = (H_0, pe[0], pe[1]) per step, final MDState,
+    seconds per step).  The reference prints its notes to stdout."""
+    from moldy_gb300.dynamics import MDState
+    exe = os.path.join(REF, "moldy_ref_md_fast" if fast else "moldy_ref_md")
+    if not os.path.exists(exe):
+        raise FileNotFoundError(f"{exe}: build it with oracle/build_ref.sh")
+    nm, nq = sysm.nmols, len(state.quat)
+    with tempfile.TemporaryDirectory() as d:
+        pin, pout = os.path.join(d, "in.mdstate"), os.path.join(d, "out.bin")
+        write_mdstate(pin, sysm, dyn, state, nsteps)
+        subprocess.run([exe, pin, pout], check=True, cwd=d, stdout=subprocess.DEVNULL)
+        raw = np.fromfile(pout, "<f8")
+    o = 3 * nsteps
+    rec = raw[:o].reshape(nsteps, 3)
+    cm = raw[o:o + 3 * nm].reshape(nm, 3)
+    o += 3 * nm
+    mo = raw[o:o + 3 * nm].reshape(nm, 3)
+    o += 3 * nm
+    qu = raw[o:o + 4 * nq].reshape(nq, 4)
+    o += 4 * nq
+    am = raw[o:o + 4 * nq].reshape(nq, 4)
+    o += 4 * nq
+    return rec, MDState(cm, mo, qu, am), float(raw[o])

@@ -1,0 +1,160 @@
+/*
+ * ref_md.c -- TEST INFRASTRUCTURE ONLY.  Runs the reference's own
+ * constant-energy dynamics (do_step, src/accel.c:626-827, with
+ * eval_forces, force_calc, ewald and the leapfrog of src/leapfrog.c) from a
+ * given state, and records the conserved quantity do_step evaluates at the
+ * half kick (H_0, src/accel.c:718-727; asked for every step) with the two
+ * potential-energy parts, then the final state.  The golden trajectories of
+ * the GPU integrator's tests come from here.
+ *
+ * usage: moldy_ref_md in.mdstate out.bin
+ *
+ * in.mdstate (little-endian, written by oracle/md.py):
+ *   "MDSTAT1\0"
+ *   int32  nsites nmols nspecies max_id ptype strict molpbc nosym nsteps 0
+ *   f64    cutoff subcell alpha k_cutoff step
+ *   f64    h[3][3]
+ *   per species: int32 nsites nmols framework rdof; int32 site_id[nsites];
+ *                f64 p_f_sites[nsites][3]; f64 mass inertia[3]
+ *   f64    potpar[max_id*max_id][8]; f64 charge[max_id]
+ *   f64    c_of_m[nmols][3] mom[nmols][3] quat[nmols_r][4] amom[nmols_r][4]
+ * out.bin: f64 per step (H_0, pe[0], pe[1]); then c_of_m, mom, quat, amom;
+ *   then f64 seconds per step.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include "defs.h"
+#include "structs.h"
+
+contr_mt control;
+int ithread = 0, nthreads = 1;
+
+void do_step(system_mt *, spec_mt *, site_mt *, pot_mt *, vec_mt (*)[2], double *, real *, mat_mt,
+             restrt_mt *, int, int);
+
+static void rd(void *p, size_t sz, size_t n, FILE *f)
+{
+   if (fread(p, sz, n, f) != n) { fprintf(stderr, "ref_md: short read\n"); exit(2); }
+}
+
+int main(int argc, char **argv)
+{
+   FILE *f, *o;
+   char magic[8];
+   int hdr[10], s, i, nsteps, nq = 0, imol = 0, iq = 0;
+   double cd[5];
+   system_mt sys;
+   spec_mt *species;
+   site_mt *site_info;
+   pot_mt *potpar;
+   restrt_mt rh;
+   double pe[NPE];
+   real dip[3];
+   mat_mt stress;
+   vec_mt (*msq)[2];
+   struct timespec t0, t1;
+
+   if (argc < 3) { fprintf(stderr, "usage: %s in.mdstate out.bin\n", argv[0]); return 2; }
+   f = fopen(argv[1], "rb");
+   if (!f) { perror(argv[1]); return 2; }
+   rd(magic, 1, 8, f);
+   if (memcmp(magic, "MDSTAT1", 7)) { fprintf(stderr, "ref_md: bad magic\n"); return 2; }
+   rd(hdr, 4, 10, f);
+   rd(cd, 8, 5, f);
+   memset(&sys, 0, sizeof sys);
+   memset(&control, 0, sizeof control);
+   memset(&rh, 0, sizeof rh);
+   sys.nsites = hdr[0]; sys.nmols = hdr[1]; sys.nspecies = hdr[2]; sys.max_id = hdr[3];
+   sys.ptype = hdr[4];
+   {
+      /* parameter count of each potential type (src/kernel.c:61-68) */
+      static const int npar[7] = {2, 3, 4, 6, 3, 0, 7};
+      if (sys.ptype < 0 || sys.ptype > 6 || npar[sys.ptype] == 0) { fprintf(stderr, "ref_md: ptype\n"); return 2; }
+      sys.n_potpar = npar[sys.ptype];
+   }
+   control.strict_cutoff = hdr[5]; control.molpbc = hdr[6]; control.nosymmetric_rot = hdr[7];
+   nsteps = hdr[8];
+   control.cutoff = cd[0]; control.subcell = cd[1]; control.alpha = cd[2]; control.k_cutoff = cd[3];
+   control.step = cd[4];
+   control.ttmass = 1.0; control.pmass = 1.0;   /* unused at constant energy, kept finite */
+   control.print_interval = 1000000000;
+   sys.h = (mat_mp)calloc(1, sizeof(mat_mt));
+   sys.hmom = (mat_mp)calloc(1, sizeof(mat_mt));
+   sys.hmomp = (mat_mp)calloc(1, sizeof(mat_mt));
+   rd(sys.h, 8, 9, f);
+   sys.ts = 1.0; sys.tsmom = 0.0;
+   species = (spec_mt *)calloc(sys.nspecies, sizeof(spec_mt));
+   for (s = 0; s < sys.nspecies; s++) {
+      int sh[4];
+      double mi[4];
+      spec_mt *sp = species + s;
+      rd(sh, 4, 4, f);
+      sp->nsites = sh[0]; sp->nmols = sh[1]; sp->framework = sh[2]; sp->rdof = sh[3];
+      sp->site_id = (int *)malloc(sizeof(int) * sp->nsites);
+      sp->p_f_sites = (vec_mp)malloc(sizeof(vec_mt) * sp->nsites);
+      rd(sp->site_id, 4, sp->nsites, f);
+      rd(sp->p_f_sites, 8, 3 * sp->nsites, f);
+      rd(mi, 8, 4, f);
+      sp->mass = mi[0]; sp->inertia[0] = mi[1]; sp->inertia[1] = mi[2]; sp->inertia[2] = mi[3];
+      if (sp->rdof > 0) nq += sp->nmols;
+      sys.d_of_f += 3 * sp->nmols + sp->rdof * sp->nmols;
+   }
+   sys.d_of_f -= 3;
+   sys.nmols_r = nq;
+   potpar = (pot_mt *)calloc((size_t)sys.max_id * sys.max_id, sizeof(pot_mt));
+   for (i = 0; i < sys.max_id * sys.max_id; i++) rd(potpar[i].p, 8, NPOTP, f);
+   site_info = (site_mt *)calloc(sys.max_id, sizeof(site_mt));
+   for (i = 0; i < sys.max_id; i++) rd(&site_info[i].charge, 8, 1, f);
+   sys.c_of_m = (vec_mp)malloc(sizeof(vec_mt) * sys.nmols);
+   sys.mom = (vec_mp)malloc(sizeof(vec_mt) * sys.nmols);
+   sys.momp = (vec_mp)calloc(sys.nmols, sizeof(vec_mt));
+   sys.quat = (quat_mp)malloc(sizeof(quat_mt) * (nq ? nq : 1));
+   sys.amom = (quat_mp)malloc(sizeof(quat_mt) * (nq ? nq : 1));
+   sys.amomp = (quat_mp)calloc(nq ? nq : 1, sizeof(quat_mt));
+   rd(sys.c_of_m, 8, 3 * (size_t)sys.nmols, f);
+   rd(sys.mom, 8, 3 * (size_t)sys.nmols, f);
+   if (nq) {
+      rd(sys.quat, 8, 4 * (size_t)nq, f);
+      rd(sys.amom, 8, 4 * (size_t)nq, f);
+   }
+   fclose(f);
+   /* species arrays point into the whole-system ones (src/startup.c:640-660) */
+   for (s = 0; s < sys.nspecies; s++) {
+      spec_mt *sp = species + s;
+      sp->c_of_m = sys.c_of_m + imol;
+      sp->mom = sys.mom + imol;
+      sp->momp = sys.momp + imol;
+      if (sp->rdof > 0) {
+         sp->quat = sys.quat + iq;
+         sp->amom = sys.amom + iq;
+         sp->amomp = sys.amomp + iq;
+         iq += sp->nmols;
+      }
+      imol += sp->nmols;
+   }
+   msq = (vec_mt(*)[2])calloc(sys.nspecies, sizeof(vec_mt[2]));
+   o = fopen(argv[2], "wb");
+   if (!o) { perror(argv[2]); return 2; }
+   clock_gettime(CLOCK_MONOTONIC, &t0);
+   for (control.istep = 1; control.istep <= nsteps; control.istep++) {
+      double rec[3];
+      do_step(&sys, species, site_info, potpar, msq, pe, dip, stress, &rh, 0, 1);
+      rec[0] = sys.H_0; rec[1] = pe[0]; rec[2] = pe[1];
+      fwrite(rec, 8, 3, o);
+   }
+   clock_gettime(CLOCK_MONOTONIC, &t1);
+   fwrite(sys.c_of_m, 8, 3 * (size_t)sys.nmols, o);
+   fwrite(sys.mom, 8, 3 * (size_t)sys.nmols, o);
+   if (nq) {
+      fwrite(sys.quat, 8, 4 * (size_t)nq, o);
+      fwrite(sys.amom, 8, 4 * (size_t)nq, o);
+   }
+   {
+      double sec = ((t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec)) / (nsteps > 0 ? nsteps : 1);
+      fwrite(&sec, 8, 1, o);
+   }
+   fclose(o);
+   return 0;
+}

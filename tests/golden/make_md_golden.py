@@ -1,0 +1,75 @@
+"""Generate the dynamics fixtures tests/golden/md_*.npz from the reference's
+own constant-energy integrator (do_step, driven by oracle/ref_md.c, built in
+place from the reference sources by oracle/build_ref.sh).
+
+Each short fixture holds a System, the per-species constants (mass,
+principal moments, rotational freedom), the timestep, a seeded thermal
+start (moldy_gb300.dynamics.thermal_state), the reference's per-step
+records (H_0 at the half kick, pe[0], pe[1]) and its final state.
+
+The drift fixtures (md_drift_*) hold the reference's conserved quantity
+every step of a long run (10^4 steps of 2048-site water at 1 fs, lazy and
+strict cutoffs; 1000 steps of 500-atom argon at 10 fs) and its CPU time per
+step, for the energy-drift comparison.
+
+usage: python tests/golden/make_md_golden.py [--skip-drift]
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import dataclasses  # noqa: E402
+
+import numpy as np  # noqa: E402
+
+from moldy_gb300 import system as S  # noqa: E402
+from moldy_gb300.dynamics import species_dynamics, thermal_state  # noqa: E402
+from oracle import md  # noqa: E402
+
+
+def case(sysm, step, temp, seed, nsteps, nosym=False):
+    dyn = species_dynamics(sysm, step, nosym)
+    st = thermal_state(sysm, dyn, temp, seed)
+    rec, fin, sec = md.run(sysm, dyn, st, nsteps)
+    return dyn, st, rec, fin, sec
+
+
+def save(name, sysm, dyn, st, rec, fin, sec, temp, seed, **extra):
+    S.save_npz(os.path.join(HERE, name + ".npz"), sysm,
+               md_mass=dyn.mass, md_inertia=dyn.inertia, md_rdof=dyn.rdof, md_step=dyn.step,
+               md_nosym=int(dyn.nosymmetric_rot), md_temp=temp, md_seed=seed,
+               c_of_m0=st.c_of_m, mom0=st.mom, quat0=st.quat, amom0=st.amom,
+               ref_rec=rec, c_of_m1=fin.c_of_m, mom1=fin.mom, quat1=fin.quat, amom1=fin.amom,
+               ref_sec_per_step=sec, **extra)
+    print(name, sysm.nsites, "sites", len(rec), "steps", "%.3g s/step" % sec)
+
+
+def main():
+    subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    w = S.water(nside=6, seed=3)
+    save("md_water864", w, *case(w, 0.001, 300.0, 4, 30), 300.0, 4)
+    ws = dataclasses.replace(w, control=dataclasses.replace(w.control, strict_cutoff=True))
+    save("md_water864_strict_nosym", ws, *case(ws, 0.001, 300.0, 5, 30, nosym=True), 300.0, 5)
+    wm = S.water(nside=6, seed=3, molpbc=True)
+    save("md_water864_molpbc", wm, *case(wm, 0.001, 300.0, 6, 30), 300.0, 6)
+    ar = S.argon_fcc()
+    save("md_argon500", ar, *case(ar, 0.01, 120.0, 7, 50), 120.0, 7)
+    rs = S.rock_salt(ncell=4)
+    save("md_rocksalt512", rs, *case(rs, 0.002, 300.0, 8, 30), 300.0, 8)
+    if "--skip-drift" in sys.argv:
+        return
+    w2 = S.water(nside=8, seed=11)
+    for strict in (False, True):
+        s = dataclasses.replace(w2, control=dataclasses.replace(w2.control, strict_cutoff=strict))
+        dyn, st, rec, fin, sec = case(s, 0.001, 300.0, 12, 10000)
+        save("md_drift_water2048" + ("_strict" if strict else ""), s, dyn, st, rec, fin, sec, 300.0, 12)
+    dyn, st, rec, fin, sec = case(ar, 0.01, 120.0, 13, 1000)
+    save("md_drift_argon500", ar, dyn, st, rec, fin, sec, 120.0, 13)
+
+
+if __name__ == "__main__":
+    main()

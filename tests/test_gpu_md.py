@@ -1,0 +1,109 @@
+"""GPU rigid-molecule dynamics (mdgpu_md_*) against the reference's own
+integrator: per-step conserved quantity and potential energies, and the
+final state, from the same seeded thermal start (fixtures made by
+tests/golden/make_md_golden.py with do_step of the reference)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+SHORT = ["md_water864", "md_water864_strict_nosym", "md_water864_molpbc", "md_argon500", "md_rocksalt512"]
+
+
+def _load(name):
+    from moldy_gb300 import system
+    from moldy_gb300.dynamics import Dynamics, MDState
+    sysm, z = system.load_npz(os.path.join(GOLDEN, name + ".npz"))
+    dyn = Dynamics(z["md_mass"], z["md_inertia"], z["md_rdof"], float(z["md_step"]), bool(z["md_nosym"]))
+    st0 = MDState(z["c_of_m0"], z["mom0"], z["quat0"], z["amom0"])
+    st1 = MDState(z["c_of_m1"], z["mom1"], z["quat1"], z["amom1"])
+    return sysm, dyn, st0, st1, z
+
+
+def _run(name, prec):
+    from moldy_gb300 import ForceField
+    from moldy_gb300.dynamics import MolecularDynamics
+    sysm, dyn, st0, st1, z = _load(name)
+    ff = ForceField(sysm, precision=prec)
+    md = MolecularDynamics(ff, dyn, st0)
+    e = md.run(len(z["ref_rec"]))
+    st = md.state()
+    ff.close()
+    return sysm, z, e, st, st1
+
+
+@pytest.mark.parametrize("name", SHORT)
+def test_fp64_dynamics_follows_reference(name):
+    sysm, z, e, st, st1 = _run(name, "fp64")
+    rec = z["ref_rec"]
+    scale = np.abs(e[:, 0]) + np.abs(e[:, 1]) + e[:, 2] + e[:, 3]
+    H = e.sum(1)
+    # the trajectories separate from the first step at the rounding level
+    # (the GPU's FP64 force sums run in another order) and the separation
+    # grows; over these few steps it stays far below 1e-8
+    assert np.all(np.abs(H - rec[:, 0]) <= 1e-8 * scale), np.max(np.abs(H - rec[:, 0]) / scale)
+    assert np.all(np.abs(e[:, 0] - rec[:, 1]) <= 1e-8 * scale)
+    assert np.all(np.abs(e[:, 1] - rec[:, 2]) <= 1e-8 * scale)
+    d = st.c_of_m - st1.c_of_m
+    d -= np.round(d)
+    assert np.max(np.abs(d)) < 1e-9
+    assert np.max(np.abs(st.mom - st1.mom)) <= 1e-7 * np.max(np.abs(st1.mom))
+    if len(st1.quat):
+        # q and -q are the same orientation
+        sgn = np.sign(np.sum(st.quat * st1.quat, 1))[:, None]
+        assert np.max(np.abs(st.quat * sgn - st1.quat)) < 1e-9
+        assert np.max(np.abs(st.amom - st1.amom)) <= 1e-7 * np.max(np.abs(st1.amom))
+
+
+@pytest.mark.parametrize("name", SHORT)
+def test_mixed_dynamics_follows_reference(name):
+    sysm, z, e, st, st1 = _run(name, "mixed")
+    rec = z["ref_rec"]
+    scale = np.abs(e[:, 0]) + np.abs(e[:, 1]) + e[:, 2] + e[:, 3]
+    H = e.sum(1)
+    assert np.all(np.abs(H - rec[:, 0]) <= 2e-5 * scale), np.max(np.abs(H - rec[:, 0]) / scale)
+    d = st.c_of_m - st1.c_of_m
+    d -= np.round(d)
+    assert np.max(np.abs(d)) < 1e-6
+
+
+def test_md_run_needs_init():
+    from moldy_gb300 import ForceField, system
+    from moldy_gb300._lib import MdgpuError
+    ff = ForceField(system.argon_fcc(ncell=3), precision="fp64")
+    with pytest.raises(MdgpuError, match="mdgpu_md_init"):
+        ff._check(ff.L.mdgpu_md_run(ff.ctx, 1, None))
+    ff.close()
+
+
+DRIFT = ["md_drift_water2048", "md_drift_water2048_strict", "md_drift_argon500"]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", DRIFT)
+def test_energy_drift_no_worse_than_reference(name, prec):
+    """The whole reference run (10^4 steps of water, 10^3 of argon) on the
+    GPU from the same start: the least-squares drift of the conserved
+    quantity and its fluctuation about the trend are no larger than the
+    reference's own, within a margin for two chaotic trajectories of the
+    same dynamics."""
+    if not os.path.exists(os.path.join(GOLDEN, name + ".npz")):
+        pytest.skip("drift fixture not generated")
+    from moldy_gb300.dynamics import drift_per_ns
+    sysm, z, e, st, st1 = _run(name, prec)
+    rec = z["ref_rec"]
+    dt = float(z["md_step"])
+    H_ref, H = rec[:, 0], e.sum(1)
+    d_ref = drift_per_ns(np.stack([H_ref, 0 * H_ref, 0 * H_ref, 0 * H_ref], 1), dt)
+    d_gpu = drift_per_ns(e, dt)
+    t = np.arange(len(H))
+    fl_ref = np.std(H_ref - np.polyval(np.polyfit(t, H_ref, 1), t))
+    fl_gpu = np.std(H - np.polyval(np.polyfit(t, H, 1), t))
+    ke = float(np.mean(e[:, 2] + e[:, 3]))
+    # margin: 50% of the reference's figure plus 1e-5 of the kinetic energy
+    assert abs(d_gpu) <= 1.5 * abs(d_ref) + 1e-5 * ke / (len(H) * dt * 1e-3), (d_gpu, d_ref)
+    assert fl_gpu <= 1.5 * fl_ref + 1e-6 * ke, (fl_gpu, fl_ref)
