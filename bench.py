@@ -1,28 +1,37 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 force path on the large rigid-water workload.
 
-A step is one force evaluation of the configuration: link-cell real-space
-forces (force_calc) plus the reciprocal-space Ewald sum (ewald), i.e. the
-work the reference's time step hands to force_calc/ewald.  Workload: rigid
+A step is one constant-energy MD step on the GPU (mdgpu_md_run): half drift
+of centres of mass and quaternions, site co-ordinates, the force evaluation
+-- link-cell real-space forces (force_calc) plus the reciprocal-space Ewald
+sum (ewald), the work the reference's step hands to them -- molecular forces
+and torques, two half kicks and the second half drift.  Workload: rigid
 4-site TIP4P-like water, 32,768 molecules = 131,072 sites in a 99.34 Å cubic
 box at 1.0 g/cm^3, Ewald alpha 0.3 /Å, cutoff 9 Å, k-cutoff for 1e-5 accuracy
-(69,876 k-vectors); seeded lattice positions and uniform random orientations
-(synthetic: there is no dataset).
+(69,876 k-vectors); seeded lattice positions, uniform random orientations and
+300 K Maxwell-Boltzmann momenta, dt = 1 fs (synthetic: there is no dataset).
 
 Default arm (--impl gb300):
-  value      steps/s of the FP32-mixed form, inputs resident in HBM, per-step
-             CUDA events on the launching stream (L2 flushed between steps);
+  value      MD steps/s of the FP32-mixed form, state resident in HBM,
+             per-step CUDA events on the launching stream (L2 flushed between
+             steps);
   fp64       the same for the plain FP64 GPU form, and their ratio;
-  e2e        steps/s through the C ABI with pinned host buffers: the H2D copy
-             of the site co-ordinates and the D2H copy of forces, energies and
-             stress inside every timed step;
+  force_eval the force evaluation alone in both forms; accuracy of the mixed
+             forces against the FP64 ones on the same configuration;
+  nve        constant-energy runs (10^4 mixed steps, 300 FP64 steps by
+             default): steps/s, ns/day, drift of the conserved quantity;
+  e2e        steps/s through the drop-in force call (mdgpu_forces) with
+             pinned host buffers: the H2D copy of the site co-ordinates and
+             the D2H copy of forces, energies and stress inside every step;
   roofline   the dominant kernel's algorithmic FLOP/s (reference op counts)
              against the FP32 FMA peak measured on this GPU;
   cpu_baseline  the reference algorithm's C restatement (oracle/port),
-             -O2 -ffast-math, on all host cores, on a bounded sample.
+             -O2 -ffast-math, on all host cores, on a bounded sample of the
+             force evaluation (the reference's integrator is under 1% of its
+             step at this size).
 --impl reference: the CPU restatement alone (the reference is serial C with no
 GPU code), on this workload, each step a bounded sample extrapolated to one
-full step.
+full force evaluation.
 """
 from __future__ import annotations
 
@@ -54,6 +63,7 @@ WORKLOAD = ("rigid 4-site water (TIP4P-like), 32768 molecules / 131072 sites, cu
 FLOPS_SFAC_PER_SITE_K = 8
 FLOPS_FORCE_PER_SITE_K = 9
 FLOPS_PAIR_LJ_ERFC = 65
+STEP_PS = 0.001                      # 1 fs
 
 
 def log(*a):
@@ -177,7 +187,10 @@ def traffic_from_profiles():
 def run_gpu(args):
     import torch
     from moldy_gb300 import _lib
+    from moldy_gb300.dynamics import (MolecularDynamics, drift_per_ns, ns_per_day, species_dynamics,
+                                      thermal_state)
     from moldy_gb300.forcefield import ForceField
+    from moldy_gb300.system import CONV_E
     import ctypes as C
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -191,8 +204,10 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
 
     sysA = make_workload(seed=7)
-    sysB = make_workload(seed=8)          # alternate configurations step to step
+    sysB = make_workload(seed=8)          # a second configuration for the force-only steps
     n = sysA.nsites
+    dyn = species_dynamics(sysA, STEP_PS)
+    state0 = thermal_state(sysA, dyn, 300.0, seed=9)
     # a dedicated (non-default) stream: the library launches on it and the
     # CUDA events below are recorded on it
     stream = torch.cuda.Stream(device=dev)
@@ -205,17 +220,14 @@ def run_gpu(args):
     d_st = torch.zeros(9, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def step(i):
+    def force_step(i):
         ff.forces_device(d_site[i % 2].data_ptr(), d_force.data_ptr(), d_pe.data_ptr(), d_st.data_ptr())
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    def timed(nsteps, warm):
-        for i in range(warm):
-            step(i)
-        torch.cuda.synchronize()
+    def timed(fn, nsteps):
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(nsteps)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(nsteps)]
         barrier()
@@ -224,7 +236,7 @@ def run_gpu(args):
         for i in range(nsteps):
             flush.zero_()                      # L2 flush between timed steps
             starts[i].record(stream)
-            step(i)
+            fn(i)
             ends[i].record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -232,46 +244,81 @@ def run_gpu(args):
         ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
         return sum(ms) / nsteps, wall
 
-    # ---- mixed form: the headline -------------------------------------
-    sampler = ClockSampler(local)
+    def max_over_ranks(x):
+        t = torch.tensor([x], device=dev)
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- the headline: MD steps on the GPU, mixed form ----------------------
+    md = MolecularDynamics(ff, dyn, state0)
+    md_step = lambda i: md.run(1)          # noqa: E731
     for i in range(args.warmup):
-        step(i)
+        md_step(i)
     torch.cuda.synchronize()
+    sampler = ClockSampler(local)
     launches0 = ff.info()["launches"]
     sampler.start()
     time.sleep(0.3)
-    ms_mixed, wall_mixed = timed(args.steps, 0)
+    ms_mixed, wall_mixed = timed(md_step, args.steps)
     clocks = sampler.stop()
     launches_timed = ff.info()["launches"] - launches0
-    ms_t = torch.tensor([ms_mixed], device=dev)
-    if dist is not None:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_mixed = float(ms_t.item())
-    f_mixed = d_force.clone()
-    step(0)
-    torch.cuda.synchronize()
-    f_mixed = d_force.clone()
-    pe_mixed = d_pe.clone()
+    ms_mixed = max_over_ranks(ms_mixed)
 
-    # ---- phase timing of one evaluation (CUDA events inside the library) --
+    # ---- FP64 form of the same MD step -----------------------------------------
+    ff.set_precision("fp64")
+    md_step(0)
+    ms_fp64, _ = timed(md_step, max(1, args.fp64_steps))
+    ms_fp64 = max_over_ranks(ms_fp64)
+    ff.set_precision("mixed")
+
+    # ---- force evaluation alone: accuracy, phases -------------------------------
+    force_step(0)
+    torch.cuda.synchronize()
+    f_mixed, pe_mixed = d_force.clone(), d_pe.clone()
+    ms_force_mixed, _ = timed(force_step, args.steps)
     ff.set_phase_timing(True)
     phases = None
     for i in range(3):
         flush.zero_()
-        step(i)
+        force_step(i)
         ph = ff.phase_times()
         phases = ph if phases is None else {k: min(phases[k], ph[k]) for k in ph}
     ff.set_phase_timing(False)
-
-    # ---- FP64 form ---------------------------------------------------------
     ff.set_precision("fp64")
-    ms_fp64, _ = timed(max(1, args.fp64_steps), 1)
-    step(0)
+    ms_force_fp64, _ = timed(force_step, max(1, args.fp64_steps))
+    force_step(0)
     torch.cuda.synchronize()
-    f64 = d_force.clone()
-    pe64 = d_pe.clone()
+    f64, pe64 = d_force.clone(), d_pe.clone()
     ferr = float(torch.sqrt(((f_mixed - f64) ** 2).sum() / (f64 ** 2).sum()).item())
     e_err = float((pe_mixed.sum() - pe64.sum()).abs().item() / pe64.sum().abs().item())
+    ff.set_precision("mixed")
+
+    # ---- NVE runs: steps/s, ns/day and energy drift ------------------------------
+    nve = {}
+    for prec, nsteps in (("mixed", args.nve_steps), ("fp64", args.nve_fp64_steps)):
+        if nsteps <= 0:
+            continue
+        ff.set_precision(prec)
+        run = MolecularDynamics(ff, dyn, state0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        en = run.run(nsteps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3 / nsteps
+        H = en.sum(1)
+        ke = float(np.mean(en[:, 2] + en[:, 3]))
+        half = en[nsteps // 2:]
+        nve[prec] = {"steps": nsteps, "step_fs": STEP_PS * 1e3, "steps_per_s": 1.0 / sec,
+                     "ns_per_day": ns_per_day(1.0 / sec, STEP_PS),
+                     "drift_kjmol_per_ns_per_mol": drift_per_ns(en, STEP_PS, sysA.nmols) * CONV_E,
+                     "drift_second_half_kjmol_per_ns_per_mol": drift_per_ns(half, STEP_PS, sysA.nmols) * CONV_E,
+                     "H_first_last_kjmol_per_mol": [float(H[0]) * CONV_E / sysA.nmols,
+                                                    float(H[-1]) * CONV_E / sysA.nmols],
+                     "ke_mean_kjmol_per_mol": ke * CONV_E / sysA.nmols,
+                     "timing": "one CUDA-event interval around the whole run (no L2 flush)"}
     ff.set_precision("mixed")
 
     # ---- end to end through the C ABI, pinned host buffers -------------------
@@ -298,11 +345,7 @@ def run_gpu(args):
     for i in range(args.steps):
         e2e_step(i)
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_t = torch.tensor([e2e_s], device=dev)
-    if dist is not None:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_s = float(e2e_t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
     info = ff.info()
 
     # ---- roofline of the dominant kernel ---------------------------------------
@@ -323,8 +366,8 @@ def run_gpu(args):
         log("timing the CPU baseline (reference algorithm restated in C) ...")
         sec, det = cpu_baseline(sysA)
         cpu = {"value": 1.0 / sec, "unit": "steps/s", "cores": det["threads"], "kind": "port",
-               "sample": (f"full real-space pass ({det['pairs']} pairs, {det['t_real_s']:.2f} s) + "
-                          f"k-vectors [0,{det['k_sample']}) of {det['nkvec']} "
+               "sample": (f"force evaluation only: full real-space pass ({det['pairs']} pairs, "
+                          f"{det['t_real_s']:.2f} s) + k-vectors [0,{det['k_sample']}) of {det['nkvec']} "
                           f"({det['t_ewald_sample_s']:.2f} s), Ewald extrapolated to "
                           f"{det['t_ewald_est_s']:.2f} s; -O2 -ffast-math, {det['threads']} threads")}
 
@@ -332,17 +375,23 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (f64 accumulation)",
-        "data": "synthetic (seeded lattice water, uniform random orientations)",
+        "vs_baseline": None, "dtype": "f32 (f64 accumulation; f64 integrator)",
+        "data": "synthetic (seeded lattice water, uniform random orientations, 300 K Maxwell-Boltzmann)",
         "config": {"workload": WORKLOAD, "nsites": n, "nkvec": nk, "pairs_per_step": info["npairs"],
+                   "step": "one constant-energy MD step on the GPU (half drift, sites, forces, "
+                           "molecular forces/torques, kicks, half drift), dt = 1 fs",
                    "l2": "flushed between timed steps (256 MiB write); per-step CUDA events summed",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"value": world * 1e3 / ms_fp64, "unit": "steps/s", "ms_per_step": ms_fp64,
                  "steps": max(1, args.fp64_steps)},
         "mixed_over_fp64": ms_fp64 / ms_mixed,
+        "force_eval": {"ms_mixed": ms_force_mixed, "ms_fp64": ms_force_fp64,
+                       "mixed_over_fp64": ms_force_fp64 / ms_force_mixed},
         "accuracy": {"force_rel_rms_mixed_vs_fp64": ferr, "energy_rel_mixed_vs_fp64": e_err},
+        "nve": nve,
         "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 3 * n * 8,
-                "d2h_bytes_per_step": 3 * n * 8 + 11 * 8 + 512},
+                "d2h_bytes_per_step": 3 * n * 8 + 11 * 8 + 512,
+                "path": "mdgpu_forces (the drop-in force call) on host arrays each step"},
         "gpu_launches": int(launches_timed),
         "phases_ms": phases,
         "roofline": {"kernel": kernel_names[dom], "bound": "fp32", "achieved": achieved,
@@ -362,6 +411,79 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_adjoint(args):
+    """Force-matching gradients on the adjoint workload: rigid water, 4096
+    molecules (16,384 sites), a batch of seeded frames; epsilon, sigma and
+    q_H scaled by seeded factors in [0.9, 1.1] (q_M = -2 q_H); reference
+    forces at the original parameters.  Times the loss + gradient over the
+    batch (torch autograd over the C ABI) in both forms and checks the
+    gradient with respect to (epsilon, sigma, q_H, alpha) against central
+    finite differences of the FP64 C restatement on all host cores."""
+    import torch
+    from moldy_gb300 import system as S
+    from moldy_gb300.fitting import FitProblem, ForceMatchLoss, water_frames, water_tables
+    from moldy_gb300.forcefield import ForceField
+    from oracle import port
+    import dataclasses
+
+    base = S.water(nside=16, seed=21)
+    frames = water_frames(base, args.adjoint_frames, seed=22)
+    theta0 = np.array([0.6485, 3.154, 0.52, base.control.alpha])
+    theta = theta0 * np.append(np.random.default_rng(23).uniform(0.9, 1.1, 3), 1.0)
+    threads = os.cpu_count() or 1
+
+    def sys_at(t, fr):
+        pot, _ = water_tables(*[torch.tensor(v, dtype=torch.float64) for v in t[:3]], base)
+        qid = np.zeros(base.max_id)
+        qid[2], qid[3] = t[2] / S.CONV_Q, -2 * t[2] / S.CONV_Q
+        return dataclasses.replace(fr, potpar=pot.numpy(), site_charge=qid,
+                                   control=dataclasses.replace(base.control, alpha=float(t[3])))
+
+    def port_forces(sysm):
+        return port.force_calc(sysm, nthreads=threads, fast=False).force + \
+            port.ewald(sysm, nthreads=threads, fast=False).force
+
+    t0 = time.perf_counter()
+    f_refs = [port_forces(sys_at(theta0, fr)) for fr in frames]
+    w = 1.0 / (len(frames) * f_refs[0].size)
+
+    def oracle_loss(t):
+        return sum(w * float(np.sum((port_forces(sys_at(t, fr)) - f) ** 2)) for fr, f in zip(frames, f_refs))
+
+    fd = np.zeros(4)
+    for k in range(4):
+        h = 1e-5 * theta[k]
+        tp, tm = theta.copy(), theta.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd[k] = (oracle_loss(tp) - oracle_loss(tm)) / (2 * h)
+    t_fd = time.perf_counter() - t0
+    out = {"metric": "force-matching loss gradient, water 16,384 sites", "unit": "s per batch",
+           "frames": len(frames), "theta": theta.tolist(), "fd_grad": fd.tolist(),
+           "fd": f"central, step 1e-5 relative, FP64 C restatement on {threads} threads ({t_fd:.0f} s)"}
+    for prec in ("mixed", "fp64"):
+        ff = ForceField(sys_at(theta, frames[0]), precision=prec)
+        pb = FitProblem(ff, [f.site for f in frames], [f.c_of_m for f in frames], f_refs, w)
+        res = None
+        for rep in range(2):   # the first pass uploads tables and builds the k-list
+            t = [torch.tensor(v, dtype=torch.float64, requires_grad=True) for v in theta]
+            pot, chg = water_tables(t[0], t[1], t[2], base)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            L = ForceMatchLoss.apply(pot, chg, t[3], pb)
+            t2 = time.perf_counter()
+            L.backward()
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            g = np.array([float(x.grad) for x in t])
+            res = {"loss": L.item(), "grad": g.tolist(), "rel_err_vs_fd": (np.abs(g - fd) / np.abs(fd)).tolist(),
+                   "s_forward": t2 - t1, "s_backward": t3 - t2,
+                   "ms_per_frame_loss_and_grad": 1e3 * (t3 - t1) / len(frames)}
+        out[prec] = res
+        ff.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -370,6 +492,13 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nve-steps", type=int, default=10000,
+                    help="mixed-form constant-energy run for ns/day and drift (0: skip)")
+    ap.add_argument("--nve-fp64-steps", type=int, default=300,
+                    help="FP64-form constant-energy run (0: skip)")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="run the force-matching gradient workload instead (prints its own JSON line)")
+    ap.add_argument("--adjoint-frames", type=int, default=64)
     ap.add_argument("--profile-case", choices=["mixed", "fp64"],
                     help="run three untimed evaluations of the workload and exit (for ncu captures)")
     args = ap.parse_args()
@@ -380,7 +509,9 @@ def main():
             _, pe, _ = ff.forces()
         log("profile case done", pe)
         return
-    if args.impl == "reference":
+    if args.adjoint:
+        run_adjoint(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

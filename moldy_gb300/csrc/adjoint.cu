@@ -543,17 +543,20 @@ extern "C" mdgpu_status mdgpu_set_params(mdgpu_ctx *c, const mdgpu_params *p)
          c->potpar.assign(p->potpar, p->potpar + n);
          c->sys_dirty = true;
          c->have_eintra = false;
+         c->gen++;
       }
    }
    if (p->chg && std::memcmp(p->chg, c->chg.data(), c->chg.size() * sizeof(double)) != 0) {
       c->chg.assign(p->chg, p->chg + c->nsites);
       c->sys_dirty = true;
+      c->gen++;
       c->have_eintra = false;
       c->have_self = false;
    }
    if (p->alpha > 0.0 && p->alpha != c->ctl.alpha) {
       if (!c->have_control) return fail(c, MDGPU_E_ARG, "mdgpu_set_control has not been called");
       c->ctl.alpha = p->alpha;
+      c->gen++;
       c->have_eintra = false;
       c->have_self = false;
    }

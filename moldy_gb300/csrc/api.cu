@@ -294,6 +294,11 @@ void mdgpu_destroy(mdgpu_ctx *c)
    a.gkpart.release(); a.blk.release();
    c->site.release(); c->force.release(); c->force_in.release(); c->cofm_in.release(); c->out.release();
    c->small.release();
+   if (c->mdh.graph) cudaGraphExecDestroy(c->mdh.graph);
+   MdDev &m = c->md;
+   m.cofm.release(); m.mom.release(); m.quat.release(); m.amom.release(); m.counter.release();
+   m.mol_spec.release(); m.mol_q.release(); m.mol_site0.release(); m.site_mol.release(); m.site_pf.release();
+   m.pf.release(); m.spec.release(); m.kpart.release(); m.energies.release(); m.err.release();
    if (c->h_out) cudaFreeHost(c->h_out);
    for (auto &e : c->ev)
       if (e) cudaEventDestroy(e);
@@ -310,6 +315,7 @@ mdgpu_status mdgpu_set_precision(mdgpu_ctx *c, mdgpu_precision p)
 {
    if (!c || (p != MDGPU_FP64 && p != MDGPU_MIXED)) return MDGPU_E_ARG;
    c->prec = p;
+   c->gen++;
    return MDGPU_OK;
 }
 
@@ -317,6 +323,7 @@ mdgpu_status mdgpu_set_stream(mdgpu_ctx *c, void *stream)
 {
    if (!c) return MDGPU_E_ARG;
    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+   c->gen++;
    return MDGPU_OK;
 }
 
@@ -377,6 +384,7 @@ static mdgpu_status set_system_impl(mdgpu_ctx *c, const mdgpu_system *s, bool ke
    c->chg.assign(s->chg, s->chg + nsites);
    c->potpar.assign(s->potpar, s->potpar + (size_t)s->max_id * s->max_id * NPOTP);
    c->have_system = true;
+   c->gen++;
    c->sys_dirty = true;
    c->rs_uploaded = false;
    if (!keep_constants) {
@@ -400,6 +408,7 @@ mdgpu_status mdgpu_set_control(mdgpu_ctx *c, const mdgpu_control *ctl)
    const bool eintra_changes = c->have_control && c->ctl.alpha != ctl->alpha;
    c->ctl = *ctl;
    c->have_control = true;
+   c->gen++;
    if (eintra_changes) {
       c->have_eintra = false;
       c->have_self = false;

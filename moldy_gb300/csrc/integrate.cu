@@ -292,11 +292,16 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
    }
 }
 
-__global__ void k_md_record(int step, const double *__restrict__ pe, const double *__restrict__ kpart, int nb,
-                            double dist_v, const DevOut *__restrict__ out, double *__restrict__ energies,
-                            int *__restrict__ err)
+// Energy record of the step; the record index is a device counter so that
+// a captured step replays unchanged.
+__global__ void k_md_record(int *__restrict__ counter, int cap, const double *__restrict__ pe,
+                            const double *__restrict__ kpart, int nb, double dist_v,
+                            const DevOut *__restrict__ out, double *__restrict__ energies, int *__restrict__ err)
 {
    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+   const int step = *counter;
+   *counter = step + 1;
+   if (step >= cap) return;
    double kt = 0.0, kr = 0.0;
    for (int b = 0; b < nb; b++) {
       kt += kpart[2 * b];
@@ -406,6 +411,11 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    if (nq > 0 && (!quat || !amom)) return fail(c, MDGPU_E_ARG, "rotating species need quaternions and angular momenta");
    H.nmols_r = nq;
    H.dist = distant_const(c);
+   if (H.graph) {
+      cudaGraphExecDestroy(H.graph);
+      H.graph = nullptr;
+   }
+   c->gen++;
    MdDev &D = c->md;
    cudaStream_t st = c->stream;
    CK(D.cofm.ensure(3 * (size_t)c->nmols));
@@ -421,6 +431,7 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    CK(D.spec.ensure(nsp));
    CK(D.kpart.ensure(2 * (size_t)((c->nmols + 255) / 256)));
    CK(D.err.ensure(1));
+   CK(D.counter.ensure(1));
    CK(cudaMemcpyAsync(D.cofm.p, c_of_m, 3 * (size_t)c->nmols * sizeof(double), cudaMemcpyHostToDevice, st));
    CK(cudaMemcpyAsync(D.mom.p, mom, 3 * (size_t)c->nmols * sizeof(double), cudaMemcpyHostToDevice, st));
    if (nq) {
@@ -440,38 +451,96 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    return MDGPU_OK;
 }
 
+// Enqueues one step on the context's stream.
+static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap, double dist_v)
+{
+   const MdHost &H = c->mdh;
+   MdDev &D = c->md;
+   cudaStream_t st = c->stream;
+   const int N = c->nsites, M = c->nmols, nbm = (M + 255) / 256;
+   k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
+                                                D.amom.p, D.err.p);
+   k_md_sites<<<(N + 255) / 256, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.cofm.p,
+                                               D.quat.p, c->site.p);
+   CK(cudaGetLastError());
+   c->launches += 2;
+   mdgpu_status s = mdgpu_forces_device(c, H.h, c->site.p, D.cofm.p, c->force.p, c->small.p, c->small.p + 2);
+   if (s) return s;
+   k_md_kick<<<nbm, 256, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.mol_site0.p, D.pf.p, c->force.p,
+                                  D.quat.p, D.mom.p, D.amom.p, D.kpart.p);
+   k_md_record<<<1, 32, 0, st>>>(D.counter.p, cap, c->small.p, D.kpart.p, nbm, dist_v, c->out.p, D.energies.p,
+                                 D.err.p);
+   k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
+                                                D.amom.p, D.err.p);
+   CK(cudaGetLastError());
+   c->launches += 3;
+   return MDGPU_OK;
+}
+
+// Captures one step as a CUDA graph (after a step has run, so every buffer
+// is allocated and every table uploaded: nothing in the step allocates or
+// synchronises any more).
+static mdgpu_status md_capture(mdgpu_ctx *c, const MdStepParams &P, int cap, double dist_v)
+{
+   MdHost &H = c->mdh;
+   cudaStream_t st = c->stream;
+   if (H.graph) {
+      cudaGraphExecDestroy(H.graph);
+      H.graph = nullptr;
+   }
+   const int64_t l0 = c->launches;
+   CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+   mdgpu_status s = md_enqueue_step(c, P, cap, dist_v);
+   cudaGraph_t g = nullptr;
+   const cudaError_t e = cudaStreamEndCapture(st, &g);
+   if (s) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+   }
+   CK(e);
+   const cudaError_t ei = cudaGraphInstantiate(&H.graph, g, 0);
+   cudaGraphDestroy(g);
+   CK(ei);
+   H.graph_launches = c->launches - l0;
+   c->launches = l0;
+   H.graph_gen = c->gen;
+   return MDGPU_OK;
+}
+
 extern "C" mdgpu_status mdgpu_md_run(mdgpu_ctx *c, int nsteps, double *energies)
 {
    if (!c || nsteps < 0) return fail(c, MDGPU_E_ARG, "invalid argument");
    if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
-   const MdHost &H = c->mdh;
+   MdHost &H = c->mdh;
    MdDev &D = c->md;
    cudaStream_t st = c->stream;
    mdgpu_status s = ensure_ready(c, H.h, true, true);
    if (s) return s;
    MdStepParams P;
    step_params(c, P);
-   const int N = c->nsites, M = c->nmols;
-   const int nbm = (M + 255) / 256;
-   CK(D.energies.ensure(4 * (size_t)(nsteps > 0 ? nsteps : 1)));
+   const int cap = nsteps > 0 ? nsteps : 1;
+   if (D.energies.n < 4 * (size_t)cap) {
+      // a larger record buffer moves the pointer a captured step holds
+      CK(D.energies.ensure(4 * (size_t)cap));
+      H.graph_gen = 0;
+   }
    CK(c->small.ensure(16));
+   CK(cudaMemsetAsync(D.counter.p, 0, sizeof(int), st));
    const double dist_v = H.dist / det3(H.h);
    for (int i = 0; i < nsteps; i++) {
-      k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
-                                                   D.amom.p, D.err.p);
-      k_md_sites<<<(N + 255) / 256, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.cofm.p,
-                                                  D.quat.p, c->site.p);
-      CK(cudaGetLastError());
-      c->launches += 2;
-      s = mdgpu_forces_device(c, H.h, c->site.p, D.cofm.p, c->force.p, c->small.p, c->small.p + 2);
-      if (s) return s;
-      k_md_kick<<<nbm, 256, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.mol_site0.p, D.pf.p, c->force.p,
-                                     D.quat.p, D.mom.p, D.amom.p, D.kpart.p);
-      k_md_record<<<1, 32, 0, st>>>(i, c->small.p, D.kpart.p, nbm, dist_v, c->out.p, D.energies.p, D.err.p);
-      k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
-                                                   D.amom.p, D.err.p);
-      CK(cudaGetLastError());
-      c->launches += 3;
+      // the first step runs directly; later ones replay a captured step
+      // unless the configuration changed since it was captured
+      const bool replay = i > 0 && !c->timing;
+      if (replay && (!H.graph || H.graph_gen != c->gen || H.graph_cap != cap)) {
+         if ((s = md_capture(c, P, cap, dist_v)) != MDGPU_OK) return s;
+         H.graph_cap = cap;
+      }
+      if (replay) {
+         CK(cudaGraphLaunch(H.graph, st));
+         c->launches += H.graph_launches;
+      } else if ((s = md_enqueue_step(c, P, cap, dist_v)) != MDGPU_OK) {
+         return s;
+      }
    }
    int err = 0;
    if (energies && nsteps > 0)

@@ -177,10 +177,16 @@ struct MdHost {
    double half = 0;                  // dt / 2
    double dist = 0;                  // distant-potential constant (energy x volume)
    int nosym = 0, saxis = 0, nmols_r = 0;
+   // one captured step (CUDA graph), replayed by mdgpu_md_run
+   cudaGraphExec_t graph = nullptr;
+   uint64_t graph_gen = 0;
+   int64_t graph_launches = 0;       // kernels one replay launches
+   int graph_cap = 0;                // record capacity it was captured with
 };
 
 struct MdDev {
    DBuf<double> cofm, mom, quat, amom;   // [nmols][3], [nmols][3], [nmols_r][4] x2
+   DBuf<int> counter;                    // index of the next energy record
    DBuf<int> mol_spec, mol_q, mol_site0, site_mol, site_pf;
    DBuf<double> pf;                      // principal-frame sites of every species
    DBuf<MdSpec> spec;
@@ -237,6 +243,9 @@ struct mdgpu_ctx {
    cudaEvent_t ev[MDGPU_NPHASES + 1] = {};
    bool ev_marked[MDGPU_NPHASES + 1] = {};
    bool have_nabor_note = false;
+   // bumped by every call that changes what a captured step would launch
+   // (system, control, parameters, precision, stream, dynamics state)
+   uint64_t gen = 1;
    int note_nx = 0, note_ny = 0, note_nz = 0, note_nabors = 0;
 };
 

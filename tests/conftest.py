@@ -16,7 +16,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
 def golden_files(prefix=""):
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith(prefix))
+    """Force-path fixtures (the md_* dynamics fixtures are named explicitly
+    by their own tests)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and f.startswith(prefix) and not f.startswith("md_"))
 
 
 @pytest.fixture(scope="session")
