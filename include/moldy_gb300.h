@@ -164,6 +164,18 @@ mdgpu_status mdgpu_pair_keys(mdgpu_ctx *ctx, const double *h, const double *site
                              const double *c_of_m, uint64_t *keys, int64_t cap,
                              int64_t *count);
 
+/* Radial-distribution histogram of one configuration, as force_calc
+ * accumulates it on RDF steps (rdf_inner/rdf_accum, src/force.c:1010-1103,
+ * src/rdf.c:94-107): every site pair the strict neighbour-cell list at
+ * `limit` reaches (on the cell grid of the force cutoff and subcell), bin =
+ * (int)(nbins/limit * r), kept when below nbins; pairs within a molecule
+ * included.  counts ([max_id][max_id][nbins], symmetric) receives the number
+ * of unordered pairs of each identifier pair per bin, exact.  The
+ * reference-signature force_calc adds these counts into the caller's own
+ * RDF array on RDF steps. */
+mdgpu_status mdgpu_rdf_counts(mdgpu_ctx *ctx, const double *h, const double *site_soa,
+                              const double *c_of_m, double limit, int nbins, uint64_t *counts);
+
 /* Reciprocal-space Ewald sum that allocates nothing.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc: code running under
  * CUDA stream capture (allocation cannot be captured into a graph), hosts

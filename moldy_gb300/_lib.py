@@ -24,6 +24,7 @@ EXPORTS = ["mdgpu_create", "mdgpu_destroy", "mdgpu_last_error", "mdgpu_set_preci
            "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak",
            "mdgpu_ewald_kspace_noalloc", "mdgpu_set_params", "mdgpu_energy_grad",
            "mdgpu_fm_loss_grad", "mdgpu_md_init", "mdgpu_md_run", "mdgpu_md_get_state",
+           "mdgpu_rdf_counts",
            "force_calc", "ewald", "poteval"]
 
 
@@ -115,6 +116,7 @@ def load():
         "mdgpu_md_init": ([vp, C.POINTER(Dynamics), dp, dp, dp, dp, dp], ip),
         "mdgpu_md_run": ([vp, ip, dp], ip),
         "mdgpu_md_get_state": ([vp, dp, dp, dp, dp], ip),
+        "mdgpu_rdf_counts": ([vp, dp, dp, dp, C.c_double, ip, C.POINTER(C.c_uint64)], ip),
         "mdgpu_energy_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.POINTER(Grad)], ip),
         "mdgpu_fm_loss_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.c_double, dp, C.POINTER(Grad)], ip),
     }

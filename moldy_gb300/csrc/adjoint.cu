@@ -434,6 +434,7 @@ static mdgpu_status ks_adjoint(mdgpu_ctx *c, bool loss)
 // Checks the adjoint's limits for the current system and control record.
 static mdgpu_status adjoint_supported(mdgpu_ctx *c)
 {
+   if (c->fw_mol >= 0) return fail(c, MDGPU_E_UNSUPPORTED, "adjoint: framework molecules are not supported");
    if (c->max_id > MDGPU_ADJ_MAX_ID)
       return fail(c, MDGPU_E_UNSUPPORTED, "adjoint: more than MDGPU_ADJ_MAX_ID site identifiers");
    if (pot_nparams(c->ptype) == 0)

@@ -127,9 +127,6 @@ mdgpu_status mdgpu::ensure_ready(mdgpu_ctx *c, const double *h, bool need_rs, bo
    if (!c->have_control) return fail(c, MDGPU_E_ARG, "mdgpu_set_control has not been called");
    mdgpu_status s = check_h(c, h);
    if (s) return s;
-   for (const auto &sp : c->spec)
-      if (sp.framework)
-         return fail(c, MDGPU_E_UNSUPPORTED, "framework species are not supported by the GPU path");
    if (c->ptype < 0 || c->ptype > 6 || c->ptype == 5)
       return fail(c, MDGPU_E_PTYPE, "KERNEL called with unknown potential type " + std::to_string(c->ptype));
    double rkey[12];
@@ -381,6 +378,30 @@ static mdgpu_status set_system_impl(mdgpu_ctx *c, const mdgpu_system *s, bool ke
       sp.p_f_sites = nullptr;
       so += sp.nsites;
    }
+   // frameworks: after every other species, one framework molecule at most
+   c->fw_mol = -1;
+   c->fw_site0 = nsites;
+   c->nmols_nf = nmols;
+   {
+      int isite2 = 0, imol2 = 0, nfw = 0;
+      bool seen_fw = false;
+      for (const auto &sp : c->spec) {
+         if (sp.framework) {
+            if (!seen_fw) {
+               c->fw_mol = imol2;
+               c->fw_site0 = isite2;
+               c->nmols_nf = imol2;
+            }
+            seen_fw = true;
+            nfw += sp.nmols;
+         } else if (seen_fw) {
+            return fail(c, MDGPU_E_UNSUPPORTED, "framework species must come after all other species");
+         }
+         isite2 += sp.nsites * sp.nmols;
+         imol2 += sp.nmols;
+      }
+      if (nfw > 1) return fail(c, MDGPU_E_UNSUPPORTED, "Multiple framework molecules are not supported");
+   }
    c->chg.assign(s->chg, s->chg + nsites);
    c->potpar.assign(s->potpar, s->potpar + (size_t)s->max_id * s->max_id * NPOTP);
    c->have_system = true;
@@ -542,6 +563,46 @@ mdgpu_status mdgpu_ewald(mdgpu_ctx *c, const double *h, double *const site[3],
    return MDGPU_OK;
 }
 
+// Unordered per-type-pair counts from the full-list counts of rs_rdf.
+static void rdf_unordered(const std::vector<unsigned long long> &full, int M, int nbins, uint64_t *out)
+{
+   for (int a = 0; a < M; a++)
+      for (int b = 0; b < M; b++)
+         for (int k = 0; k < nbins; k++) {
+            const size_t ab = ((size_t)a * M + b) * nbins + k, ba = ((size_t)b * M + a) * nbins + k;
+            out[ab] = a == b ? full[ab] / 2 : (full[ab] + full[ba]) / 2;
+         }
+}
+
+static mdgpu_status rdf_download(mdgpu_ctx *c, int nbins, std::vector<unsigned long long> &full)
+{
+   full.resize((size_t)c->max_id * c->max_id * nbins);
+   CKR(cudaMemcpyAsync(full.data(), c->rd.rdf_counts.p, full.size() * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, c->stream));
+   return sync_out(c);
+}
+
+mdgpu_status mdgpu_rdf_counts(mdgpu_ctx *c, const double *h, const double *site_soa, const double *c_of_m,
+                              double limit, int nbins, uint64_t *counts)
+{
+   if (!c || !site_soa || !counts) return fail(c, MDGPU_E_ARG, "NULL argument");
+   mdgpu_status s = ensure_ready(c, h, true, false);
+   if (s) return s;
+   const size_t N = c->nsites;
+   CKR(cudaMemcpyAsync(c->site.p, site_soa, 3 * N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+   if (c->ctl.molpbc) {
+      if (!c_of_m) return fail(c, MDGPU_E_ARG, "molecular cutoff needs the centres of mass");
+      CKR(cudaMemcpyAsync(c->cofm_in.p, c_of_m, 3 * c->nmols * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+   }
+   CKR(cudaMemsetAsync(c->out.p, 0, sizeof(DevOut), c->stream));
+   if ((s = rs_launch(c, c->site.p, c->cofm_in.p, c->force.p, true, nullptr, 0, nullptr)) != MDGPU_OK) return s;
+   if ((s = rs_rdf(c, limit, nbins)) != MDGPU_OK) return s;
+   std::vector<unsigned long long> full;
+   if ((s = rdf_download(c, nbins, full)) != MDGPU_OK) return s;
+   rdf_unordered(full, c->max_id, nbins, counts);
+   return MDGPU_OK;
+}
+
 mdgpu_status mdgpu_synchronize(mdgpu_ctx *c)
 {
    if (!c) return MDGPU_E_ARG;
@@ -618,6 +679,7 @@ double mdgpu_poteval(const double *potpar, double r, int ptype, double chgsq, do
 extern contr_mt control __attribute__((weak));
 extern int nthreads __attribute__((weak));
 void note(char *, ...) __attribute__((weak));
+void *rdf_ptr(int *size) __attribute__((weak));   // src/rdf.c:58-62
 void message(int *, ...) __attribute__((weak));
 
 }  // extern "C"
@@ -650,6 +712,20 @@ void ref_note(const char *fmt, ...)
    va_end(ap);
    if (&control != nullptr && &note != nullptr)
       note((char *)"%s", buf);
+   else
+      std::printf(" *I* %s\n", buf);
+}
+
+// message(..., INFO, ...) of the reference (src/output.c:131-168)
+void ref_info(const char *fmt, ...)
+{
+   char buf[512];
+   va_list ap;
+   va_start(ap, fmt);
+   std::vsnprintf(buf, sizeof buf, fmt, ap);
+   va_end(ap);
+   if (&control != nullptr && &message != nullptr)
+      message(nullptr, nullptr, 0, (char *)"%s", buf);
    else
       std::printf(" *I* %s\n", buf);
 }
@@ -748,6 +824,38 @@ void ref_check(mdgpu_ctx *c, mdgpu_status s)
 
 extern "C" {
 
+// Adds this configuration's pair counts into the caller's RDF histogram the
+// way rdf_accum does (src/rdf.c:94-107): each counted pair adds 1/density to
+// a float bin, evaluated as (float)((double)bin + 1/density).  Every addend
+// of a bin is the same, so repeating the addition count times gives the
+// reference's value whatever order its pairs came in.
+static void ref_rdf_accumulate(mdgpu_ctx *c, system_mt *system)
+{
+   const int nbins = control.nbins, M = c->max_id;
+   mdgpu_status s = rs_rdf(c, control.limit, nbins);
+   std::vector<unsigned long long> full;
+   if (s == MDGPU_OK) s = rdf_download(c, nbins, full);
+   ref_check(c, s);
+   std::vector<uint64_t> cnt(full.size());
+   rdf_unordered(full, M, nbins, cnt.data());
+   int size = 0;
+   float *base = (float *)rdf_ptr(&size);
+   const double hm[9] = {system->h[0][0], system->h[0][1], system->h[0][2], system->h[1][0], system->h[1][1],
+                         system->h[1][2], system->h[2][0], system->h[2][1], system->h[2][2]};
+   const double density = system->nsites / det3(hm);
+   const double invrho = 1.0 / density;
+   float *bin = base;
+   for (int a = 1; a < M; a++)          // init_rdf's layout, src/rdf.c:71-91
+      for (int b = a; b < M; b++, bin += nbins) {
+         if (bin + nbins > base + size) ref_fatal("moldy_gb300: RDF array smaller than expected");
+         for (int k = 0; k < nbins; k++) {
+            float v = bin[k];
+            for (uint64_t n = cnt[((size_t)a * M + b) * nbins + k]; n > 0; n--) v = (float)((double)v + invrho);
+            bin[k] = v;
+         }
+      }
+}
+
 void force_calc(real **site, real **site_force, system_mt *system, spec_mt *species, real *chg,
                 pot_mt *potpar, double *pe, mat_mt stress)
 {
@@ -755,11 +863,12 @@ void force_calc(real **site, real **site_force, system_mt *system, spec_mt *spec
    double h[9];
    ref_sync(c, system, species, chg, potpar, h);
    // force_calc also accumulates the radial distribution function on RDF
-   // steps (src/force.c:1302-1313); that part is not on the GPU path
-   if (control.rdf_interval > 0 && control.istep >= control.begin_rdf &&
-       control.istep % control.rdf_interval == 0)
-      ref_fatal("moldy_gb300: RDF accumulation is not available on the GPU force path "
-                "(set rdf-interval=0)");
+   // steps (src/force.c:1302-1313): the histogram is taken on the GPU over
+   // the cells this call binned and added into the caller's rdf array
+   const bool rdf_step = control.rdf_interval > 0 && control.istep >= control.begin_rdf &&
+                         control.istep % control.rdf_interval == 0;
+   if (rdf_step && !rdf_ptr)
+      ref_fatal("moldy_gb300: RDF accumulation needs the caller's rdf.c (rdf_ptr)");
    double st[9];
    for (int i = 0; i < 9; i++) st[i] = stress[i / 3][i % 3];
    mdgpu_status s = mdgpu_force_calc(c, h, site, site_force, &system->c_of_m[0][0], pe, st);
@@ -785,6 +894,7 @@ void force_calc(real **site, real **site_force, system_mt *system, spec_mt *spec
       ref_warn("%lld further site pairs closer than %fA.",
                (long long)(c->info.n_too_close - MAX_TOO_CLOSE_REC), std::sqrt(TOO_CLOSE));
    for (int i = 0; i < 9; i++) stress[i / 3][i % 3] = st[i];
+   if (rdf_step) ref_rdf_accumulate(c, system);
 }
 
 void ewald(real **site, real **site_force, system_mp system, spec_mt *species, real *chg, double *pe,
@@ -802,6 +912,13 @@ void ewald(real **site, real **site_force, system_mp system, spec_mt *species, r
          for (double v : c->chg) t += v;
          return t;
       }();
+      if (c->fw_mol >= 0) {   // charged framework (src/ewald.c:405-413)
+         double q_fw = 0;
+         for (size_t i = (size_t)c->fw_site0; i < c->chg.size(); i++) q_fw += c->chg[i];
+         const double corr = 3.14159265358979323846 * q_fw * q_fw / (2.0 * c->ctl.alpha * c->ctl.alpha);
+         ref_info("Framework has net electric charge of %.2g - correction of %g kJmol(-1) added to self energy",
+                  q_fw * CONV_Q, corr / c->kl.vol * CONV_E);
+      }
       if (std::fabs(q_net) * CONV_Q > 1.0e-5) {
          const double corr = 3.14159265358979323846 * q_net * q_net / (2.0 * c->ctl.alpha * c->ctl.alpha);
          ref_warn("System has net electric charge of %.2g - correction of %g kJmol(-1) added to self energy",

@@ -183,6 +183,27 @@ mdgpu_status build_rs_geom(const double *h, const mdgpu_control &ctl, RsGeom &g)
    return MDGPU_OK;
 }
 
+// Strict stencil for the radial distribution function (src/force.c:1307-1308:
+// strict_neighbour_list at the RDF limit on the force call's cell grid),
+// with each half-space offset followed by its mirror.
+mdgpu_status build_rdf_stencil(const double *h, double limit, int nx, int ny, int nz, std::vector<int4> &full)
+{
+   std::vector<int> half;
+   mdgpu_status s = build_stencil(h, limit, nx, ny, nz, true, half);
+   if (s != MDGPU_OK) return s;
+   full.clear();
+   for (size_t e = 0; e < half.size() / 3; e++) {
+      const int dx = half[3 * e], dy = half[3 * e + 1], dz = half[3 * e + 2];
+      if (dx == 0 && dy == 0 && dz == 0) {
+         full.push_back(make_int4(0, 0, 0, 1));
+      } else {
+         full.push_back(make_int4(dx, dy, dz, 0));
+         full.push_back(make_int4(-dx, -dy, -dz, 0));
+      }
+   }
+   return MDGPU_OK;
+}
+
 // k-vectors in the half sphere |k| < k_c, in the order ewald() builds them
 // (src/ewald.c:441-461), grouped into items of up to KI consecutive l values
 // of one (h,k) column; plus the per-k prefactors (src/ewald.c:510-511).

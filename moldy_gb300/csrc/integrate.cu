@@ -349,6 +349,7 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    if (!c->have_system || !c->have_control)
       return fail(c, MDGPU_E_ARG, "mdgpu_set_system and mdgpu_set_control come first");
    if (!(dyn->step > 0.0)) return fail(c, MDGPU_E_ARG, "the timestep must be positive");
+   if (c->fw_mol >= 0) return fail(c, MDGPU_E_UNSUPPORTED, "dynamics with a framework molecule are not supported");
    mdgpu_status s = ensure_ready(c, h, true, true);
    if (s) return s;
    MdHost &H = c->mdh;

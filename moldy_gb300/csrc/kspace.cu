@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(FT_THREADS)
 k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
           const float2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
           const float4 *__restrict__ kd, const int4 *__restrict__ ph, const float2 *__restrict__ zz,
-          const double *__restrict__ chg, const int *__restrict__ sorted, int N,
+          const double *__restrict__ chg, const int *__restrict__ sorted, int N, int obase,
           double *__restrict__ fpart)
 {
    __shared__ int4 s_it[FT_ITEMS];
@@ -400,20 +400,22 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    kahan_add(fxb, exb, pxb);
    kahan_add(fyb, eyb, pyb);
    kahan_add(fzb, ezb, pzb);
+   // site oi's partial goes to row oi - obase of [3][N] (obase = 0 except
+   // for a subset of sites held compactly)
    double *dst = fpart + (size_t)blockIdx.y * 3 * N;
    if (live0) {
       const int oi = sorted[i0];   // slot i0 holds site oi
       const double q = chg[oi];
-      dst[oi] = q * ((double)fxa - (double)exa);
-      dst[N + oi] = q * ((double)fya - (double)eya);
-      dst[2 * N + oi] = q * ((double)fza - (double)eza);
+      dst[oi - obase] = q * ((double)fxa - (double)exa);
+      dst[N + oi - obase] = q * ((double)fya - (double)eya);
+      dst[2 * N + oi - obase] = q * ((double)fza - (double)eza);
    }
    if (live1) {
       const int oi = sorted[i1];
       const double q = chg[oi];
-      dst[oi] = q * ((double)fxb - (double)exb);
-      dst[N + oi] = q * ((double)fyb - (double)eyb);
-      dst[2 * N + oi] = q * ((double)fzb - (double)ezb);
+      dst[oi - obase] = q * ((double)fxb - (double)exb);
+      dst[N + oi - obase] = q * ((double)fyb - (double)eyb);
+      dst[2 * N + oi - obase] = q * ((double)fzb - (double)ezb);
    }
 }
 
@@ -422,7 +424,7 @@ k_force64(const int4 *__restrict__ item, const int *__restrict__ item_k0,
           const double2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
           const double4 *__restrict__ kd, const ulonglong2 *__restrict__ pha,
           const ulonglong2 *__restrict__ phb, const double2 *__restrict__ zz,
-          const double *__restrict__ chg, const int *__restrict__ sorted, int N,
+          const double *__restrict__ chg, const int *__restrict__ sorted, int N, int obase,
           double *__restrict__ fpart)
 {
    __shared__ int4 s_it[FT_ITEMS];
@@ -476,10 +478,128 @@ k_force64(const int4 *__restrict__ item, const int *__restrict__ item_k0,
       const int oi = sorted[i];   // slot i holds site oi
       const double q = chg[oi];
       double *dst = fpart + (size_t)blockIdx.y * 3 * N;
-      dst[oi] = q * Fx;
-      dst[N + oi] = q * Fy;
-      dst[2 * N + oi] = q * Fz;
+      dst[oi - obase] = q * Fx;
+      dst[N + oi - obase] = q * Fy;
+      dst[2 * N + oi - obase] = q * Fz;
    }
+}
+
+// ----------------------------------------------------------- frameworks
+// With a framework molecule, ewald() leaves out framework-framework terms
+// (src/ewald.c:528-579): the energy is 1/2 coeff (Cn (Cn + 2 Cf) + Sn (Sn +
+// 2 Sf)) from the non-framework (n) and framework (f) structure factors;
+// non-framework sites feel the whole S(k), framework sites only Sn.  The
+// charges are split into the two channels in the per-slot records (the
+// framework sites are the last ones, site index >= fw0), each channel gets
+// its own structure-factor pass, and the framework sites' forces are
+// corrected by a force pass over them alone with the framework
+// coefficients negated.
+__global__ void k_fw_split(int N, int fw0, const int *__restrict__ sorted, int mixed, int4 *__restrict__ ph32,
+                           int4 *__restrict__ phf32, ulonglong2 *__restrict__ ph64b,
+                           ulonglong2 *__restrict__ phf64b, int *__restrict__ fslot)
+{
+   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   if (p >= N) return;
+   const int s = sorted[p];
+   const bool f = s >= fw0;
+   if (f) fslot[s - fw0] = p;
+   if (mixed) {
+      int4 v = ph32[p], w = v;
+      if (f) v.w = __float_as_int(0.f); else w.w = __float_as_int(0.f);
+      ph32[p] = v;
+      phf32[p] = w;
+   } else {
+      ulonglong2 v = ph64b[p], w = v;
+      if (f) v.y = (unsigned long long)__double_as_longlong(0.0); else w.y = (unsigned long long)__double_as_longlong(0.0);
+      ph64b[p] = v;
+      phf64b[p] = w;
+   }
+}
+
+// The framework sites' per-slot records, compacted (site fw0 + i at row i).
+__global__ void k_fw_gather(int nf, int fw0, const int *__restrict__ fslot, int mixed, const int4 *__restrict__ ph32,
+                            const float2 *__restrict__ zp32, const ulonglong2 *__restrict__ ph64a,
+                            const ulonglong2 *__restrict__ ph64b, const double2 *__restrict__ z64,
+                            int4 *__restrict__ phc, float2 *__restrict__ zpc, ulonglong2 *__restrict__ pac,
+                            ulonglong2 *__restrict__ pbc, double2 *__restrict__ zc, int *__restrict__ sortedc)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= nf) return;
+   const int p = fslot[i];
+   sortedc[i] = fw0 + i;
+   if (mixed) {
+      phc[i] = ph32[p];
+      for (int t = 0; t < KI; t++) zpc[(size_t)i * KI + t] = zp32[(size_t)p * KI + t];
+   } else {
+      pac[i] = ph64a[p];
+      pbc[i] = ph64b[p];
+      zc[i] = z64[p];
+   }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256)
+k_kreduce_fw(int nk, int nchunks, const float2 *__restrict__ pn32, const float2 *__restrict__ pf32,
+             const double2 *__restrict__ pn64, const double2 *__restrict__ pf64,
+             const double *__restrict__ kvec, const double *__restrict__ coeff,
+             const double *__restrict__ coeff2, float4 *__restrict__ kd32, float4 *__restrict__ kdf32,
+             double4 *__restrict__ kd64, double4 *__restrict__ kdf64, double *__restrict__ blk)
+{
+   __shared__ double red[32];
+   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+   double pek = 0, st[6] = {0, 0, 0, 0, 0, 0};
+   if (k < nk) {
+      double Cn = 0.0, Sn = 0.0, Cf = 0.0, Sf = 0.0;
+      for (int c = 0; c < nchunks; c++) {
+         const size_t o = (size_t)c * nk + k;
+         if (MIXED) {
+            Cn += (double)pn32[o].x;
+            Sn += (double)pn32[o].y;
+            Cf += (double)pf32[o].x;
+            Sf += (double)pf32[o].y;
+         } else {
+            Cn += pn64[o].x;
+            Sn += pn64[o].y;
+            Cf += pf64[o].x;
+            Sf += pf64[o].y;
+         }
+      }
+      const double kx = kvec[k], ky = kvec[nk + k], kz = kvec[2 * nk + k];
+      const double cf = coeff[k], cf2 = coeff2[k];
+      pek = 0.5 * cf * (Cn * (Cn + Cf + Cf) + Sn * (Sn + Sf + Sf));
+      st[0] = pek - pek * cf2 * kx * kx;
+      st[1] = -(pek * cf2 * kx * ky);
+      st[2] = -(pek * cf2 * kx * kz);
+      st[3] = pek - pek * cf2 * ky * ky;
+      st[4] = -(pek * cf2 * ky * kz);
+      st[5] = pek - pek * cf2 * kz * kz;
+      const double A = cf * (Cn + Cf), B = cf * (Sn + Sf);
+      if (MIXED) {
+         kd32[k] = make_float4((float)A, (float)B, (float)kz, 0.f);
+         kdf32[k] = make_float4((float)(-cf * Cf), (float)(-cf * Sf), (float)kz, 0.f);
+      } else {
+         kd64[k] = make_double4(A, B, kz, 0.0);
+         kdf64[k] = make_double4(-cf * Cf, -cf * Sf, kz, 0.0);
+      }
+   }
+   double s = bsum(pek, red);
+   if (threadIdx.x == 0) blk[blockIdx.x * 8] = s;
+   for (int i = 0; i < 6; i++) {
+      s = bsum(st[i], red);
+      if (threadIdx.x == 0) blk[blockIdx.x * 8 + 1 + i] = s;
+   }
+}
+
+// force[comp][fw0 + i] += sum over splits of fpart[split][comp][i], i < nf
+__global__ void k_fsum_fw(int nf, int N, int fw0, int nsplit, const double *__restrict__ fpart,
+                          double *__restrict__ force)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= 3 * nf) return;
+   double s = 0.0;
+   for (int k = 0; k < nsplit; k++) s += fpart[(size_t)k * 3 * nf + i];
+   const int comp = i / nf, r = i - comp * nf;
+   force[(size_t)comp * N + fw0 + r] += s;
 }
 
 __global__ void k_fsum(int n3, int nsplit, const double *__restrict__ fpart, double *__restrict__ force,
@@ -586,27 +706,58 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
                                            d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
    CK(cudaGetLastError());
    KsShape sh = mixed ? ks_shape(N, ni, 1, 2) : ks_shape(N, ni, 1, 1);
+   const int fw0 = c->fw_site0, nf = N - fw0;   // framework sites, if any
+   if (nf > 0) {
+      CK(d.fslot.ensure(nf));
+      if (mixed) CK(d.phf32.ensure(N)); else CK(d.phf64b.ensure(N));
+      k_fw_split<<<(N + 255) / 256, 256, 0, st>>>(N, fw0, c->rd.sorted.p, mixed ? 1 : 0, d.ph32.p, d.phf32.p,
+                                                  d.ph64b.p, d.phf64b.p, d.fslot.p);
+      c->launches += 1;
+   }
    phase_mark(c, MDGPU_PH_SFAC);
+   const dim3 gs((ni + 127) / 128, sh.chunks);
    if (mixed) {
       CK(d.part32.ensure((size_t)sh.chunks * nk));
-      dim3 g((ni + 127) / 128, sh.chunks);
-      k_sfac32<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, N, sh.chunk, nk, d.part32.p);
+      k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, N, sh.chunk, nk, d.part32.p);
+      if (nf > 0) {
+         CK(d.partf32.ensure((size_t)sh.chunks * nk));
+         k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.phf32.p, d.zp32.p, N, sh.chunk, nk,
+                                      d.partf32.p);
+      }
    } else {
       CK(d.part64.ensure((size_t)sh.chunks * nk));
-      dim3 g((ni + 127) / 128, sh.chunks);
-      k_sfac64<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, d.ph64b.p, d.z64.p, N, sh.chunk,
-                                  nk, d.part64.p);
+      k_sfac64<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, d.ph64b.p, d.z64.p, N, sh.chunk,
+                                   nk, d.part64.p);
+      if (nf > 0) {
+         CK(d.partf64.ensure((size_t)sh.chunks * nk));
+         k_sfac64<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, d.phf64b.p, d.z64.p, N, sh.chunk,
+                                      nk, d.partf64.p);
+      }
    }
    CK(cudaGetLastError());
    const int nbk = (nk + 255) / 256;
    CK(d.blk.ensure((size_t)nbk * 8));
    phase_mark(c, MDGPU_PH_KREDUCE);
-   if (mixed)
+   if (nf > 0) {
+      if (mixed) {
+         CK(d.kdatf32.ensure(nk));
+         k_kreduce_fw<true><<<nbk, 256, 0, st>>>(nk, sh.chunks, d.part32.p, d.partf32.p, nullptr, nullptr,
+                                                 d.kz64.p, d.coeff.p, d.coeff2.p, d.kdat32.p, d.kdatf32.p,
+                                                 nullptr, nullptr, d.blk.p);
+      } else {
+         CK(d.kdatf64.ensure(nk));
+         k_kreduce_fw<false><<<nbk, 256, 0, st>>>(nk, sh.chunks, nullptr, nullptr, d.part64.p, d.partf64.p,
+                                                  d.kz64.p, d.coeff.p, d.coeff2.p, nullptr, nullptr, d.kdat64.p,
+                                                  d.kdatf64.p, d.blk.p);
+      }
+      c->launches += 2;
+   } else if (mixed) {
       k_kreduce<true><<<nbk, 256, 0, st>>>(nk, sh.chunks, d.part32.p, nullptr, d.kz64.p, d.coeff.p,
                                            d.coeff2.p, d.kdat32.p, nullptr, d.blk.p);
-   else
+   } else {
       k_kreduce<false><<<nbk, 256, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
                                             d.coeff2.p, nullptr, d.kdat64.p, d.blk.p);
+   }
    k_kfinal<<<1, 32, 0, st>>>(d.blk.p, nbk, out);
    CK(cudaGetLastError());
    CK(d.fpart.ensure((size_t)sh.splits * 3 * N));
@@ -614,16 +765,45 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    dim3 gf((N + 255) / 256, sh.splits);
    if (mixed)
       k_force32<<<gf, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
-                                    d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, c->rd.sorted.p, N,
-                                    d.fpart.p);
+                                           d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, c->rd.sorted.p, N, 0,
+                                           d.fpart.p);
    else
       k_force64<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, sh.per_split,
-                                    d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, c->rd.sorted.p, N,
+                                    d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, c->rd.sorted.p, N, 0,
                                     d.fpart.p);
    CK(cudaGetLastError());
    phase_mark(c, MDGPU_PH_FINAL);
    k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, sh.splits, d.fpart.p, d_force, accumulate ? 1 : 0);
    CK(cudaGetLastError());
+   if (nf > 0) {
+      // the framework sites' framework-framework k-space forces, taken off
+      const KsShape shf = ks_shape(nf, ni, 1, mixed ? 2 : 1);
+      CK(d.sortedc.ensure(nf));
+      CK(d.fpartf.ensure((size_t)shf.splits * 3 * nf));
+      if (mixed) {
+         CK(d.phc32.ensure(nf));
+         CK(d.zpc32.ensure((size_t)nf * KI));
+      } else {
+         CK(d.pac64.ensure(nf));
+         CK(d.pbc64.ensure(nf));
+         CK(d.zc64.ensure(nf));
+      }
+      k_fw_gather<<<(nf + 255) / 256, 256, 0, st>>>(nf, fw0, d.fslot.p, mixed ? 1 : 0, d.ph32.p, d.zp32.p,
+                                                    d.ph64a.p, d.ph64b.p, d.z64.p, d.phc32.p, d.zpc32.p,
+                                                    d.pac64.p, d.pbc64.p, d.zc64.p, d.sortedc.p);
+      const dim3 gff((nf + 255) / 256, shf.splits);
+      if (mixed)
+         k_force32<<<gff, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, shf.per_split,
+                                               d.kdatf32.p, d.phc32.p, d.zpc32.p, c->rd.chg.p, d.sortedc.p, nf,
+                                               fw0, d.fpartf.p);
+      else
+         k_force64<<<gff, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, shf.per_split,
+                                        d.kdatf64.p, d.pac64.p, d.pbc64.p, d.zc64.p, c->rd.chg.p, d.sortedc.p, nf,
+                                        fw0, d.fpartf.p);
+      k_fsum_fw<<<(3 * nf + 255) / 256, 256, 0, st>>>(nf, N, fw0, shf.splits, d.fpartf.p, d_force);
+      CK(cudaGetLastError());
+      c->launches += 3;
+   }
    c->launches += 6;
    return MDGPU_OK;
 }

@@ -38,6 +38,7 @@ struct RsGeom {
 // Builds the stencil and cell geometry; returns MDGPU_E_CUTOFF as the
 // reference's FATAL CUTOFF would fire.
 mdgpu_status build_rs_geom(const double *h, const mdgpu_control &ctl, RsGeom &g);
+mdgpu_status build_rdf_stencil(const double *h, double limit, int nx, int ny, int nz, std::vector<int4> &full);
 
 // ---- host-side k-vector list ---------------------------------------------
 struct KList {
@@ -119,6 +120,10 @@ struct RsDev {
    DBuf<float> pot32;
    DBuf<double> part;      // per-block partial energies/virials
    DBuf<unsigned long long> keys;
+   DBuf<int4> rdf_full;    // RDF stencil (strict, at the RDF limit)
+   DBuf<unsigned long long> rdf_counts;
+   double rdf_key[11] = {0};
+   int rdf_nfull = 0;
 };
 
 struct KsDev {
@@ -139,6 +144,16 @@ struct KsDev {
    DBuf<double2> part64;
    DBuf<double> fpart;     // [splits][3][N] force partials
    DBuf<double> blk;       // per-block energy/stress partials
+   // framework molecule: framework-charge channel, its structure factor,
+   // negated framework coefficients, its sites' records held compactly
+   DBuf<int> fslot, sortedc;
+   DBuf<int4> phf32, phc32;
+   DBuf<ulonglong2> phf64b, pac64, pbc64;
+   DBuf<float2> partf32, zpc32;
+   DBuf<double2> partf64, zc64;
+   DBuf<float4> kdatf32;
+   DBuf<double4> kdatf64;
+   DBuf<double> fpartf;
 };
 
 // Buffers of the adjoint (parameter-gradient) passes.
@@ -205,6 +220,10 @@ struct mdgpu_ctx {
    // system
    bool have_system = false, have_control = false;
    int nsites = 0, nmols = 0, max_id = 0, ptype = 0;
+   // the framework molecule (species flagged framework come last; the
+   // reference supports one framework molecule, src/force.c:1218-1220):
+   // its index, its first site and the count of molecules before it
+   int fw_mol = -1, fw_site0 = 0, nmols_nf = 0;
    std::vector<mdgpu_species> spec;
    std::vector<int> spec_ids;       // concatenated per-species site ids
    std::vector<double> spec_pf;     // concatenated principal-frame sites
@@ -262,6 +281,10 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
 // c->ad.res64/res32 when loss.
 mdgpu_status rs_adjoint(mdgpu_ctx *c, bool loss);
 int pot_nparams(int ptype);     // parameters the potential type reads
+// Site-pair distance histogram of the sites binned by the last rs_launch:
+// full-list counts [max_id][max_id][nbins] into c->rd.rdf_counts (zeroed
+// first); each unordered pair appears once from each side.
+mdgpu_status rs_rdf(mdgpu_ctx *c, double limit, int nbins);
 // kspace.cu
 mdgpu_status ks_prepare(mdgpu_ctx *c);
 mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate);

@@ -35,6 +35,10 @@ namespace mdgpu {
 
 struct RsParams {
    int nsites, nent, nx, ny, nz, ncells, nfull, max_id, molpbc, strict, ptype, pot_in_smem;
+   // the framework molecule (-1: none), its first site, and the number of
+   // molecule entities binned by centre of mass in molecular-cutoff mode
+   // (the framework's sites are binned one by one, src/force.c:458-470)
+   int fw_mol, fw_site0, nmol_ent;
    double hinv[9];
    double h[9];
    double reloc[27][3];
@@ -83,9 +87,11 @@ __global__ void k_bin(RsParams P, const double *__restrict__ site, const double 
    if (e >= P.nent) return;
    int bad = 0;
    double s0, s1, s2;
-   if (!P.molpbc) {
+   const bool by_site = !P.molpbc || e >= P.nmol_ent;
+   const int si = !P.molpbc ? e : P.fw_site0 + (e - P.nmol_ent);   // site of a site entity
+   if (by_site) {
       const int N = P.nsites;
-      double x = site[e], y = site[N + e], z = site[2 * N + e];
+      double x = site[si], y = site[N + si], z = site[2 * N + si];
       s0 = hrow(P.hinv, x, y, z);
       s1 = hrow(P.hinv + 3, x, y, z);
       s2 = hrow(P.hinv + 6, x, y, z);
@@ -99,8 +105,8 @@ __global__ void k_bin(RsParams P, const double *__restrict__ site, const double 
    int cz = cellbin_dev(s2, P.nz, (double)P.nz, &bad);
    int c = cz + P.nz * (cy + P.ny * cx);
    if (bad) atomicOr(&out->err, 1);
-   if (!P.molpbc) {
-      cell_of[e] = c;
+   if (by_site) {
+      cell_of[si] = c;
       atomicAdd(&cell_count[c], 1);
    } else {
       int f = mol_first[e], n = mol_n[e];
@@ -540,6 +546,7 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
       walk_stencil<MIXED>(P, p, c, lane, cell_start, full, off_hi, off_lo, rows, [&](int j, int k, int kimg) {
          R rx, ry, rz, r2, qj;
          const int2 tj = __ldg(&tag[j]);
+         if (ti.y == P.fw_mol && tj.y == P.fw_mol) return;   // no framework-framework pairs
          pair_sep<MIXED>(P, j, k, kimg, rows, xi32, xi64, pos64, pos32, rx, ry, rz, r2, qj);
          if (MODE == 1) {
             const long long a = oi, bb = sorted[j];
@@ -844,7 +851,7 @@ k_pairs_adj(RsParams P, AdjParams A, const int *__restrict__ cell_start,
          }
          walk_stencil<MIXED>(P, p, c, lane, cell_start, full, off_hi, off_lo, rows, [&](int j, int k, int kimg) {
             const int2 tj = __ldg(&tag[j]);
-            if (tj.x != b) return;
+            if (tj.x != b || (ti.y == P.fw_mol && tj.y == P.fw_mol)) return;
             R rx, ry, rz, r2, qj;
             pair_sep<MIXED>(P, j, k, kimg, rows, xi32, xi64, pos64, pos32, rx, ry, rz, r2, qj);
             bool too_close, clip;
@@ -914,6 +921,61 @@ __global__ void k_adj_slots(const double *__restrict__ gpart, int nblocks, int n
    slots[q] = s;
 }
 
+// --------------------------------------------------------------------- RDF
+// Site-pair distance histogram (rdf_inner + rdf_accum, src/force.c:1010-1103,
+// src/rdf.c:94-107): the same warp-per-site walk over the strict stencil at
+// the RDF limit, r^2 in FP64 with the reference's operation order from the
+// original co-ordinates, bin = (int)(rbin sqrt(r^2)) kept when < nbins.
+// Counts per (id_i, id_j, bin) in a shared-memory histogram per block when it
+// fits (HIST_SMEM), else directly in global memory.
+constexpr int HIST_SMEM = 8192;
+
+__global__ void __launch_bounds__(PAIR_WARPS * 32)
+k_rdf(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ slot_cell,
+      const int4 *__restrict__ full, const int2 *__restrict__ tag, const int *__restrict__ sorted,
+      const double *__restrict__ site, double rbin, int nbins, unsigned long long *__restrict__ counts)
+{
+   __shared__ unsigned int hist[HIST_SMEM];
+   __shared__ int s_inc[PAIR_WARPS][32], s_jb[PAIR_WARPS][32], s_info[PAIR_WARPS][32];
+   const int nh = P.max_id * P.max_id * nbins;
+   const bool in_smem = nh <= HIST_SMEM;
+   if (in_smem)
+      for (int q = threadIdx.x; q < nh; q += blockDim.x) hist[q] = 0u;
+   __syncthreads();
+   const int N = P.nsites;
+   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int p = blockIdx.x * PAIR_WARPS + w;
+   const WalkRows rows{s_inc[w], s_jb[w], s_info[w], nullptr, nullptr};
+   if (p < N) {
+      const int c = slot_cell[p];
+      const int oi = sorted[p];
+      const int2 ti = tag[p];
+      const int idi = ti.x;
+      const double xi = site[oi], yi = site[N + oi], zi = site[2 * N + oi];
+      walk_stencil<false>(P, p, c, lane, cell_start, full, nullptr, nullptr, rows, [&](int j, int, int kimg) {
+         if (ti.y == P.fw_mol && __ldg(&tag[j]).y == P.fw_mol) return;
+         const int oj = sorted[j];
+         const double *rl = P.reloc[kimg];
+         const double rx = __dadd_rn(__dsub_rn(site[oj], xi), rl[0]);
+         const double ry = __dadd_rn(__dsub_rn(site[N + oj], yi), rl[1]);
+         const double rz = __dadd_rn(__dsub_rn(site[2 * N + oj], zi), rl[2]);
+         const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+         const int bin = __double2int_rz(__dmul_rn(rbin, sqrt(r2)));
+         if (bin < nbins) {
+            const int q = (idi * P.max_id + __ldg(&tag[j]).x) * nbins + bin;
+            if (in_smem)
+               atomicAdd(&hist[q], 1u);
+            else
+               atomicAdd(&counts[q], 1ull);
+         }
+      });
+   }
+   __syncthreads();
+   if (in_smem)
+      for (int q = threadIdx.x; q < nh; q += blockDim.x)
+         if (hist[q]) atomicAdd(&counts[q], (unsigned long long)hist[q]);
+}
+
 // -------------------------------------------------------------- host side
 static RsParams make_params(mdgpu_ctx *c)
 {
@@ -921,7 +983,10 @@ static RsParams make_params(mdgpu_ctx *c)
    memset(&P, 0, sizeof P);
    const RsGeom &g = c->rs;
    P.nsites = c->nsites;
-   P.nent = c->ctl.molpbc ? c->nmols : c->nsites;
+   P.fw_mol = c->fw_mol;
+   P.fw_site0 = c->fw_site0;
+   P.nmol_ent = c->nmols_nf;
+   P.nent = c->ctl.molpbc ? c->nmols_nf + (c->nsites - c->fw_site0) : c->nsites;
    P.nx = g.nx; P.ny = g.ny; P.nz = g.nz; P.ncells = g.ncells;
    P.nfull = (int)g.full.size();
    P.max_id = c->max_id;
@@ -1093,6 +1158,42 @@ mdgpu_status rs_adjoint(mdgpu_ctx *c, bool loss)
    k_adj_slots<<<(A.nslot + 255) / 256, 256, 0, st>>>(a.gpart.p, nblk, A.nslot, a.slots.p);
    CK(cudaGetLastError());
    c->launches += 2;
+   return MDGPU_OK;
+}
+
+mdgpu_status rs_rdf(mdgpu_ctx *c, double limit, int nbins)
+{
+   RsDev &d = c->rd;
+   const RsGeom &g = c->rs;
+   cudaStream_t st = c->stream;
+   if (!(limit > 0.0) || nbins <= 0) return fail(c, MDGPU_E_ARG, "RDF limit and bin count must be positive");
+   double key[11];
+   std::memcpy(key, g.h, 9 * sizeof(double));
+   key[9] = limit;
+   key[10] = (double)(g.nx + 1000 * (g.ny + 1000 * g.nz));
+   if (d.rdf_nfull == 0 || std::memcmp(key, d.rdf_key, sizeof key) != 0) {
+      std::vector<int4> full;
+      mdgpu_status s = build_rdf_stencil(g.h, limit, g.nx, g.ny, g.nz, full);
+      if (s == MDGPU_E_CUTOFF)
+         return fail(c, s, "RDF limit > 1 * cell dimension (neighbour cells beyond one image)");
+      if (s) return fail(c, s, "RDF stencil");
+      CK(d.rdf_full.ensure(full.size()));
+      CK(cudaMemcpyAsync(d.rdf_full.p, full.data(), full.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+      d.rdf_nfull = (int)full.size();
+      std::memcpy(d.rdf_key, key, sizeof key);
+   }
+   const size_t nh = (size_t)c->max_id * c->max_id * nbins;
+   CK(d.rdf_counts.ensure(nh));
+   CK(cudaMemsetAsync(d.rdf_counts.p, 0, nh * sizeof(unsigned long long), st));
+   RsParams P = make_params(c);
+   P.nfull = d.rdf_nfull;
+   const double rbin = (double)nbins / limit;   // src/rdf.c:99
+   const int N = c->nsites;
+   k_rdf<<<(N + PAIR_WARPS - 1) / PAIR_WARPS, PAIR_WARPS * 32, 0, st>>>(
+      P, d.cell_start.p, d.slot_cell.p, d.rdf_full.p, d.tag.p, d.sorted.p, c->cur_site, rbin, nbins, d.rdf_counts.p);
+   CK(cudaGetLastError());
+   c->launches += 1;
    return MDGPU_OK;
 }
 

@@ -162,6 +162,18 @@ class ForceField:
         self._check(st)
         return np.sort(keys[:cnt.value])
 
+    def rdf_counts(self, limit: float, nbins: int, site: Optional[np.ndarray] = None,
+                   c_of_m: Optional[np.ndarray] = None) -> np.ndarray:
+        """Unordered site-pair counts [max_id, max_id, nbins] of the
+        reference's RDF accumulation (bin = int(nbins/limit * r))."""
+        site = np.ascontiguousarray(self.sysm.site if site is None else site, np.float64)
+        cm = np.ascontiguousarray(self.sysm.c_of_m if c_of_m is None else c_of_m, np.float64)
+        M = self.sysm.max_id
+        out = np.zeros(M * M * nbins, np.uint64)
+        self._check(self.L.mdgpu_rdf_counts(self.ctx, _dp(self._h()), _dp(site), _dp(cm), float(limit), int(nbins),
+                                            out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out.reshape(M, M, nbins)
+
     # -- adjoint -------------------------------------------------------------
     def _params(self, potpar, chg, alpha):
         keep = []

@@ -43,19 +43,26 @@ class RefResult:
     stdout: str
     t_force: Optional[float] = None
     t_ewald: Optional[float] = None
+    rdf: Optional[np.ndarray] = None   # the reference's float RDF histogram (rdf_ptr layout)
 
     def notes(self):
         return [l.strip() for l in self.stdout.splitlines() if l.strip().startswith("*")]
 
 
-def run(sysm, want_pairs: bool = False, repeats: int = 1, fast: bool = False) -> RefResult:
+def run(sysm, want_pairs: bool = False, repeats: int = 1, fast: bool = False,
+        rdf: Optional[tuple] = None) -> RefResult:
+    """rdf = (limit, nbins): also accumulate the reference's RDF histogram on
+    the first force_calc call."""
     from moldy_gb300.system import write_mdsys
     exe = os.path.join(REF_DIR, "moldy_ref_harness_fast" if fast else "moldy_ref_harness")
     n = sysm.nsites
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.mdsys"), os.path.join(td, "out.bin")
         write_mdsys(fin, sysm, want_pairs)
-        cp = subprocess.run([exe, fin, fout, str(repeats)], capture_output=True, text=True)
+        env = dict(os.environ)
+        if rdf is not None:
+            env["MDGPU_REF_RDF"] = f"{float(rdf[0])!r} {int(rdf[1])}"
+        cp = subprocess.run([exe, fin, fout, str(repeats)], capture_output=True, text=True, env=env)
         if cp.returncode != 0:
             raise RuntimeError(f"reference harness failed ({cp.returncode}): {cp.stdout[-2000:]}{cp.stderr[-2000:]}")
         raw = open(fout, "rb").read()
@@ -72,8 +79,13 @@ def run(sysm, want_pairs: bool = False, repeats: int = 1, fast: bool = False) ->
     pairs = None
     if npairs >= 0:
         pairs = np.frombuffer(raw, dtype="<i4", count=3 * npairs, offset=off + 8).reshape(-1, 3).copy()
+    off += 8 + (12 * npairs if npairs > 0 else 0)
+    hist = None
+    if rdf is not None:
+        size = int(np.frombuffer(raw, dtype="<i8", count=1, offset=off)[0])
+        hist = np.frombuffer(raw, dtype="<f4", count=size, offset=off + 8).copy()
     tf = te = None
     m = re.search(r"HARNESS_TIMING force_calc (\S+) ewald (\S+)", cp.stdout)
     if m:
         tf, te = float(m.group(1)), float(m.group(2))
-    return RefResult(fr, float(per), sr, fe, float(pee), se, pairs, cp.stdout, tf, te)
+    return RefResult(fr, float(per), sr, fe, float(pee), se, pairs, cp.stdout, tf, te, hist)

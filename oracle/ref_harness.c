@@ -20,6 +20,12 @@
  * Only the tests and the fixture generator run this program; it is never on
  * the product path and is not built on machines without the reference.
  *
+ * With MDGPU_REF_RDF="limit nbins" in the environment the first force_calc
+ * call also accumulates the reference's radial distribution histogram
+ * (rdf_inner/rdf_accum, src/force.c:1010-1103, src/rdf.c:94-107, after
+ * init_rdf) and the histogram (rdf_ptr's float array) is appended to the
+ * output as int64 size + float[size].
+ *
  * usage: moldy_ref_harness in.mdsys out.bin [repeats]
  */
 #define _GNU_SOURCE
@@ -39,6 +45,8 @@ void force_calc(real **site, real **site_force, system_mt *system, spec_mt *spec
                 real *chg, pot_mt *potpar, double *pe, mat_mt stress);
 void ewald(real **site, real **site_force, system_mp system, spec_mt *species,
            real *chg, double *pe, mat_mt stress);
+void init_rdf(system_mp system);
+gptr *rdf_ptr(int *size);
 
 /* ---- pair capture ------------------------------------------------------ */
 static int      cap_on = 0;
@@ -134,6 +142,18 @@ int main(int argc, char **argv)
    control.page_width = 132;
    control.page_length = 1000000;
    cap_on = hdr[7];
+   {
+      const char *e = getenv("MDGPU_REF_RDF");
+      double lim;
+      int nb;
+      if (e && sscanf(e, "%lf %d", &lim, &nb) == 2) {
+         control.limit = lim;
+         control.nbins = nb;
+         control.rdf_interval = 1;   /* step 0 is an RDF step (src/force.c:1302-1304) */
+         control.begin_rdf = 0;
+         control.istep = 0;
+      }
+   }
 
    memset(&sys, 0, sizeof sys);
    sys.nsites = nsites; sys.nmols = nmols; sys.nspecies = nspecies; sys.max_id = max_id;
@@ -184,7 +204,9 @@ int main(int argc, char **argv)
       f_ew[i] = fe + (size_t)i * nsites;
    }
 
+   if (control.rdf_interval > 0) init_rdf(&sys);
    for (r = 0; r < repeats; r++) {
+      if (r > 0) control.rdf_interval = 0;   /* one accumulation only */
       memset(fr, 0, sizeof(double) * 3 * nsites);
       memset(fe, 0, sizeof(double) * 3 * nsites);
       memset(stress_r, 0, sizeof stress_r);
@@ -217,6 +239,13 @@ int main(int argc, char **argv)
       int64_t n = hdr[7] ? cap_n : -1;
       fwrite(&n, 8, 1, o);
       if (n > 0) fwrite(cap_pairs, 4, 3 * (size_t)n, o);
+   }
+   if (getenv("MDGPU_REF_RDF")) {
+      int size = 0;
+      float *h = (float *)rdf_ptr(&size);
+      int64_t n = size;
+      fwrite(&n, 8, 1, o);
+      fwrite(h, 4, (size_t)size, o);
    }
    fclose(o);
    return 0;

@@ -79,7 +79,7 @@ def make(name, sysm):
 
 def examples():
     exe = os.path.join(ROOT, "oracle", "_ref", "moldy_ref_examples")
-    for c in ["water", "tips2", "tip4p", "mgclh2o", "argon", "quartz"]:
+    for c in ["water", "tips2", "tip4p", "mgclh2o", "argon", "quartz", "clay"]:
         with tempfile.TemporaryDirectory() as td:
             wd = os.path.join(td, "ex")
             shutil.copytree(os.path.join(REF_SRC, "examples"), wd)

@@ -10,6 +10,12 @@
  * writes forces/energies/stress in the layout of oracle/ref_harness.c, so the
  * tests compare it with the reference's golden outputs.
  *
+ * With DRIVER_RDF="limit nbins" in the environment the first call is an RDF
+ * step (control.rdf_interval = 1 at istep 0): the library adds the pair
+ * histogram into the driver's RDF array, which stands in for the
+ * reference's rdf.c (rdf_ptr, src/rdf.c:58-62, with init_rdf's layout), and
+ * the array is appended to the output as int64 size + float[size].
+ *
  * usage: ref_abi_driver in.mdsys out.bin
  */
 #include <stdarg.h>
@@ -53,6 +59,15 @@ void message(int *nerrs, ...)
    }
 }
 
+static float *rdf_base = NULL;
+static int rdf_size = 0;
+
+void *rdf_ptr(int *size)
+{
+   *size = rdf_size;
+   return rdf_base;
+}
+
 static void rd(void *p, size_t sz, size_t n, FILE *f)
 {
    if (fread(p, sz, n, f) != n) {
@@ -90,6 +105,19 @@ int main(int argc, char **argv)
    control.subcell = cd[1];
    control.alpha = cd[2];
    control.k_cutoff = cd[3];
+   if (getenv("DRIVER_RDF")) {
+      double lim;
+      int nb;
+      if (sscanf(getenv("DRIVER_RDF"), "%lf %d", &lim, &nb) == 2) {
+         control.limit = lim;
+         control.nbins = nb;
+         control.rdf_interval = 1;
+         control.begin_rdf = 0;
+         control.istep = 0;
+         rdf_size = nb * max_id * (max_id - 1) / 2;
+         rdf_base = (float *)calloc(rdf_size, sizeof(float));
+      }
+   }
    memset(&sys, 0, sizeof sys);
    sys.nsites = nsites; sys.nmols = nmols; sys.nspecies = nspecies; sys.max_id = max_id;
    sys.ptype = hdr[4];
@@ -149,6 +177,12 @@ int main(int argc, char **argv)
    fwrite(&pe[1], 8, 1, o);
    fwrite(stress_e, 8, 9, o);
    fwrite(&npairs, 8, 1, o);
+   if (rdf_base) {
+      int64_t n = rdf_size;
+      fwrite(&n, 8, 1, o);
+      fwrite(rdf_base, 4, (size_t)rdf_size, o);
+      control.rdf_interval = 0;   /* the second call below is not an RDF step */
+   }
    fclose(o);
    /* a second step on the same arrays: the notes must not repeat */
    memset(fr, 0, 6 * sizeof(double) * (size_t)nsites);

@@ -27,15 +27,22 @@ def driver():
     return out
 
 
-def run_driver(exe, sysm, precision):
+def run_driver(exe, sysm, precision, rdf=None):
     n = sysm.nsites
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.mdsys"), os.path.join(td, "out.bin")
         write_mdsys(fin, sysm)
         env = dict(os.environ, MDGPU_PRECISION=precision)
+        if rdf is not None:
+            env["DRIVER_RDF"] = f"{float(rdf[0])!r} {int(rdf[1])}"
         cp = subprocess.run([exe, fin, fout], capture_output=True, text=True, env=env)
         assert cp.returncode == 0, cp.stdout + cp.stderr
         d = np.fromfile(fout, dtype="<f8", count=2 * (3 * n + 10))
+        if rdf is not None:
+            raw = open(fout, "rb").read()
+            off = 8 * (2 * (3 * n + 10) + 1)
+            size = int(np.frombuffer(raw, "<i8", 1, off)[0])
+            return np.frombuffer(raw, "<f4", size, off + 8).copy()
     fr = d[:3 * n].reshape(3, n)
     o = 3 * n + 10
     return (fr, d[3 * n], d[3 * n + 1:o].reshape(3, 3), d[o:o + 3 * n].reshape(3, n), d[o + 3 * n],
@@ -62,3 +69,13 @@ def test_reference_signatures_reproduce_the_reference(driver, name, prec, tol):
     want = [str(n) for n in z["notes"] if str(n).startswith("*I*")]
     got = [l.strip() for l in out.splitlines() if l.strip().startswith("*I*")]
     assert got == want, (got, want)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["rdf_water864", "rdf_argon500"])
+def test_rdf_step_fills_the_callers_histogram_like_the_reference(driver, name, prec):
+    """An RDF step through the reference's force_calc signature adds into the
+    caller's RDF array exactly what the reference's rdf_accum adds."""
+    sysm, z = load_npz(os.path.join(GOLDEN, name + ".npz"))
+    got = run_driver(driver, sysm, prec, rdf=(float(z["rdf_limit"]), int(z["rdf_nbins"])))
+    assert np.array_equal(got, z["ref_rdf"]), int(np.sum(got != z["ref_rdf"]))
