@@ -13,7 +13,11 @@
  * made from force_inner (src/force.c:960), the pairs
  * (isite = nab[jmin-1], nab[j], pbctrans[j]) for j in [jmin, jmax)
  * (the cell's own sites come first in nab and jmin advances once per site,
- * src/force.c:889-917).  kernel() calls made by poteval() during the
+ * src/force.c:889-917).  A framework site is called with jmin = 0 against
+ * the non-framework sites [0, nfnab[0]) (src/force.c:904-908); the
+ * framework entries head each cell's list (framework species come last and
+ * the lists are LIFO), so they are taken in the cell's list order, read
+ * from the cell list handed to site_neighbour_list.  kernel() calls made by poteval() during the
  * first-call intramolecular correction happen before any neighbour list
  * exists and are not recorded.
  *
@@ -49,6 +53,12 @@ void init_rdf(system_mp system);
 gptr *rdf_ptr(int *size);
 
 /* ---- pair capture ------------------------------------------------------ */
+/* a link-cell entry (src/force.c:42-46) */
+typedef struct cell_s {
+   int isite, num, frame_type;
+   struct cell_s *next;
+} cell_entry;
+static int      fw_queue[4096], fw_head = 0, fw_n = 0;
 static int      cap_on = 0;
 static int     *cap_nab = NULL, *cap_trans = NULL;
 static int64_t  cap_n = 0, cap_cap = 0;
@@ -64,6 +74,15 @@ int site_neighbour_list(int *nab, int *pbctrans, int n_nab_sites, int *nfnab,
    if (!orig) orig = (snl_fn)dlsym(RTLD_NEXT, "site_neighbour_list");
    cap_nab = nab;
    cap_trans = pbctrans;
+   fw_head = fw_n = 0;
+   if (n_frame_types > 1) {
+      const cell_entry *e = ((cell_entry **)cell)[iz + nz * (iy + ny * ix)];
+      for (; e; e = e->next)
+         if (e->frame_type) {
+            int k;
+            for (k = 0; k < e->num && fw_n < 4096; k++) fw_queue[fw_n++] = e->isite + k;
+         }
+   }
    return orig(nab, pbctrans, n_nab_sites, nfnab, n_frame_types, n_nabors, ix, iy, iz,
                nx, ny, nz, nabor, cell, pbclookup);
 }
@@ -76,8 +95,8 @@ void kernel(int jmin, int nnab, real *forceij, double *pe, real *r_sqr, real *na
    static kern_fn orig = NULL;
    int j;
    if (!orig) orig = (kern_fn)dlsym(RTLD_NEXT, "kernel");
-   if (cap_on && cap_nab && jmin > 0) {
-      int isite = cap_nab[jmin - 1];
+   if (cap_on && cap_nab && (jmin > 0 || fw_head < fw_n)) {
+      int isite = jmin > 0 ? cap_nab[jmin - 1] : fw_queue[fw_head++];
       for (j = jmin; j < nnab; j++) {
          if (cap_n >= cap_cap) {
             cap_cap = cap_cap ? 2 * cap_cap : (1 << 20);
