@@ -30,6 +30,7 @@
 #include <cstring>
 
 #include "mdgpu_internal.h"
+#include "f32x2.cuh"
 #include "phase.cuh"
 
 namespace mdgpu {
@@ -101,7 +102,7 @@ __device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c)
 
 
 // ---------------------------------------------------------------- S(k)
-constexpr int SF_TILE = 128;
+constexpr int SF_TILE = 128;     // sites per shared-memory tile (FP64 pass: half)
 
 // Each site's k-vectors of one item are seed * zp[t] with zp[t] =
 // exp(2 pi i t s_z) from the per-site table (k_prep): every term is at most
@@ -155,7 +156,6 @@ k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nit
          if (t < hd.w) dst[t] = make_float2(ac[t], as[t]);
    }
 }
-
 
 __global__ void __launch_bounds__(128)
 k_sfac64(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nitems,
@@ -305,9 +305,12 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    __shared__ int4 s_it[FT_ITEMS];
    __shared__ float2 s_kxy[FT_ITEMS];
    __shared__ int s_k0[FT_ITEMS];
-   __shared__ float4 s_kd[FT_ITEMS * KI];
+   // per k, duplicated for the paired instructions: (A, A, -B, -B), (kz, kz)
+   __shared__ ulonglong2 s_ab[FT_ITEMS * KI];
+   __shared__ unsigned long long s_kz[FT_ITEMS * KI];
    // two sites per thread, FT_THREADS apart: they share every load of the
-   // per-k coefficients and the item bookkeeping
+   // per-k coefficients and the item bookkeeping, and run as the two lanes
+   // of paired FP32 instructions (f32x2)
    const int i0 = blockIdx.x * (2 * FT_THREADS) + threadIdx.x, i1 = i0 + FT_THREADS;
    const bool live0 = i0 < N, live1 = i1 < N;
    const int4 va = live0 ? ph[i0] : make_int4(0, 0, 0, 0);
@@ -316,15 +319,13 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    // k-vectors of an item are seed * zp[t], so per-site phase errors do not
    // accumulate along l (the force multiplies them by |S(k)|, which is of
    // order N q at the Bragg peaks of a crystal).
-   float zca[KI], zsa[KI], zcb[KI], zsb[KI];
+   f2x zc[KI], zs[KI];
 #pragma unroll
    for (int t = 0; t < KI; t++) {
       const float2 za = live0 ? zz[(size_t)i0 * KI + t] : make_float2(1.f, 0.f);
       const float2 zb = live1 ? zz[(size_t)i1 * KI + t] : make_float2(1.f, 0.f);
-      zca[t] = za.x;
-      zsa[t] = za.y;
-      zcb[t] = zb.x;
-      zsb[t] = zb.y;
+      zc[t] = pk2(za.x, zb.x);
+      zs[t] = pk2(za.y, zb.y);
    }
    const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
    // compensated (Kahan) FP32 sums, taken every 4 items of plain FP32
@@ -332,7 +333,7 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    // retires two lanes per clock per SM; a periodic FP64 fold halved the rate)
    float fxa = 0.f, fya = 0.f, fza = 0.f, exa = 0.f, eya = 0.f, eza = 0.f;
    float fxb = 0.f, fyb = 0.f, fzb = 0.f, exb = 0.f, eyb = 0.f, ezb = 0.f;
-   float pxa = 0.f, pya = 0.f, pza = 0.f, pxb = 0.f, pyb = 0.f, pzb = 0.f;
+   f2x px = 0ull, py = 0ull, pz = 0ull;
    int npart = 0;
    for (int tb = a; tb < b; tb += FT_ITEMS) {
       const int nt = min(FT_ITEMS, b - tb);
@@ -344,7 +345,11 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
          s_kxy[q] = item_kxy[tb + q];
          s_k0[q] = item_k0[tb + q] - kb;
       }
-      for (int q = threadIdx.x; q < ke - kb; q += blockDim.x) s_kd[q] = kd[kb + q];
+      for (int q = threadIdx.x; q < ke - kb; q += blockDim.x) {
+         const float4 k4 = kd[kb + q];
+         s_ab[q] = make_ulonglong2(pk2(k4.x, k4.x), pk2(-k4.y, -k4.y));
+         s_kz[q] = pk2(k4.z, k4.z);
+      }
       __syncthreads();
       for (int q = 0; q < nt; q++) {
          const int4 hd = s_it[q];
@@ -357,49 +362,53 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
          float sa0, ca0, sb0, cb0;
          sincos_poly(pa, &sa0, &ca0);
          sincos_poly(pb, &sb0, &cb0);
-         float sfa = 0.f, skza = 0.f, sfb = 0.f, skzb = 0.f;
-         const float4 *kq = s_kd + s_k0[q];
+         const f2x c0 = pk2(ca0, cb0), s0 = pk2(sa0, sb0), ns0 = pk2(-sa0, -sb0);
+         f2x sf = 0ull, skz = 0ull;
+         const ulonglong2 *abq = s_ab + s_k0[q];
+         const unsigned long long *kzq = s_kz + s_k0[q];
 #pragma unroll
          for (int t = 0; t < KI; t++) {
             if (t < hd.w) {
-               const float4 k4 = kq[t];
-               const float csa = ca0 * zca[t] - sa0 * zsa[t];
-               const float sna = fmaf(sa0, zca[t], ca0 * zsa[t]);
-               const float fa = fmaf(sna, k4.x, -csa * k4.y);
-               sfa += fa;
-               skza = fmaf(k4.z, fa, skza);
-               const float csb = cb0 * zcb[t] - sb0 * zsb[t];
-               const float snb = fmaf(sb0, zcb[t], cb0 * zsb[t]);
-               const float fb = fmaf(snb, k4.x, -csb * k4.y);
-               sfb += fb;
-               skzb = fmaf(k4.z, fb, skzb);
+               const ulonglong2 ab = abq[t];
+               const f2x cs = fma2(c0, zc[t], mul2(ns0, zs[t]));   // cos of k.r, both sites
+               const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));    // sin of k.r
+               const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));       // sin A - cos B
+               sf = add2(sf, f);
+               skz = fma2(kzq[t], f, skz);
             }
          }
          const float2 kxy = s_kxy[q];
-         pxa = fmaf(kxy.x, sfa, pxa);
-         pya = fmaf(kxy.y, sfa, pya);
-         pza += skza;
-         pxb = fmaf(kxy.x, sfb, pxb);
-         pyb = fmaf(kxy.y, sfb, pyb);
-         pzb += skzb;
+         px = fma2(pk2(kxy.x, kxy.x), sf, px);
+         py = fma2(pk2(kxy.y, kxy.y), sf, py);
+         pz = add2(pz, skz);
          if (++npart == 4) {
-            kahan_add(fxa, exa, pxa);
-            kahan_add(fya, eya, pya);
-            kahan_add(fza, eza, pza);
-            kahan_add(fxb, exb, pxb);
-            kahan_add(fyb, eyb, pyb);
-            kahan_add(fzb, ezb, pzb);
-            pxa = pya = pza = pxb = pyb = pzb = 0.f;
+            float xa, xb, ya, yb, za, zb;
+            upk2(px, xa, xb);
+            upk2(py, ya, yb);
+            upk2(pz, za, zb);
+            kahan_add(fxa, exa, xa);
+            kahan_add(fya, eya, ya);
+            kahan_add(fza, eza, za);
+            kahan_add(fxb, exb, xb);
+            kahan_add(fyb, eyb, yb);
+            kahan_add(fzb, ezb, zb);
+            px = py = pz = 0ull;
             npart = 0;
          }
       }
    }
-   kahan_add(fxa, exa, pxa);
-   kahan_add(fya, eya, pya);
-   kahan_add(fza, eza, pza);
-   kahan_add(fxb, exb, pxb);
-   kahan_add(fyb, eyb, pyb);
-   kahan_add(fzb, ezb, pzb);
+   {
+      float xa, xb, ya, yb, za, zb;
+      upk2(px, xa, xb);
+      upk2(py, ya, yb);
+      upk2(pz, za, zb);
+      kahan_add(fxa, exa, xa);
+      kahan_add(fya, eya, ya);
+      kahan_add(fza, eza, za);
+      kahan_add(fxb, exb, xb);
+      kahan_add(fyb, eyb, yb);
+      kahan_add(fzb, ezb, zb);
+   }
    // site oi's partial goes to row oi - obase of [3][N] (obase = 0 except
    // for a subset of sites held compactly)
    double *dst = fpart + (size_t)blockIdx.y * 3 * N;
