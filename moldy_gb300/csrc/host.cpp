@@ -5,6 +5,7 @@
 // per-site and per-pair work runs in the CUDA kernels.  Built with
 // -ffp-contract=off: every expression is evaluated in the written order, as
 // the reference's binning and cut-off decisions require.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -258,6 +259,35 @@ mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl)
       }
    kl.nk = nk;
    kl.nitems = (int)kl.item.size();
+   // Items with the same k count side by side, full ones first: a warp (or a
+   // block, in the force pass) then meets one count at a time and the full
+   // items take a path with no per-k predicate.  Only the order of the sum
+   // over k changes.
+   std::vector<int> order(kl.nitems);
+   for (int i = 0; i < kl.nitems; i++) order[i] = i;
+   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return kl.item[a].w > kl.item[b].w; });
+   KList o;
+   o.item.reserve(kl.nitems);
+   int k0 = 0;
+   for (int i : order) {
+      const int4 it = kl.item[i];
+      o.item.push_back(it);
+      o.item_k0.push_back(k0);
+      o.item_kxy.push_back(kl.item_kxy[i]);
+      for (int t = 0; t < it.w; t++) {
+         const int k = kl.item_k0[i] + t;
+         o.kz.push_back(kl.kz[k]);
+         o.coeff.push_back(kl.coeff[k]);
+         o.coeff2.push_back(kl.coeff2[k]);
+      }
+      k0 += it.w;
+   }
+   kl.item.swap(o.item);
+   kl.item_k0.swap(o.item_k0);
+   kl.item_kxy.swap(o.item_kxy);
+   kl.kz.swap(o.kz);
+   kl.coeff.swap(o.coeff);
+   kl.coeff2.swap(o.coeff2);
    return MDGPU_OK;
 }
 

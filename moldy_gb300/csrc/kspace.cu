@@ -129,21 +129,40 @@ k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nit
       for (int q = threadIdx.x; q < nt; q += blockDim.x) sph[q] = ph[tb + q];
       for (int q = threadIdx.x; q < nt * KI; q += blockDim.x) szp[q] = zp[(size_t)tb * KI + q];
       __syncthreads();
-      for (int q = 0; q < nt; q++) {
-         const int4 v = sph[q];
-         const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
-         float sn, cs;
-         sincos_poly(p, &sn, &cs);
-         const float qv = __int_as_float(v.w);
-         cs *= qv;
-         sn *= qv;
-         const float2 *z = szp + q * KI;
+      if (hd.w == KI) {   // full items (grouped first in the list): no per-k predicate
+         for (int q = 0; q < nt; q++) {
+            const int4 v = sph[q];
+            const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
+            float sn, cs;
+            sincos_poly(p, &sn, &cs);
+            const float qv = __int_as_float(v.w);
+            cs *= qv;
+            sn *= qv;
+            const float2 *z = szp + q * KI;
 #pragma unroll
-         for (int t = 0; t < KI; t++) {
-            if (t < hd.w) {
+            for (int t = 0; t < KI; t++) {
                const float2 zt = z[t];
                ac[t] = fmaf(cs, zt.x, fmaf(-sn, zt.y, ac[t]));
                as[t] = fmaf(sn, zt.x, fmaf(cs, zt.y, as[t]));
+            }
+         }
+      } else {
+         for (int q = 0; q < nt; q++) {
+            const int4 v = sph[q];
+            const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
+            float sn, cs;
+            sincos_poly(p, &sn, &cs);
+            const float qv = __int_as_float(v.w);
+            cs *= qv;
+            sn *= qv;
+            const float2 *z = szp + q * KI;
+#pragma unroll
+            for (int t = 0; t < KI; t++) {
+               if (t < hd.w) {
+                  const float2 zt = z[t];
+                  ac[t] = fmaf(cs, zt.x, fmaf(-sn, zt.y, ac[t]));
+                  as[t] = fmaf(sn, zt.x, fmaf(cs, zt.y, as[t]));
+               }
             }
          }
       }
@@ -366,15 +385,27 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
          f2x sf = 0ull, skz = 0ull;
          const ulonglong2 *abq = s_ab + s_k0[q];
          const unsigned long long *kzq = s_kz + s_k0[q];
+         if (hd.w == KI) {   // full item (block-uniform): no per-k predicate
 #pragma unroll
-         for (int t = 0; t < KI; t++) {
-            if (t < hd.w) {
+            for (int t = 0; t < KI; t++) {
                const ulonglong2 ab = abq[t];
                const f2x cs = fma2(c0, zc[t], mul2(ns0, zs[t]));   // cos of k.r, both sites
                const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));    // sin of k.r
                const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));       // sin A - cos B
                sf = add2(sf, f);
                skz = fma2(kzq[t], f, skz);
+            }
+         } else {
+#pragma unroll
+            for (int t = 0; t < KI; t++) {
+               if (t < hd.w) {
+                  const ulonglong2 ab = abq[t];
+                  const f2x cs = fma2(c0, zc[t], mul2(ns0, zs[t]));
+                  const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));
+                  const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));
+                  sf = add2(sf, f);
+                  skz = fma2(kzq[t], f, skz);
+               }
             }
          }
          const float2 kxy = s_kxy[q];

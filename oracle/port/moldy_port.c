@@ -388,6 +388,8 @@ typedef struct {
    int nx, ny, nz, ncells, n_nabors;
    off3 *nabor;
    int *ent_site, *ent_num;  /* cell entries (sites, or molecules)   */
+   int *ent_fw;              /* entry belongs to the framework       */
+   int n_frame_types;        /* 1, or 2 with a framework (force.c:445-458) */
    int *cell_start, *cell_ent;/* entries of each cell, LIFO order     */
    double reloc[NIMG][3];
    int64_t nab_cap;
@@ -428,24 +430,30 @@ static void *force_inner(void *arg)
    for (icell = T->tid; icell < S->ncells; icell += S->nthreads) {   /* force.c:856 */
       int ix = icell / (ny * nz), iy = icell / nz - ny * ix, iz = icell - nz * (iy + ny * ix);
       int64_t nnab = 0;
-      int jnab, e, jmin, jmax;
+      int jnab, e, jmin, jmax, ft, nfnab0 = 0;
       if (S->cell_start[icell] == S->cell_start[icell + 1]) continue;
-      /* site neighbour list (src/force.c:521-569) */
-      for (jnab = 0; jnab < S->n_nabors; jnab++) {
-         int ex = ix + S->nabor[jnab].d[0] + nx, ey = iy + S->nabor[jnab].d[1] + ny,
-             ez = iz + S->nabor[jnab].d[2] + nz;
-         int ii = ex / nx, jj = ey / ny, kk = ez / nz;
-         int jc = (ez - kk * nz) + nz * ((ey - jj * ny) + ny * (ex - ii * nx));
-         int ktrans = 9 * ii + 3 * jj + kk;
-         for (e = S->cell_start[jc]; e < S->cell_start[jc + 1]; e++) {
-            int ent = S->cell_ent[e], s;
-            for (s = 0; s < S->ent_num[ent]; s++) {
-               if (nnab >= cap) { T->err = PORT_E_TONAB; goto done; }
-               nab[nnab] = S->ent_site[ent] + s;
-               tr[nnab] = ktrans;
-               nnab++;
+      /* site neighbour list (src/force.c:521-569): non-framework sites of
+       * every stencil cell, then framework sites of every stencil cell but
+       * the cell's own */
+      for (ft = 0; ft < S->n_frame_types; ft++) {
+         for (jnab = ft == 0 ? 0 : 1; jnab < S->n_nabors; jnab++) {
+            int ex = ix + S->nabor[jnab].d[0] + nx, ey = iy + S->nabor[jnab].d[1] + ny,
+                ez = iz + S->nabor[jnab].d[2] + nz;
+            int ii = ex / nx, jj = ey / ny, kk = ez / nz;
+            int jc = (ez - kk * nz) + nz * ((ey - jj * ny) + ny * (ex - ii * nx));
+            int ktrans = 9 * ii + 3 * jj + kk;
+            for (e = S->cell_start[jc]; e < S->cell_start[jc + 1]; e++) {
+               int ent = S->cell_ent[e], s;
+               if (S->ent_fw[ent] != ft) continue;
+               for (s = 0; s < S->ent_num[ent]; s++) {
+                  if (nnab >= cap) { T->err = PORT_E_TONAB; goto done; }
+                  nab[nnab] = S->ent_site[ent] + s;
+                  tr[nnab] = ktrans;
+                  nnab++;
+               }
             }
          }
+         if (ft == 0) nfnab0 = (int)nnab;
       }
       if (nnab > T->nab_max) T->nab_max = nnab;
       for (j = 0; j < nnab; j++) {                  /* gathers, force.c:877-884 */
@@ -459,11 +467,17 @@ static void *force_inner(void *arg)
       jmax = (int)nnab;
       for (e = S->cell_start[icell]; e < S->cell_start[icell + 1]; e++) {
          int ent = S->cell_ent[e], isite;
+         if (S->ent_fw[ent]) {                       /* force.c:904-908 */
+            jmin = 0;
+            jmax = nfnab0;
+         } else {
+            jmax = (int)nnab;
+         }
          for (isite = S->ent_site[ent]; isite < S->ent_site[ent] + S->ent_num[ent]; isite++) {
             double xi = S->x[isite], yi = S->y[isite], zi = S->z[isite];
             double si0 = 0.0, si1 = 0.0, si2 = 0.0;
             const double *prow = sys->potpar + (size_t)S->id[isite] * max_id * NPOTP_;
-            jmin++;                                  /* force.c:917 */
+            if (!S->ent_fw[ent]) jmin++;             /* force.c:916-917 */
             for (j = jmin; j < jmax; j++) {
                const double *pp = prow + (size_t)S->id[nab[j]] * NPOTP_;
                for (k = 0; k < NPOTP_; k++) pv[k][j] = pp[k];
@@ -544,8 +558,6 @@ int port_force_calc(const port_system *sys, const double *site, double *site_for
    memset(info, 0, sizeof *info);
    if (!sys || N <= 0 || nthreads < 1 || (pairs && nthreads != 1)) return PORT_E_ARG;
    if (sys->ptype < 0 || sys->ptype > 6 || sys->ptype == 5) return PORT_E_PTYPE;
-   for (s = 0; s < sys->nspecies; s++)
-      if (sys->spec_framework[s]) return PORT_E_FRAMEWORK;
    memset(&S, 0, sizeof S);
    S.sys = sys; S.x = x; S.y = y; S.z = z; S.nthreads = nthreads;
    S.pairs = pairs; S.pairs_cap = pairs_cap;
@@ -560,7 +572,8 @@ int port_force_calc(const port_system *sys, const double *site, double *site_for
    info->nx = S.nx; info->ny = S.ny; info->nz = S.nz;
    /* intramolecular correction, force.c:1156-1171 */
    for (s = 0; s < sys->nspecies; s++) {
-      eintra += sys->spec_nmols[s] * mol_intra(sys, sys->spec_site_id + so, sys->spec_pf + 3 * so,
+      if (!sys->spec_framework[s])   /* force.c:1159-1163 */
+         eintra += sys->spec_nmols[s] * mol_intra(sys, sys->spec_site_id + so, sys->spec_pf + 3 * so,
                                                sys->spec_nsites[s]);
       so += sys->spec_nsites[s];
    }
@@ -586,13 +599,16 @@ int port_force_calc(const port_system *sys, const double *site, double *site_for
    inv3(hm, hinv);
    S.ent_site = (int *)malloc(sizeof(int) * N);
    S.ent_num = (int *)malloc(sizeof(int) * N);
+   S.ent_fw = (int *)malloc(sizeof(int) * N);
+   S.n_frame_types = 1;
    {
       int *ent_cell = (int *)malloc(sizeof(int) * N);
       double fnx = S.nx, fny = S.ny, fnz = S.nz;
       isite = 0; imol = 0;
       for (s = 0; s < sys->nspecies; s++)
          for (m = 0; m < sys->spec_nmols[s]; m++, imol++) {
-            if (!sys->molpbc) {
+            if (sys->spec_framework[s]) S.n_frame_types = 2;
+            if (!sys->molpbc || sys->spec_framework[s]) {
                for (i = 0; i < sys->spec_nsites[s]; i++, isite++) {
                   double a0 = x[isite], a1 = y[isite], a2 = z[isite], s0, s1, s2;
                   s0 = hinv[0][0] * a0 + hinv[0][1] * a1 + hinv[0][2] * a2;
@@ -603,6 +619,7 @@ int port_force_calc(const port_system *sys, const double *site, double *site_for
                                            S.ny * bin1(s0, S.nx, fnx, eps, &bad));
                   S.ent_site[nent] = isite;
                   S.ent_num[nent] = 1;
+                  S.ent_fw[nent] = sys->spec_framework[s] ? 1 : 0;
                   nent++;
                }
             } else {
@@ -612,6 +629,7 @@ int port_force_calc(const port_system *sys, const double *site, double *site_for
                                         S.ny * bin1(c[0], S.nx, fnx, eps, &bad));
                S.ent_site[nent] = isite;
                S.ent_num[nent] = sys->spec_nsites[s];
+               S.ent_fw[nent] = 0;
                nent++;
                isite += sys->spec_nsites[s];
             }
@@ -721,7 +739,7 @@ int port_force_calc(const port_system *sys, const double *site, double *site_for
    free(T);
    free(th);
 out:
-   free(S.id); free(S.molmap); free(S.chg); free(S.ent_site); free(S.ent_num);
+   free(S.id); free(S.molmap); free(S.chg); free(S.ent_site); free(S.ent_num); free(S.ent_fw);
    free(S.cell_start); free(S.cell_ent); free(S.nabor);
    return err;
 }

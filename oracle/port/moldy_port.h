@@ -56,7 +56,7 @@ enum {
    PORT_E_RANGE = -3,        /* co-ordinate out of range in binning           */
    PORT_E_TONAB = -4,        /* neighbour-site list capacity exceeded (TONAB)  */
    PORT_E_PTYPE = -5,        /* unknown potential type (UNKPTY)               */
-   PORT_E_FRAMEWORK = -6,    /* frameworks are not supported                 */
+   PORT_E_FRAMEWORK = -6,    /* (not returned: frameworks are restated too)  */
    PORT_E_NOMEM = -7,
    PORT_E_PAIRCAP = -8       /* pair output buffer too small                  */
 };

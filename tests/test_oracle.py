@@ -21,9 +21,6 @@ def rel_rms(a, b):
 def test_port_matches_reference_fixture(name, port_built):
     port = port_built
     sysm, z = load_npz(os.path.join(GOLDEN, name + ".npz"))
-    if any(sp.framework for sp in sysm.species):
-        pytest.skip("the C restatement covers systems without a framework molecule; "
-                    "framework fixtures are held against the reference's own outputs (GPU tests)")
     r = port.force_calc(sysm, want_pairs=True)
     # real space: the port evaluates the same expressions in the same order
     assert rel_rms(r.force, z["force_real"]) < 1e-13
