@@ -278,7 +278,7 @@ void mdgpu_destroy(mdgpu_ctx *c)
    r.sorted.release(); r.blocksum.release(); r.pos64.release(); r.pos32.release(); r.tag.release();
    r.molmap.release(); r.siteid.release(); r.ent_mol.release(); r.chg.release(); r.cofm.release();
    r.full.release(); r.off_hi.release(); r.off_lo.release(); r.pot64.release(); r.pot32.release();
-   r.part.release(); r.keys.release();
+   r.part.release(); r.part2.release(); r.keys.release();
    KsDev &k = c->kd;
    k.item.release(); k.item_k0.release(); k.item_kxy64.release(); k.item_kxy32.release();
    k.kz64.release(); k.coeff.release(); k.coeff2.release(); k.kdat32.release(); k.kdat64.release();

@@ -292,26 +292,40 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
    }
 }
 
-// Energy record of the step; the record index is a device counter so that
-// a captured step replays unchanged.
-__global__ void k_md_record(int *__restrict__ counter, int cap, const double *__restrict__ pe,
-                            const double *__restrict__ kpart, int nb, double dist_v,
-                            const DevOut *__restrict__ out, double *__restrict__ energies, int *__restrict__ err)
+// Energy record of the step (one block of 128 threads): the kinetic-energy
+// block sums reduced in a fixed order; the record index is a device counter
+// so that a captured step replays unchanged.
+__global__ void __launch_bounds__(128)
+k_md_record(int *__restrict__ counter, int cap, const double *__restrict__ pe, const double *__restrict__ kpart,
+            int nb, double dist_v, const DevOut *__restrict__ out, double *__restrict__ energies,
+            int *__restrict__ err)
 {
-   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-   const int step = *counter;
-   *counter = step + 1;
-   if (step >= cap) return;
+   __shared__ double sh[2][128];
+   const int t = threadIdx.x;
    double kt = 0.0, kr = 0.0;
-   for (int b = 0; b < nb; b++) {
+   for (int b = t; b < nb; b += 128) {
       kt += kpart[2 * b];
       kr += kpart[2 * b + 1];
    }
+   sh[0][t] = kt;
+   sh[1][t] = kr;
+   __syncthreads();
+   for (int w = 64; w > 0; w >>= 1) {
+      if (t < w) {
+         sh[0][t] += sh[0][t + w];
+         sh[1][t] += sh[1][t + w];
+      }
+      __syncthreads();
+   }
+   if (t != 0) return;
+   const int step = *counter;
+   *counter = step + 1;
+   if (step >= cap) return;
    double *e = energies + 4 * (size_t)step;
    e[0] = pe[0] + dist_v;
    e[1] = pe[1];
-   e[2] = kt;
-   e[3] = kr;
+   e[2] = sh[0][0];
+   e[3] = sh[1][0];
    if (out->err & 1) *err |= 1;
 }
 
@@ -469,7 +483,7 @@ static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap
    if (s) return s;
    k_md_kick<<<nbm, 256, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.mol_site0.p, D.pf.p, c->force.p,
                                   D.quat.p, D.mom.p, D.amom.p, D.kpart.p);
-   k_md_record<<<1, 32, 0, st>>>(D.counter.p, cap, c->small.p, D.kpart.p, nbm, dist_v, c->out.p, D.energies.p,
+   k_md_record<<<1, 128, 0, st>>>(D.counter.p, cap, c->small.p, D.kpart.p, nbm, dist_v, c->out.p, D.energies.p,
                                  D.err.p);
    k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
                                                 D.amom.p, D.err.p);

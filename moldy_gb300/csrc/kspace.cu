@@ -292,13 +292,26 @@ k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__
    }
 }
 
-__global__ void k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *out)
+// Per-block energy/stress partials summed in a fixed order by one block of
+// 256 threads (launch with 256): thread t takes blocks t, t+256, ..., then a
+// fixed-shape tree.
+__global__ void __launch_bounds__(256) k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *out)
 {
-   int k = threadIdx.x;
-   if (k >= 7) return;
-   double s = 0.0;
-   for (int b = 0; b < nblocks; b++) s += blk[b * 8 + k];
-   if (k == 0) out->pe_k = s; else out->st_k[k - 1] = s;
+   __shared__ double sh[7][256];
+   const int t = threadIdx.x;
+   double v[7] = {0, 0, 0, 0, 0, 0, 0};
+   for (int b = t; b < nblocks; b += blockDim.x)
+      for (int k = 0; k < 7; k++) v[k] += blk[b * 8 + k];
+   for (int k = 0; k < 7; k++) sh[k][t] = v[k];
+   __syncthreads();
+   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (t < w)
+         for (int k = 0; k < 7; k++) sh[k][t] += sh[k][t + w];
+      __syncthreads();
+   }
+   if (t < 7) {
+      if (t == 0) out->pe_k = sh[0][0]; else out->st_k[t - 1] = sh[t][0];
+   }
 }
 
 // ---------------------------------------------------------------- forces
@@ -798,7 +811,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       k_kreduce<false><<<nbk, 256, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
                                             d.coeff2.p, nullptr, d.kdat64.p, d.blk.p);
    }
-   k_kfinal<<<1, 32, 0, st>>>(d.blk.p, nbk, out);
+   k_kfinal<<<1, 256, 0, st>>>(d.blk.p, nbk, out);
    CK(cudaGetLastError());
    CK(d.fpart.ensure((size_t)sh.splits * 3 * N));
    phase_mark(c, MDGPU_PH_KFORCE);

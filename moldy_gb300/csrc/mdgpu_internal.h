@@ -119,6 +119,7 @@ struct RsDev {
    DBuf<double> pot64;
    DBuf<float> pot32;
    DBuf<double> part;      // per-block partial energies/virials
+   DBuf<double> part2;     // their first-level sums
    DBuf<unsigned long long> keys;
    DBuf<int4> rdf_full;    // RDF stencil (strict, at the RDF limit)
    DBuf<unsigned long long> rdf_counts;

@@ -258,7 +258,7 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    k_sfac32<<<dim3((ni + 127) / 128, chunks), 128, 0, st>>>(item, k0, ni, ph, zp, N, chunk, nk, part);
    const int nbk = (nk + 255) / 256;
    k_kreduce_na<<<nbk, 256, 0, st>>>(nk, chunks, part, kvec, coef, coef2, kdat, blk);
-   k_kfinal<<<1, 32, 0, st>>>(blk, nbk, out);
+   k_kfinal<<<1, 256, 0, st>>>(blk, nbk, out);
    int splits = (ni + 7) / 8;
    if (splits > MAX_SPLITS) splits = MAX_SPLITS;
    if (splits < 1) splits = 1;

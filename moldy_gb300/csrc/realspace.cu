@@ -638,23 +638,43 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
    if (lane == 0 && cnt) atomicAdd((unsigned long long *)&out->npairs2, cnt);
 }
 
-// One block of 256 threads: thread t sums blocks t, t+256, ... of each
-// component, then a fixed-shape tree combines the 256 partial sums (the
-// result does not depend on timing).
-__global__ void __launch_bounds__(256) k_reduce_rs(const double *__restrict__ part, int nblocks, DevOut *out)
+// Per-block energy/virial partials of the pair kernel summed in a fixed
+// order, in two levels: RS_RED blocks of 256 threads each reduce a fixed
+// slice of the partials into one record (k_reduce_rs), then one block sums
+// those (k_reduce_rs2).  The result does not depend on timing.
+constexpr int RS_RED = 64;
+
+__device__ __forceinline__ void tree7(double (*sh)[256], int t)
 {
-   __shared__ double sh[7][256];
-   const int t = threadIdx.x;
-   double s[7] = {0, 0, 0, 0, 0, 0, 0};
-   for (int b = t; b < nblocks; b += 256)
-      for (int k = 0; k < 7; k++) s[k] += part[b * 8 + k];
-   for (int k = 0; k < 7; k++) sh[k][t] = s[k];
    __syncthreads();
    for (int w = 128; w > 0; w >>= 1) {
       if (t < w)
          for (int k = 0; k < 7; k++) sh[k][t] += sh[k][t + w];
       __syncthreads();
    }
+}
+
+__global__ void __launch_bounds__(256) k_reduce_rs(const double *__restrict__ part, int nblocks,
+                                                   double *__restrict__ part2)
+{
+   __shared__ double sh[7][256];
+   const int t = threadIdx.x;
+   const int per = (nblocks + gridDim.x - 1) / gridDim.x;
+   const int b0 = blockIdx.x * per, b1 = min(nblocks, b0 + per);
+   double s[7] = {0, 0, 0, 0, 0, 0, 0};
+   for (int b = b0 + t; b < b1; b += 256)
+      for (int k = 0; k < 7; k++) s[k] += part[b * 8 + k];
+   for (int k = 0; k < 7; k++) sh[k][t] = s[k];
+   tree7(sh, t);
+   if (t < 7) part2[blockIdx.x * 8 + t] = sh[t][0];
+}
+
+__global__ void __launch_bounds__(256) k_reduce_rs2(const double *__restrict__ part2, int n, DevOut *out)
+{
+   __shared__ double sh[7][256];
+   const int t = threadIdx.x;
+   for (int k = 0; k < 7; k++) sh[k][t] = t < n ? part2[t * 8 + k] : 0.0;
+   tree7(sh, t);
    if (t == 0) {
       out->pe_rs = sh[0][0];
       for (int k = 0; k < 6; k++) out->vir_rs[k] = sh[k + 1][0];
@@ -1247,9 +1267,11 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
    CK(e);
    c->launches += 1;
    if (mode == 0) {
-      k_reduce_rs<<<1, 256, 0, st>>>(d.part.p, (N + PAIR_WARPS - 1) / PAIR_WARPS, out);
+      CK(d.part2.ensure(8 * RS_RED));
+      k_reduce_rs<<<RS_RED, 256, 0, st>>>(d.part.p, (N + PAIR_WARPS - 1) / PAIR_WARPS, d.part2.p);
+      k_reduce_rs2<<<1, 256, 0, st>>>(d.part2.p, RS_RED, out);
       CK(cudaGetLastError());
-      c->launches += 1;
+      c->launches += 2;
    }
    phase_mark(c, MDGPU_PH_KPREP);
    return MDGPU_OK;
