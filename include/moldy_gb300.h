@@ -35,7 +35,8 @@ typedef enum {
                                 (src/force.c:126-135)                            */
    MDGPU_E_PTYPE = 6,        /* unknown potential type (UNKPTY, src/kernel.c:183)*/
    MDGPU_E_CAPACITY = 7,     /* an output buffer or internal limit is too small  */
-   MDGPU_E_NOMEM = 8         /* device allocation failed                         */
+   MDGPU_E_NOMEM = 8,        /* device allocation failed                         */
+   MDGPU_E_IO = 9            /* a dump file could not be opened or written       */
 } mdgpu_status;
 
 typedef enum {
@@ -287,9 +288,78 @@ mdgpu_status mdgpu_md_run(mdgpu_ctx *ctx, int nsteps, double *energies);
 mdgpu_status mdgpu_md_get_state(mdgpu_ctx *ctx, double *c_of_m, double *mom, double *quat,
                                 double *amom);
 
-/* Measures the device's dense FMA throughput (TFLOP/s, FMA = 2 flops) in
- * FP32 (fp64 = 0) or FP64: the roofline denominators of the force kernels,
- * whose bound is the FMA pipe.  No counterpart in the reference. */
+/* ---- Dump records (the periodic dump of do_step, src/accel.c:811-820,
+ * and its conversion, dump_convert, src/dump.c:550-620).  A record is
+ * FP32 and its contents follow the bits of dump_level:
+ *   bit 0: Cartesian centres of mass h s [nmols][3], quaternions
+ *          [nmols_r][4], h [3][3], thermostat variable ts (1 here), total
+ *          potential energy pe[0] + pe[1];
+ *   bit 1: centre-of-mass velocities [nmols][3], principal angular
+ *          velocities [nmols_r][3], h momentum [3][3] and thermostat
+ *          momentum (both 0 here);
+ *   bit 3: molecular forces [nmols][3], principal-frame torques
+ *          [nmols_r][3], the virial stress [3][3] of eval_forces (site
+ *          virial, molecular correction, distant-pressure term).
+ * Size in floats: mdgpu_dump_size (DUMP_SIZE, src/defs.h:294-297). */
+int mdgpu_dump_size(int dump_level, int nmols, int nmols_r);
+
+/* Advances nsteps steps as mdgpu_md_run and, after step k (1-based) with
+ * k >= first and (k - first) % interval == 0, converts the state into the
+ * next record of records ([nrec][mdgpu_dump_size] floats, caller-owned,
+ * nrec the number of such steps).  The conversion runs on the device; the
+ * records are copied back in batches. */
+mdgpu_status mdgpu_md_run_dump(mdgpu_ctx *ctx, int nsteps, int first, int interval, int dump_level,
+                               double *energies, float *records);
+
+/* ---- Dump files (src/dump.c).  A sequence of files named from a template
+ * holding a printf integer conversion (the file number; "%d" is appended
+ * when there is none), each a header (dump_mt), the system description
+ * (dump_sysinfo_mt with one mol_mt per species) and up to maxdumps records;
+ * the header's record count is rewritten after every record, as dump()
+ * does.  Native files are the struct images of an LP64 build of the
+ * reference; XDR files are its big-endian XDR encoding (src/xdr.c:150-183),
+ * with "(XDR)" after the version.  A file that exists already is not
+ * overwritten (MDGPU_E_IO): the reference would try other names. */
+typedef struct {                /* mol_mt, src/structs.h:220-230              */
+   float inertia[3];
+   float mass;
+   float dipole;                /* |sum of q p| over the principal-frame sites */
+   float charge;                /* molecular charge                           */
+   int nmols, rdof, framework;
+   char name[32];
+} mdgpu_dump_species;
+
+typedef struct {
+   const char *title;           /* run title (up to 127 characters)           */
+   long istep;                  /* step of the first record                   */
+   long dump_interval;
+   int dump_level;
+   int maxdumps;                /* records per file                           */
+   float deltat;                /* timestep * dump_interval                   */
+   int nmols, nmols_r, nspecies;
+   const mdgpu_dump_species *species;   /* [nspecies]                        */
+   int xdr;                     /* 1: XDR encoding                            */
+   unsigned long dump_init;     /* sequence stamp (0: the current time)       */
+   unsigned long restart_timestamp;
+} mdgpu_dump_info;
+
+typedef struct mdgpu_dumpfile mdgpu_dumpfile;
+
+/* Opens a sequence; *df is set even on failure (for mdgpu_dump_errmsg)
+ * unless out of memory. */
+mdgpu_status mdgpu_dump_open(mdgpu_dumpfile **df, const char *name_template, const mdgpu_dump_info *info);
+/* Appends one record (mdgpu_dump_size floats), starting the next file of
+ * the sequence when the current one holds maxdumps. */
+mdgpu_status mdgpu_dump_append(mdgpu_dumpfile *df, const float *record);
+/* Name of the file the last record went to. */
+const char *mdgpu_dump_filename(const mdgpu_dumpfile *df);
+const char *mdgpu_dump_errmsg(const mdgpu_dumpfile *df);
+void mdgpu_dump_close(mdgpu_dumpfile *df);
+
+/* Measures the device's dense FMA throughput (TFLOP/s, FMA = 2 flops):
+ * mode 0 scalar FP32 (FFMA), 1 FP64 (DFMA), 2 FP32 as paired (f32x2)
+ * instructions.  The roofline denominators of the force kernels, whose
+ * bound is the FMA pipe.  No counterpart in the reference. */
 mdgpu_status mdgpu_fma_peak(int device, int fp64, double *tflops);
 
 /* Potential at one distance (poteval, src/force.c:632-650): reference-site

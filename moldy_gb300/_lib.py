@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "libmoldy_gb300.so")
 
 STATUS = {0: "MDGPU_OK", 1: "MDGPU_E_ARG", 2: "MDGPU_E_CUDA", 3: "MDGPU_E_UNSUPPORTED",
           4: "MDGPU_E_CUTOFF", 5: "MDGPU_E_RANGE", 6: "MDGPU_E_PTYPE", 7: "MDGPU_E_CAPACITY",
-          8: "MDGPU_E_NOMEM"}
+          8: "MDGPU_E_NOMEM", 9: "MDGPU_E_IO"}
 FP64, MIXED = 0, 1
 
 #: every function include/*.h declares, with the library that must export it
@@ -24,7 +24,8 @@ EXPORTS = ["mdgpu_create", "mdgpu_destroy", "mdgpu_last_error", "mdgpu_set_preci
            "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak",
            "mdgpu_ewald_kspace_noalloc", "mdgpu_set_params", "mdgpu_energy_grad",
            "mdgpu_fm_loss_grad", "mdgpu_md_init", "mdgpu_md_run", "mdgpu_md_get_state",
-           "mdgpu_rdf_counts",
+           "mdgpu_rdf_counts", "mdgpu_dump_size", "mdgpu_md_run_dump", "mdgpu_dump_open",
+           "mdgpu_dump_append", "mdgpu_dump_filename", "mdgpu_dump_errmsg", "mdgpu_dump_close",
            "force_calc", "ewald", "poteval"]
 
 
@@ -68,6 +69,21 @@ class Grad(C.Structure):
 class Dynamics(C.Structure):
     _fields_ = [("mass", C.POINTER(C.c_double)), ("inertia", C.POINTER(C.c_double)),
                 ("rdof", C.POINTER(C.c_int)), ("step", C.c_double), ("nosymmetric_rot", C.c_int)]
+
+
+class DumpSpecies(C.Structure):
+    """mol_mt of the reference's dump header (src/structs.h:220-230)."""
+    _fields_ = [("inertia", C.c_float * 3), ("mass", C.c_float), ("dipole", C.c_float),
+                ("charge", C.c_float), ("nmols", C.c_int), ("rdof", C.c_int), ("framework", C.c_int),
+                ("name", C.c_char * 32)]
+
+
+class DumpInfo(C.Structure):
+    _fields_ = [("title", C.c_char_p), ("istep", C.c_long), ("dump_interval", C.c_long),
+                ("dump_level", C.c_int), ("maxdumps", C.c_int), ("deltat", C.c_float),
+                ("nmols", C.c_int), ("nmols_r", C.c_int), ("nspecies", C.c_int),
+                ("species", C.POINTER(DumpSpecies)), ("xdr", C.c_int), ("dump_init", C.c_ulong),
+                ("restart_timestamp", C.c_ulong)]
 
 
 NPOTP = 8
@@ -116,6 +132,13 @@ def load():
         "mdgpu_md_init": ([vp, C.POINTER(Dynamics), dp, dp, dp, dp, dp], ip),
         "mdgpu_md_run": ([vp, ip, dp], ip),
         "mdgpu_md_get_state": ([vp, dp, dp, dp, dp], ip),
+        "mdgpu_dump_size": ([ip, ip, ip], ip),
+        "mdgpu_md_run_dump": ([vp, ip, ip, ip, ip, dp, C.POINTER(C.c_float)], ip),
+        "mdgpu_dump_open": ([C.POINTER(vp), C.c_char_p, C.POINTER(DumpInfo)], ip),
+        "mdgpu_dump_append": ([vp, C.POINTER(C.c_float)], ip),
+        "mdgpu_dump_filename": ([vp], C.c_char_p),
+        "mdgpu_dump_errmsg": ([vp], C.c_char_p),
+        "mdgpu_dump_close": ([vp], None),
         "mdgpu_rdf_counts": ([vp, dp, dp, dp, C.c_double, ip, C.POINTER(C.c_uint64)], ip),
         "mdgpu_energy_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.POINTER(Grad)], ip),
         "mdgpu_fm_loss_grad": ([vp, C.POINTER(Params), dp, dp, dp, dp, C.c_double, dp, C.POINTER(Grad)], ip),

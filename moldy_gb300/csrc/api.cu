@@ -296,6 +296,7 @@ void mdgpu_destroy(mdgpu_ctx *c)
    m.cofm.release(); m.mom.release(); m.quat.release(); m.amom.release(); m.counter.release();
    m.mol_spec.release(); m.mol_q.release(); m.mol_site0.release(); m.site_mol.release(); m.site_pf.release();
    m.pf.release(); m.spec.release(); m.kpart.release(); m.energies.release(); m.err.release();
+   m.molf.release(); m.molt.release(); m.vpart.release(); m.virc.release(); m.rec.release();
    if (c->h_out) cudaFreeHost(c->h_out);
    for (auto &e : c->ev)
       if (e) cudaEventDestroy(e);

@@ -595,7 +595,7 @@ static double dist_pot(const double *p, double rc, int ptype)
    }
 }
 
-double distant_const(const mdgpu_ctx *c)
+static double distant_impl(const mdgpu_ctx *c, bool pressure)
 {
    const int M = c->max_id;
    std::vector<long long> count(M, 0);
@@ -604,12 +604,20 @@ double distant_const(const mdgpu_ctx *c)
       for (int k = 0; k < sp.nsites; k++) count[c->spec_ids[so + k]] += sp.nmols;
       so += sp.nsites;
    }
+   const double rc = c->ctl.cutoff;
    double cst = 0.0;
    for (int id = 1; id < M; id++)
-      for (int jd = 1; jd < M; jd++)
-         cst -= 2 * PI * (double)count[id] * (double)count[jd] *
-                dist_pot(c->potpar.data() + ((size_t)id + (size_t)M * jd) * NPOTP, c->ctl.cutoff, c->ptype);
+      for (int jd = 1; jd < M; jd++) {
+         const double *p = c->potpar.data() + ((size_t)id + (size_t)M * jd) * NPOTP;
+         cst -= 2 * PI * (double)count[id] * (double)count[jd] * dist_pot(p, rc, c->ptype);
+         if (pressure)
+            cst += 2.0 / 3.0 * PI * (double)count[id] * (double)count[jd] * (rc * rc * rc) *
+                   host_poteval(p, rc, c->ptype, 0.0, c->ctl.alpha);
+      }
    return cst;
 }
+
+double distant_const(const mdgpu_ctx *c) { return distant_impl(c, false); }
+double distant_pconst(const mdgpu_ctx *c) { return distant_impl(c, true); }
 
 }  // namespace mdgpu

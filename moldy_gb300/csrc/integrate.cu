@@ -22,6 +22,7 @@
 //   k_md_drift   second half-step of the co-ordinates.
 // Matrix-vector products and axpy updates keep the reference's operation
 // order without fused multiply-adds (src/matrix.c mat_vec_mul, mvaxpy).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -210,7 +211,8 @@ __global__ void __launch_bounds__(256)
 k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict__ mol_spec,
           const int *__restrict__ mol_q, const int *__restrict__ mol_site0, const double *__restrict__ pf,
           const double *__restrict__ force, const double *__restrict__ quat, double *__restrict__ mom,
-          double *__restrict__ amom, double *__restrict__ kpart)
+          double *__restrict__ amom, double *__restrict__ kpart, double *__restrict__ molf,
+          double *__restrict__ molt)
 {
    __shared__ double sh[2][256];
    const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -239,7 +241,9 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
             }
             T[i] = t;
          }
+         for (int k = 0; k < 3; k++) molt[3 * (size_t)qi + k] = T[k];
       }
+      for (int k = 0; k < 3; k++) molf[3 * (size_t)m + k] = F[k];
       const double *a = P.kick;
       double *pm = mom + 3 * (size_t)m;
       double x[3] = {pm[0], pm[1], pm[2]};
@@ -330,6 +334,155 @@ k_md_record(int *__restrict__ counter, int cap, const double *__restrict__ pe, c
 }
 
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+
+// ------------------------------------------------------------ dump records
+// Sum over sites of f (x) d, d = R(q) p the site's offset from its centre of
+// mass: the site-to-molecular virial correction of eval_forces
+// (src/accel.c:576-601), sum f.r - sum F.R over sites and molecules, which is
+// this sum.  Block partials [9], then one block sums them in fixed order.
+__global__ void __launch_bounds__(256)
+k_md_virc(MdStepParams P, const int *__restrict__ site_mol, const int *__restrict__ site_pf,
+          const double *__restrict__ pf, const int *__restrict__ mol_q, const double *__restrict__ quat,
+          const double *__restrict__ force, double *__restrict__ part)
+{
+   __shared__ double sh[9][256];
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const int N = P.nsites, t = threadIdx.x;
+   double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+   if (i < N) {
+      const int m = site_mol[i];
+      const double *p = pf + 3 * (size_t)site_pf[i];
+      const int qi = mol_q[m];
+      double d[3] = {p[0], p[1], p[2]};
+      if (qi >= 0) {
+         double R[9];
+         q_to_rot(quat + 4 * (size_t)qi, R);
+         matvec(R, p[0], p[1], p[2], d);
+      }
+      const double f[3] = {force[i], force[(size_t)N + i], force[2 * (size_t)N + i]};
+      for (int a = 0; a < 3; a++)
+         for (int b = 0; b < 3; b++) v[3 * a + b] = f[a] * d[b];
+   }
+   for (int k = 0; k < 9; k++) sh[k][t] = v[k];
+   __syncthreads();
+   for (int w = 128; w > 0; w >>= 1) {
+      if (t < w)
+         for (int k = 0; k < 9; k++) sh[k][t] += sh[k][t + w];
+      __syncthreads();
+   }
+   if (t < 9) part[9 * (size_t)blockIdx.x + t] = sh[t][0];
+}
+
+__global__ void __launch_bounds__(256) k_md_virc2(const double *__restrict__ part, int nb, double *__restrict__ virc)
+{
+   __shared__ double sh[9][256];
+   const int t = threadIdx.x;
+   double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+   for (int b = t; b < nb; b += 256)
+      for (int k = 0; k < 9; k++) v[k] += part[9 * (size_t)b + k];
+   for (int k = 0; k < 9; k++) sh[k][t] = v[k];
+   __syncthreads();
+   for (int w = 128; w > 0; w >>= 1) {
+      if (t < w)
+         for (int k = 0; k < 9; k++) sh[k][t] += sh[k][t + w];
+      __syncthreads();
+   }
+   if (t < 9) virc[t] = sh[t][0];
+}
+
+// Offsets of the parts of a record (-1: absent), in dump_convert's order.
+struct DumpLayout {
+   int pos, quat, h, vel, avel, hmom, frc, trq, st;
+};
+
+static int dump_layout(int level, int n, int nr, DumpLayout &L)
+{
+   int o = 0;
+   L = DumpLayout{-1, -1, -1, -1, -1, -1, -1, -1, -1};
+   if (level & 1) {
+      L.pos = o;
+      L.quat = o + 3 * n;
+      L.h = L.quat + 4 * nr;   // then ts, pe
+      o = L.h + 11;
+   }
+   if (level & 2) {
+      L.vel = o;
+      L.avel = o + 3 * n;
+      L.hmom = L.avel + 3 * nr;   // then tsmom
+      o = L.hmom + 10;
+   }
+   if (level & 8) {
+      L.frc = o;
+      L.trq = o + 3 * n;
+      L.st = L.trq + 3 * nr;
+      o = L.st + 9;
+   }
+   return o;
+}
+
+// One thread per molecule: the state after the step converted as
+// dump_convert does (src/dump.c:550-620): h s, quaternions; velocities
+// h^-T mom / m (ts = 1, zero h momentum); principal angular velocities
+// amom / I; molecular forces and torques.  Thread 0 adds h, ts, the total
+// potential energy, the zero h and thermostat momenta, and the stress.
+__global__ void k_md_dump(MdStepParams P, DumpLayout L, const MdSpec *__restrict__ spec,
+                          const int *__restrict__ mol_spec, const int *__restrict__ mol_q,
+                          const double *__restrict__ cofm, const double *__restrict__ mom,
+                          const double *__restrict__ quat, const double *__restrict__ amom,
+                          const double *__restrict__ molf, const double *__restrict__ molt,
+                          const double *__restrict__ small, const double *__restrict__ virc, double dist_v,
+                          double distp_v, float *__restrict__ rec)
+{
+   const int m = blockIdx.x * blockDim.x + threadIdx.x;
+   if (m == 0) {
+      if (L.h >= 0) {
+         for (int k = 0; k < 9; k++) rec[L.h + k] = (float)P.h[k];
+         rec[L.h + 9] = 1.0f;
+         rec[L.h + 10] = (float)(DA(DA(small[0], dist_v), small[1]));
+      }
+      if (L.hmom >= 0)
+         for (int k = 0; k < 10; k++) rec[L.hmom + k] = 0.0f;
+      if (L.st >= 0) {
+         // force_calc and ewald fill the upper triangle; eval_forces mirrors
+         // it, subtracts the molecular correction and adds the distant
+         // pressure term on the diagonal
+         double S[9];
+         for (int k = 0; k < 9; k++) S[k] = small[2 + k];
+         for (int i = 0; i < 3; i++)
+            for (int j = i + 1; j < 3; j++) S[3 * j + i] = S[3 * i + j];
+         for (int k = 0; k < 9; k++) S[k] = DS(S[k], virc[k]);
+         for (int i = 0; i < 3; i++) S[4 * i] = DA(S[4 * i], distp_v);
+         for (int k = 0; k < 9; k++) rec[L.st + k] = (float)S[k];
+      }
+   }
+   if (m >= P.nmols) return;
+   const MdSpec &S = spec[mol_spec[m]];
+   const int qi = mol_q[m];
+   const double *s = cofm + 3 * (size_t)m;
+   if (L.pos >= 0) {
+      double r[3];
+      matvec(P.h, s[0], s[1], s[2], r);
+      for (int k = 0; k < 3; k++) rec[L.pos + 3 * m + k] = (float)r[k];
+      if (qi >= 0)
+         for (int k = 0; k < 4; k++) rec[L.quat + 4 * qi + k] = (float)quat[4 * (size_t)qi + k];
+   }
+   if (L.vel >= 0) {
+      const double *x = mom + 3 * (size_t)m, *hi = P.hinv;
+      const double rm = 1.0 / S.mass;
+      for (int i = 0; i < 3; i++) {
+         const double v = DA(DA(DM(hi[i], x[0]), DM(hi[3 + i], x[1])), DM(hi[6 + i], x[2]));
+         rec[L.vel + 3 * m + i] = (float)DA(DM(v, rm), 0.0);
+      }
+      if (qi >= 0)
+         for (int i = 0; i < 3; i++)
+            rec[L.avel + 3 * qi + i] = (float)DM(amom[4 * (size_t)qi + i + 1], S.rinertia[i]);
+   }
+   if (L.frc >= 0) {
+      for (int k = 0; k < 3; k++) rec[L.frc + 3 * m + k] = (float)molf[3 * (size_t)m + k];
+      if (qi >= 0)
+         for (int k = 0; k < 3; k++) rec[L.trq + 3 * qi + k] = (float)molt[3 * (size_t)qi + k];
+   }
+}
 
 static void step_params(const mdgpu_ctx *c, MdStepParams &P)
 {
@@ -426,6 +579,7 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    if (nq > 0 && (!quat || !amom)) return fail(c, MDGPU_E_ARG, "rotating species need quaternions and angular momenta");
    H.nmols_r = nq;
    H.dist = distant_const(c);
+   H.distp = distant_pconst(c);
    if (H.graph) {
       cudaGraphExecDestroy(H.graph);
       H.graph = nullptr;
@@ -445,6 +599,8 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    CK(D.pf.ensure(c->spec_pf.size()));
    CK(D.spec.ensure(nsp));
    CK(D.kpart.ensure(2 * (size_t)((c->nmols + 255) / 256)));
+   CK(D.molf.ensure(3 * (size_t)c->nmols));
+   CK(D.molt.ensure(3 * (size_t)nq + 3));
    CK(D.err.ensure(1));
    CK(D.counter.ensure(1));
    CK(cudaMemcpyAsync(D.cofm.p, c_of_m, 3 * (size_t)c->nmols * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -467,7 +623,8 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
 }
 
 // Enqueues one step on the context's stream.
-static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap, double dist_v)
+static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap, double dist_v,
+                                    bool virc = false)
 {
    const MdHost &H = c->mdh;
    MdDev &D = c->md;
@@ -481,8 +638,17 @@ static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap
    c->launches += 2;
    mdgpu_status s = mdgpu_forces_device(c, H.h, c->site.p, D.cofm.p, c->force.p, c->small.p, c->small.p + 2);
    if (s) return s;
+   if (virc) {
+      // molecular correction of the virial, with the quaternions of this
+      // force evaluation (the drift after the kick moves them)
+      const int nbs = (N + 255) / 256;
+      k_md_virc<<<nbs, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.quat.p, c->force.p,
+                                     D.vpart.p);
+      k_md_virc2<<<1, 256, 0, st>>>(D.vpart.p, nbs, D.virc.p);
+      c->launches += 2;
+   }
    k_md_kick<<<nbm, 256, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.mol_site0.p, D.pf.p, c->force.p,
-                                  D.quat.p, D.mom.p, D.amom.p, D.kpart.p);
+                                  D.quat.p, D.mom.p, D.amom.p, D.kpart.p, D.molf.p, D.molt.p);
    k_md_record<<<1, 128, 0, st>>>(D.counter.p, cap, c->small.p, D.kpart.p, nbm, dist_v, c->out.p, D.energies.p,
                                  D.err.p);
    k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
@@ -522,13 +688,23 @@ static mdgpu_status md_capture(mdgpu_ctx *c, const MdStepParams &P, int cap, dou
    return MDGPU_OK;
 }
 
-extern "C" mdgpu_status mdgpu_md_run(mdgpu_ctx *c, int nsteps, double *energies)
+// nsteps steps; with records, a dump record after step k (1-based) when
+// k >= first and (k - first) % interval == 0, converted on the device into a
+// batch buffer that is copied back whenever it fills.
+static mdgpu_status md_run_impl(mdgpu_ctx *c, int nsteps, double *energies, int first, int interval,
+                                int level, float *records)
 {
    if (!c || nsteps < 0) return fail(c, MDGPU_E_ARG, "invalid argument");
    if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
    MdHost &H = c->mdh;
    MdDev &D = c->md;
    cudaStream_t st = c->stream;
+   DumpLayout DL;
+   const int dsize = records ? dump_layout(level, c->nmols, H.nmols_r, DL) : 0;
+   if (records) {
+      if (first < 1 || interval < 1) return fail(c, MDGPU_E_ARG, "dump steps need first >= 1 and interval >= 1");
+      if (dsize == 0) return fail(c, MDGPU_E_ARG, "dump level selects nothing (bits 0, 1, 3)");
+   }
    mdgpu_status s = ensure_ready(c, H.h, true, true);
    if (s) return s;
    MdStepParams P;
@@ -540,12 +716,29 @@ extern "C" mdgpu_status mdgpu_md_run(mdgpu_ctx *c, int nsteps, double *energies)
       H.graph_gen = 0;
    }
    CK(c->small.ensure(16));
+   const int nrec = records && nsteps >= first ? (nsteps - first) / interval + 1 : 0;
+   int batch = 0;
+   if (nrec > 0) {
+      // device batch of records: up to 256 MiB
+      batch = (int)std::min<size_t>((size_t)nrec, std::max<size_t>(1, ((size_t)64 << 20) / (size_t)dsize));
+      CK(D.rec.ensure((size_t)batch * dsize));
+      if (level & 8) {
+         CK(D.vpart.ensure(9 * (size_t)((c->nsites + 255) / 256)));
+         CK(D.virc.ensure(9));
+      }
+   }
    CK(cudaMemsetAsync(D.counter.p, 0, sizeof(int), st));
-   const double dist_v = H.dist / det3(H.h);
+   const double vol = det3(H.h);
+   const double dist_v = H.dist / vol, distp_v = H.distp / vol;
+   int r = 0, r_done = 0;
    for (int i = 0; i < nsteps; i++) {
+      const int k = i + 1;
+      const bool dump = nrec > 0 && k >= first && (k - first) % interval == 0;
       // the first step runs directly; later ones replay a captured step
-      // unless the configuration changed since it was captured
-      const bool replay = i > 0 && !c->timing;
+      // unless the configuration changed since it was captured (a step
+      // whose record needs the virial correction also runs directly)
+      const bool virc = dump && (level & 8);
+      const bool replay = i > 0 && !c->timing && !virc;
       if (replay && (!H.graph || H.graph_gen != c->gen || H.graph_cap != cap)) {
          if ((s = md_capture(c, P, cap, dist_v)) != MDGPU_OK) return s;
          H.graph_cap = cap;
@@ -553,8 +746,25 @@ extern "C" mdgpu_status mdgpu_md_run(mdgpu_ctx *c, int nsteps, double *energies)
       if (replay) {
          CK(cudaGraphLaunch(H.graph, st));
          c->launches += H.graph_launches;
-      } else if ((s = md_enqueue_step(c, P, cap, dist_v)) != MDGPU_OK) {
+      } else if ((s = md_enqueue_step(c, P, cap, dist_v, virc)) != MDGPU_OK) {
          return s;
+      }
+      if (dump) {
+         const int M = c->nmols;
+         k_md_dump<<<(M + 127) / 128, 128, 0, st>>>(P, DL, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p,
+                                                    D.quat.p, D.amom.p, D.molf.p, D.molt.p, c->small.p,
+                                                    D.virc.p, dist_v, distp_v,
+                                                    D.rec.p + (size_t)(r % batch) * dsize);
+         CK(cudaGetLastError());
+         c->launches += 1;
+         r++;
+         if (r % batch == 0 || r == nrec) {
+            const int nb = r - r_done;
+            CK(cudaMemcpyAsync(records + (size_t)r_done * dsize, D.rec.p, (size_t)nb * dsize * sizeof(float),
+                               cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            r_done = r;
+         }
       }
    }
    int err = 0;
@@ -565,6 +775,25 @@ extern "C" mdgpu_status mdgpu_md_run(mdgpu_ctx *c, int nsteps, double *energies)
    if (err & 1) return fail(c, MDGPU_E_RANGE, "Co-ordinate out of range in BIN (fill_cells)");
    if (err & 2) return fail(c, MDGPU_E_RANGE, "quaternion normalisation error (QNORM2)");
    return MDGPU_OK;
+}
+
+extern "C" mdgpu_status mdgpu_md_run(mdgpu_ctx *c, int nsteps, double *energies)
+{
+   return md_run_impl(c, nsteps, energies, 0, 0, 0, nullptr);
+}
+
+extern "C" mdgpu_status mdgpu_md_run_dump(mdgpu_ctx *c, int nsteps, int first, int interval, int dump_level,
+                                          double *energies, float *records)
+{
+   if (!records) return fail(c, MDGPU_E_ARG, "NULL records");
+   return md_run_impl(c, nsteps, energies, first, interval, dump_level, records);
+}
+
+// DUMP_SIZE, src/defs.h:294-297
+extern "C" int mdgpu_dump_size(int level, int nmols, int nmols_r)
+{
+   DumpLayout L;
+   return dump_layout(level, nmols, nmols_r, L);
 }
 
 extern "C" mdgpu_status mdgpu_md_get_state(mdgpu_ctx *c, double *c_of_m, double *mom, double *quat,

@@ -70,6 +70,8 @@ void ewald_self_sheet_grad(const std::vector<mdgpu_species> &spec, const std::ve
 // Constant of the distant-potential correction (distant_const,
 // src/accel.c:293-328 with dist_pot, src/kernel.c:103-150): energy x volume.
 double distant_const(const mdgpu_ctx *c);
+// The pressure form (iflag 1 of the same function, src/accel.c:316-320).
+double distant_pconst(const mdgpu_ctx *c);
 double det3(const double *a);
 void inv3(const double *a, double *b);
 
@@ -192,6 +194,7 @@ struct MdHost {
    double h[9];
    double half = 0;                  // dt / 2
    double dist = 0;                  // distant-potential constant (energy x volume)
+   double distp = 0;                 // distant-pressure constant (stress x volume)
    int nosym = 0, saxis = 0, nmols_r = 0;
    // one captured step (CUDA graph), replayed by mdgpu_md_run
    cudaGraphExec_t graph = nullptr;
@@ -208,6 +211,9 @@ struct MdDev {
    DBuf<MdSpec> spec;
    DBuf<double> kpart, energies;
    DBuf<int> err;
+   DBuf<double> molf, molt;              // molecular forces, principal torques
+   DBuf<double> vpart, virc;             // virial correction (dump records)
+   DBuf<float> rec;                      // batch of dump records
 };
 
 }  // namespace mdgpu

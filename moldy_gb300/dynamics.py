@@ -130,6 +130,19 @@ class MolecularDynamics:
         self.ff._check(self.L.mdgpu_md_run(self.ff.ctx, int(nsteps), _dp(e)))
         return e[:nsteps]
 
+    def run_dump(self, nsteps: int, interval: int, level: int, first: int = 1):
+        """Advance nsteps as run() and return (energies, records): a dump
+        record ([mdgpu_dump_size] float32, the layout of dump_convert,
+        src/dump.c:550-620) after step k when k >= first and
+        (k - first) % interval == 0, converted on the GPU."""
+        nrec = (nsteps - first) // interval + 1 if nsteps >= first else 0
+        size = self.L.mdgpu_dump_size(int(level), self.ff.sysm.nmols, self.nq)
+        rec = np.zeros((max(nrec, 1), max(size, 1)), np.float32)
+        e = np.zeros((max(nsteps, 1), 4))
+        self.ff._check(self.L.mdgpu_md_run_dump(self.ff.ctx, int(nsteps), int(first), int(interval), int(level),
+                                                _dp(e), rec.ctypes.data_as(C.POINTER(C.c_float))))
+        return e[:nsteps], rec[:nrec]
+
     def state(self) -> MDState:
         sysm = self.ff.sysm
         cm, mo = np.zeros((sysm.nmols, 3)), np.zeros((sysm.nmols, 3))

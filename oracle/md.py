@@ -39,9 +39,13 @@ def write_mdstate(path: str, sysm, dyn, state, nsteps: int) -> None:
             f.write(np.ascontiguousarray(a, "<f8").tobytes())
 
 
-def run(sysm, dyn, state, nsteps: int, fast: bool = False) -> Tuple[np.ndarray, object, float]:
+def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None):
     """(records [nsteps, 3] = (H_0, pe[0], pe[1]) per step, final MDState,
-    seconds per step).  The reference prints its notes to stdout."""
+    seconds per step).  The reference prints its notes to stdout.
+
+    dump = (name, level, interval, ndumps, title) has the reference write
+    its dump files (from step 1); they are returned as a fourth item,
+    {file name: bytes}."""
     from moldy_gb300.dynamics import MDState
     exe = os.path.join(REF, "moldy_ref_md_fast" if fast else "moldy_ref_md")
     if not os.path.exists(exe):
@@ -50,8 +54,15 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False) -> Tuple[np.ndarray, 
     with tempfile.TemporaryDirectory() as d:
         pin, pout = os.path.join(d, "in.mdstate"), os.path.join(d, "out.bin")
         write_mdstate(pin, sysm, dyn, state, nsteps)
-        subprocess.run([exe, pin, pout], check=True, cwd=d, stdout=subprocess.DEVNULL)
+        args = [exe, pin, pout] + ([str(x) for x in dump] if dump else [])
+        subprocess.run(args, check=True, cwd=d, stdout=subprocess.DEVNULL)
         raw = np.fromfile(pout, "<f8")
+        files = {}
+        if dump:
+            for fn in sorted(os.listdir(d)):
+                if fn not in ("in.mdstate", "out.bin"):
+                    with open(os.path.join(d, fn), "rb") as fh:
+                        files[fn] = fh.read()
     o = 3 * nsteps
     rec = raw[:o].reshape(nsteps, 3)
     cm = raw[o:o + 3 * nm].reshape(nm, 3)
@@ -62,4 +73,6 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False) -> Tuple[np.ndarray, 
     o += 4 * nq
     am = raw[o:o + 4 * nq].reshape(nq, 4)
     o += 4 * nq
+    if dump:
+        return rec, MDState(cm, mo, qu, am), float(raw[o]), files
     return rec, MDState(cm, mo, qu, am), float(raw[o])

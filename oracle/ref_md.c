@@ -7,7 +7,13 @@
  * potential-energy parts, then the final state.  The golden trajectories of
  * the GPU integrator's tests come from here.
  *
- * usage: moldy_ref_md in.mdstate out.bin
+ * usage: moldy_ref_md in.mdstate out.bin [dump-name level interval ndumps title]
+ *
+ * With the optional arguments the reference's own periodic dump (dump(),
+ * src/dump.c:278-499, called from do_step, src/accel.c:811-820) writes its
+ * files from step 1 (begin-dump 1) into the working directory; species are
+ * named spec0, spec1, ... and carry the molecular charge and dipole that
+ * the reference's start-up computes (src/startup.c:487-496, 571-580).
  *
  * in.mdstate (little-endian, written by oracle/md.py):
  *   "MDSTAT1\0"
@@ -25,6 +31,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <math.h>
 #include "defs.h"
 #include "structs.h"
 
@@ -56,7 +63,7 @@ int main(int argc, char **argv)
    vec_mt (*msq)[2];
    struct timespec t0, t1;
 
-   if (argc < 3) { fprintf(stderr, "usage: %s in.mdstate out.bin\n", argv[0]); return 2; }
+   if (argc < 3) { fprintf(stderr, "usage: %s in.mdstate out.bin [dump-name level interval ndumps title]\n", argv[0]); return 2; }
    f = fopen(argv[1], "rb");
    if (!f) { perror(argv[1]); return 2; }
    rd(magic, 1, 8, f);
@@ -133,6 +140,26 @@ int main(int argc, char **argv)
          iq += sp->nmols;
       }
       imol += sp->nmols;
+   }
+   if (argc >= 8) {
+      strncpy(control.dump_file, argv[3], L_name - 3);
+      control.dump_level = atoi(argv[4]);
+      control.dump_interval = atol(argv[5]);
+      control.maxdumps = atoi(argv[6]);
+      strncpy(control.title, argv[7], L_name - 1);
+      control.begin_dump = 1;
+      for (s = 0; s < sys.nspecies; s++) {
+         spec_mt *sp = species + s;
+         double dip[3] = {0.0, 0.0, 0.0};
+         int k;
+         sprintf(sp->name, "spec%d", s);
+         sp->charge = 0.0;
+         for (i = 0; i < sp->nsites; i++) {
+            sp->charge += site_info[sp->site_id[i]].charge;
+            for (k = 0; k < 3; k++) dip[k] += sp->p_f_sites[i][k] * site_info[sp->site_id[i]].charge;
+         }
+         sp->dipole = sp->rdof > 0 ? sqrt(dip[0] * dip[0] + dip[1] * dip[1] + dip[2] * dip[2]) : 0.0;
+      }
    }
    msq = (vec_mt(*)[2])calloc(sys.nspecies, sizeof(vec_mt[2]));
    o = fopen(argv[2], "wb");

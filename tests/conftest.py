@@ -16,10 +16,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
 def golden_files(prefix=""):
-    """Force-path fixtures (the md_* dynamics and rdf_* histogram fixtures
-    are named explicitly by their own tests)."""
+    """Force-path fixtures (the md_* dynamics, rdf_* histogram and dump_*
+    file fixtures are named explicitly by their own tests)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and f.startswith(prefix) and not f.startswith(("md_", "rdf_")))
+                  if f.endswith(".npz") and f.startswith(prefix) and not f.startswith(("md_", "rdf_", "dump_")))
 
 
 @pytest.fixture(scope="session")
