@@ -213,9 +213,10 @@ k_adj_site32(const int4 *__restrict__ item, const int *__restrict__ item_k0, con
    float zc[KI], zs[KI];
 #pragma unroll
    for (int t = 0; t < KI; t++) {
-      const float2 z = live ? zz[(size_t)i * KI + t] : make_float2(1.f, 0.f);
-      zc[t] = z.x;
-      zs[t] = z.y;
+      // the table holds a site's KI cosines, then its KI sines
+      const float *zf = reinterpret_cast<const float *>(zz) + (size_t)i * 2 * KI;
+      zc[t] = live ? zf[t] : 1.f;
+      zs[t] = live ? zf[KI + t] : 0.f;
    }
    float vx = 0.f, vy = 0.f, vz = 0.f;
    if (live && loss) {

@@ -253,12 +253,23 @@ mdgpu_status mdgpu_create(mdgpu_ctx **out, int device, mdgpu_precision precision
    }
    if (device < 0 || device >= n) return MDGPU_E_ARG;
    mdgpu_ctx *c = new mdgpu_ctx();
+   int lo_pri = 0, hi_pri = 0;
    c->device = device;
    c->prec = precision;
    if (cudaSetDevice(device) != cudaSuccess ||
        cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri) != cudaSuccess ||
+       cudaStreamCreateWithPriority(&c->side_stream, cudaStreamNonBlocking, hi_pri) != cudaSuccess ||
+       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&c->ev_pairs, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
        cudaMallocHost((void **)&c->h_out, sizeof(DevOut)) != cudaSuccess) {
       cudaGetLastError();
+      if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+      if (c->ev_pairs) cudaEventDestroy(c->ev_pairs);
+      if (c->ev_join) cudaEventDestroy(c->ev_join);
+      if (c->side_stream) cudaStreamDestroy(c->side_stream);
+      if (c->own_stream) cudaStreamDestroy(c->own_stream);
       delete c;
       return MDGPU_E_CUDA;
    }
@@ -300,6 +311,10 @@ void mdgpu_destroy(mdgpu_ctx *c)
    if (c->h_out) cudaFreeHost(c->h_out);
    for (auto &e : c->ev)
       if (e) cudaEventDestroy(e);
+   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+   if (c->ev_pairs) cudaEventDestroy(c->ev_pairs);
+   if (c->ev_join) cudaEventDestroy(c->ev_join);
+   if (c->side_stream) cudaStreamDestroy(c->side_stream);
    if (c->own_stream) cudaStreamDestroy(c->own_stream);
    delete c;
 }
@@ -449,10 +464,28 @@ mdgpu_status mdgpu_forces_device(mdgpu_ctx *c, const double *h, const double *d_
    if (s) return s;
    for (bool &m : c->ev_marked) m = false;
    CKR(cudaMemsetAsync(c->out.p, 0, sizeof(DevOut), c->stream));
-   s = rs_launch(c, d_site, d_cofm, d_force, false, nullptr, 0, nullptr);
-   if (s) return s;
    const bool ew = c->ctl.alpha > ALPHAMIN;
-   if (ew) {
+   // With Ewald, the k-space passes (FP32-pipe-bound) run on a second,
+   // high-priority stream beside the pair kernel (latency- and integer-bound),
+   // so their blocks fill the SMs as pair blocks retire; the k-space force
+   // sum waits for the pair kernel's forces.  Phase timing keeps the order.
+   const bool overlap = ew && !c->timing;
+   s = rs_launch(c, d_site, d_cofm, d_force, overlap, nullptr, 0, nullptr);
+   if (s) return s;
+   if (overlap) {
+      cudaStream_t main = c->stream;
+      CKR(cudaEventRecord(c->ev_fork, main));
+      CKR(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+      s = rs_pairs(c, d_force, nullptr, 0);
+      if (s) return s;
+      CKR(cudaEventRecord(c->ev_pairs, main));
+      c->stream = c->side_stream;
+      s = ks_launch(c, d_site, d_force, true, c->ev_pairs);
+      c->stream = main;
+      if (s) return s;
+      CKR(cudaEventRecord(c->ev_join, c->side_stream));
+      CKR(cudaStreamWaitEvent(main, c->ev_join, 0));
+   } else if (ew) {
       s = ks_launch(c, d_site, d_force, true);
       if (s) return s;
    } else {

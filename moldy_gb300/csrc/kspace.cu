@@ -75,11 +75,14 @@ __global__ void k_prep(int N, const int *__restrict__ sorted, const double *__re
       unsigned int uz32 = (unsigned int)((uz + 0x80000000ull) >> 32);
       ph32[i] = make_int4((int)ux32, (int)uy32, (int)uz32, __float_as_int((float)q));
       z32[i] = make_float2((float)cz, (float)sz);
-      // exp(2 pi i t s_z), t = 0..KI-1, each from its exact integer phase
+      // exp(2 pi i t s_z), t = 0..KI-1, each from its exact integer phase;
+      // the site's KI cosines, then its KI sines
+      float *zf = reinterpret_cast<float *>(zp32) + (size_t)i * 2 * KI;
       for (int t = 0; t < KI; t++) {
          float st, ct;
          sincos_rev32((unsigned int)t * uz32, &st, &ct);
-         zp32[(size_t)i * KI + t] = make_float2(ct, st);
+         zf[t] = ct;
+         zf[KI + t] = st;
       }
    } else {
       ph64a[i] = make_ulonglong2(ux, uy);
@@ -109,60 +112,56 @@ constexpr int SF_TILE = 128;     // sites per shared-memory tile (FP64 pass: hal
 // two roundings from its exact phase, so no error accumulates along l.  The
 // structure factor of a crystal is a near-cancelling sum, and its force
 // error grows with the per-site phase error.
+//
+// The accumulators of neighbouring k (t, t+1) run as the two lanes of paired
+// FP32 instructions: the table holds a site's KI cosines and then its KI
+// sines, so one 128-bit shared load gives the (t, t+1) and (t+2, t+3) pairs
+// with no repacking, and each lane rounds exactly as the scalar form
+// fmaf(c, zc, fmaf(-s, zs, acc)) does.
+static_assert(KI % 4 == 0, "the structure-factor pass takes k in fours");
+
 __global__ void __launch_bounds__(128)
 k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nitems,
          const int4 *__restrict__ ph, const float2 *__restrict__ zp, int N, int chunk, int nk,
          float2 *__restrict__ part)
 {
    __shared__ int4 sph[SF_TILE];
-   __shared__ float2 szp[SF_TILE * KI];
+   __shared__ __align__(16) float szp[SF_TILE * 2 * KI];
    const int it = blockIdx.x * blockDim.x + threadIdx.x;
    const int4 hd = it < nitems ? item[it] : make_int4(0, 0, 0, 0);
    const int s0 = blockIdx.y * chunk, s1 = min(N, s0 + chunk);
-   float ac[KI], as[KI];
+   f2x ac[KI / 2], as[KI / 2];   // (t, t+1) pairs of Re and Im S(k)
 #pragma unroll
-   for (int t = 0; t < KI; t++) ac[t] = as[t] = 0.f;
+   for (int j = 0; j < KI / 2; j++) ac[j] = as[j] = 0ull;
    const unsigned int H = (unsigned int)hd.x, K = (unsigned int)hd.y, L = (unsigned int)hd.z;
+   const float4 *zsrc = reinterpret_cast<const float4 *>(zp);
+   float4 *zdst = reinterpret_cast<float4 *>(szp);
    for (int tb = s0; tb < s1; tb += SF_TILE) {
       const int nt = min(SF_TILE, s1 - tb);
       __syncthreads();
       for (int q = threadIdx.x; q < nt; q += blockDim.x) sph[q] = ph[tb + q];
-      for (int q = threadIdx.x; q < nt * KI; q += blockDim.x) szp[q] = zp[(size_t)tb * KI + q];
+      for (int q = threadIdx.x; q < nt * (KI / 2); q += blockDim.x) zdst[q] = zsrc[(size_t)tb * (KI / 2) + q];
       __syncthreads();
-      if (hd.w == KI) {   // full items (grouped first in the list): no per-k predicate
-         for (int q = 0; q < nt; q++) {
-            const int4 v = sph[q];
-            const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
-            float sn, cs;
-            sincos_poly(p, &sn, &cs);
-            const float qv = __int_as_float(v.w);
-            cs *= qv;
-            sn *= qv;
-            const float2 *z = szp + q * KI;
+      const int nq4 = (hd.w + 3) >> 2;   // k quads of this item (uniform over a warp but at group edges)
+      for (int q = 0; q < nt; q++) {
+         const int4 v = sph[q];
+         const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
+         float sn, cs;
+         sincos_poly(p, &sn, &cs);
+         const float qv = __int_as_float(v.w);
+         cs *= qv;
+         sn *= qv;
+         const f2x c2 = pk2(cs, cs), s2 = pk2(sn, sn), ns2 = neg2(s2);
+         const ulonglong2 *zc = reinterpret_cast<const ulonglong2 *>(szp + q * 2 * KI);
+         const ulonglong2 *zs = zc + KI / 4;
 #pragma unroll
-            for (int t = 0; t < KI; t++) {
-               const float2 zt = z[t];
-               ac[t] = fmaf(cs, zt.x, fmaf(-sn, zt.y, ac[t]));
-               as[t] = fmaf(sn, zt.x, fmaf(cs, zt.y, as[t]));
-            }
-         }
-      } else {
-         for (int q = 0; q < nt; q++) {
-            const int4 v = sph[q];
-            const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
-            float sn, cs;
-            sincos_poly(p, &sn, &cs);
-            const float qv = __int_as_float(v.w);
-            cs *= qv;
-            sn *= qv;
-            const float2 *z = szp + q * KI;
-#pragma unroll
-            for (int t = 0; t < KI; t++) {
-               if (t < hd.w) {
-                  const float2 zt = z[t];
-                  ac[t] = fmaf(cs, zt.x, fmaf(-sn, zt.y, ac[t]));
-                  as[t] = fmaf(sn, zt.x, fmaf(cs, zt.y, as[t]));
-               }
+         for (int j = 0; j < KI / 4; j++) {
+            if (j < nq4) {
+               const ulonglong2 c = zc[j], sv = zs[j];
+               ac[2 * j] = fma2(c2, c.x, fma2(ns2, sv.x, ac[2 * j]));
+               as[2 * j] = fma2(s2, c.x, fma2(c2, sv.x, as[2 * j]));
+               ac[2 * j + 1] = fma2(c2, c.y, fma2(ns2, sv.y, ac[2 * j + 1]));
+               as[2 * j + 1] = fma2(s2, c.y, fma2(c2, sv.y, as[2 * j + 1]));
             }
          }
       }
@@ -171,8 +170,13 @@ k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nit
       const int k0 = item_k0[it];
       float2 *dst = part + (size_t)blockIdx.y * nk + k0;
 #pragma unroll
-      for (int t = 0; t < KI; t++)
-         if (t < hd.w) dst[t] = make_float2(ac[t], as[t]);
+      for (int j = 0; j < KI / 2; j++) {
+         float c0, c1, v0, v1;
+         upk2(ac[j], c0, c1);
+         upk2(as[j], v0, v1);
+         if (2 * j < hd.w) dst[2 * j] = make_float2(c0, v0);
+         if (2 * j + 1 < hd.w) dst[2 * j + 1] = make_float2(c1, v1);
+      }
    }
 }
 
@@ -354,10 +358,11 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    f2x zc[KI], zs[KI];
 #pragma unroll
    for (int t = 0; t < KI; t++) {
-      const float2 za = live0 ? zz[(size_t)i0 * KI + t] : make_float2(1.f, 0.f);
-      const float2 zb = live1 ? zz[(size_t)i1 * KI + t] : make_float2(1.f, 0.f);
-      zc[t] = pk2(za.x, zb.x);
-      zs[t] = pk2(za.y, zb.y);
+      // the table holds a site's KI cosines, then its KI sines
+      const float *za = reinterpret_cast<const float *>(zz) + (size_t)i0 * 2 * KI;
+      const float *zb = reinterpret_cast<const float *>(zz) + (size_t)i1 * 2 * KI;
+      zc[t] = pk2(live0 ? za[t] : 1.f, live1 ? zb[t] : 1.f);
+      zs[t] = pk2(live0 ? za[KI + t] : 0.f, live1 ? zb[KI + t] : 0.f);
    }
    const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
    // compensated (Kahan) FP32 sums, taken every 4 items of plain FP32
@@ -739,7 +744,7 @@ KsShape ks_shape(int N, int nitems, int ipt, int spt)
    return s;
 }
 
-mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate)
+mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate, cudaEvent_t join)
 {
    KsDev &d = c->kd;
    const KList &kl = c->kl;
@@ -748,6 +753,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    const bool mixed = c->prec == MDGPU_MIXED;
    DevOut *out = c->out.p;
    if (nk == 0) {
+      if (join) CK(cudaStreamWaitEvent(st, join, 0));
       if (!accumulate) CK(cudaMemsetAsync(d_force, 0, 3 * (size_t)N * sizeof(double), st));
       return MDGPU_OK;
    }
@@ -826,6 +832,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
                                     d.fpart.p);
    CK(cudaGetLastError());
    phase_mark(c, MDGPU_PH_FINAL);
+   if (join) CK(cudaStreamWaitEvent(st, join, 0));
    k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, sh.splits, d.fpart.p, d_force, accumulate ? 1 : 0);
    CK(cudaGetLastError());
    if (nf > 0) {

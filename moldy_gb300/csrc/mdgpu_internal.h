@@ -267,6 +267,10 @@ struct mdgpu_ctx {
    int64_t launches = 0;
    bool timing = false;
    cudaEvent_t ev[MDGPU_NPHASES + 1] = {};
+   // second (high-priority) stream: the k-space passes run on it beside
+   // the pair kernel
+   cudaStream_t side_stream = nullptr;
+   cudaEvent_t ev_fork = nullptr, ev_pairs = nullptr, ev_join = nullptr;
    bool ev_marked[MDGPU_NPHASES + 1] = {};
    bool have_nabor_note = false;
    // bumped by every call that changes what a captured step would launch
@@ -287,6 +291,9 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
 // into c->ad.gq ([2][N], written) and c->ad.slots; residual weights from
 // c->ad.res64/res32 when loss.
 mdgpu_status rs_adjoint(mdgpu_ctx *c, bool loss);
+// The pair kernel and its energy/virial reduction over the sites binned by
+// the last rs_launch, on c->stream (rs_launch without cells_only runs both).
+mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys, int64_t key_cap);
 int pot_nparams(int ptype);     // parameters the potential type reads
 // Site-pair distance histogram of the sites binned by the last rs_launch:
 // full-list counts [max_id][max_id][nbins] into c->rd.rdf_counts (zeroed
@@ -294,7 +301,10 @@ int pot_nparams(int ptype);     // parameters the potential type reads
 mdgpu_status rs_rdf(mdgpu_ctx *c, double limit, int nbins);
 // kspace.cu
 mdgpu_status ks_prepare(mdgpu_ctx *c);
-mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate);
+// join: an event the final force sum waits for (the pair kernel running on
+// another stream writes d_force first), or null.
+mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool accumulate,
+                       cudaEvent_t join = nullptr);
 struct KsShape {
    int chunks, chunk, splits, per_split;
 };

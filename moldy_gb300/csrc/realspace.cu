@@ -1249,6 +1249,19 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
    c->launches += 7;
    phase_mark(c, MDGPU_PH_PAIRS);
    if (cells_only) return MDGPU_OK;
+   return rs_pairs(c, d_force, d_keys, key_cap);
+#undef CK
+}
+
+mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys, int64_t key_cap)
+{
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+   RsDev &d = c->rd;
+   cudaStream_t st = c->stream;
+   RsParams P = make_params(c);
+   const int N = c->nsites;
+   DevOut *out = c->out.p;
+   const bool mixed = c->prec == MDGPU_MIXED && d_keys == nullptr;
    const size_t potb = (size_t)c->max_id * c->max_id * NPOTP * (mixed ? sizeof(float) : sizeof(double));
    P.pot_in_smem = potb <= 96 * 1024;
    const size_t smem = P.pot_in_smem ? potb : 0;
