@@ -679,7 +679,10 @@ static mdgpu_status md_capture(mdgpu_ctx *c, const MdStepParams &P, int cap, dou
       return s;
    }
    CK(e);
-   const cudaError_t ei = cudaGraphInstantiate(&H.graph, g, 0);
+   // the node priorities captured from the streams (the k-space passes run
+   // on a high-priority stream beside the pair kernel) only apply with
+   // this flag
+   const cudaError_t ei = cudaGraphInstantiateWithFlags(&H.graph, g, cudaGraphInstantiateFlagUseNodePriority);
    cudaGraphDestroy(g);
    CK(ei);
    H.graph_launches = c->launches - l0;
@@ -734,11 +737,12 @@ static mdgpu_status md_run_impl(mdgpu_ctx *c, int nsteps, double *energies, int 
    for (int i = 0; i < nsteps; i++) {
       const int k = i + 1;
       const bool dump = nrec > 0 && k >= first && (k - first) % interval == 0;
-      // the first step runs directly; later ones replay a captured step
-      // unless the configuration changed since it was captured (a step
-      // whose record needs the virial correction also runs directly)
+      // a step runs directly until one has run since the configuration last
+      // changed (every buffer is then allocated); later ones replay a
+      // captured step (a step whose record needs the virial correction also
+      // runs directly)
       const bool virc = dump && (level & 8);
-      const bool replay = i > 0 && !c->timing && !virc;
+      const bool replay = (i > 0 || H.warm_gen == c->gen) && !c->timing && !virc;
       if (replay && (!H.graph || H.graph_gen != c->gen || H.graph_cap != cap)) {
          if ((s = md_capture(c, P, cap, dist_v)) != MDGPU_OK) return s;
          H.graph_cap = cap;
@@ -746,8 +750,9 @@ static mdgpu_status md_run_impl(mdgpu_ctx *c, int nsteps, double *energies, int 
       if (replay) {
          CK(cudaGraphLaunch(H.graph, st));
          c->launches += H.graph_launches;
-      } else if ((s = md_enqueue_step(c, P, cap, dist_v, virc)) != MDGPU_OK) {
-         return s;
+      } else {
+         if ((s = md_enqueue_step(c, P, cap, dist_v, virc)) != MDGPU_OK) return s;
+         H.warm_gen = c->gen;
       }
       if (dump) {
          const int M = c->nmols;

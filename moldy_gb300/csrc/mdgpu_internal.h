@@ -201,6 +201,7 @@ struct MdHost {
    uint64_t graph_gen = 0;
    int64_t graph_launches = 0;       // kernels one replay launches
    int graph_cap = 0;                // record capacity it was captured with
+   uint64_t warm_gen = 0;            // configuration of the last direct step
 };
 
 struct MdDev {
