@@ -36,7 +36,7 @@ namespace mdgpu {
 
 // kernels of kspace.cu
 __global__ void k_sfac32(const int4 *item, const int *item_k0, int nitems, const int4 *ph, const float2 *zp,
-                         int N, int chunk, int nk, float2 *part);
+                         int N, int chunk, int nk, float2 *part, int *err);
 __global__ void k_sfac64(const int4 *item, const int *item_k0, int nitems, const ulonglong2 *pha,
                          const ulonglong2 *phb, const double2 *zz, int N, int chunk, int nk, double2 *part);
 __global__ void k_fsum(int n3, int nsplit, const double *fpart, double *force, int accumulate);
@@ -393,7 +393,7 @@ static mdgpu_status ks_adjoint(mdgpu_ctx *c, bool loss)
       for (int ch = 0; ch < 3; ch++) {
          if (mixed)
             k_sfac32<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, a.phv32.p + (size_t)ch * N, d.zp32.p, N,
-                                        sh.chunk, nk, a.partv32.p + ch * plane);
+                                        sh.chunk, nk, a.partv32.p + ch * plane, &c->out.p->err);
          else
             k_sfac64<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, a.phv64.p + (size_t)ch * N, d.z64.p,
                                         N, sh.chunk, nk, a.partv64.p + ch * plane);

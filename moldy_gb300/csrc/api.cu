@@ -219,6 +219,8 @@ mdgpu_status mdgpu::sync_out(mdgpu_ctx *c)
    fill_info(c);
    if (c->h_out->err & 1)
       return fail(c, MDGPU_E_RANGE, "Co-ordinate out of range in BIN (fill_cells)");
+   if (c->h_out->err & 4)
+      return fail(c, MDGPU_E_CUDA, "a structure-factor tile copy did not complete (bounded wait expired)");
    return MDGPU_OK;
 }
 

@@ -120,51 +120,114 @@ constexpr int SF_TILE = 128;     // sites per shared-memory tile (FP64 pass: hal
 // fmaf(c, zc, fmaf(-s, zs, acc)) does.
 static_assert(KI % 4 == 0, "the structure-factor pass takes k in fours");
 
+// Tiles of a chunk's sites reach shared memory by bulk asynchronous copies
+// (the TMA engine's cp.async.bulk, completion counted on an mbarrier) into
+// two buffers: tile j+1 is in flight while tile j is summed.  A tile is
+// contiguous in global memory (per-slot records and tables), 16-byte
+// aligned, and a multiple of 16 bytes long, as the bulk copy requires.
+constexpr int SF_TILE32 = 128;              // sites per buffer
+constexpr unsigned int SF_WAIT_LIMIT = 1u << 22;   // try_wait rounds before giving up
+
+__device__ __forceinline__ unsigned int smem_addr(const void *p)
+{
+   return (unsigned int)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned int bytes, unsigned long long *bar)
+{
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                :
+                : "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                : "memory");
+}
+
+// Bounded wait for the given phase of an mbarrier; false if it did not
+// complete (the caller records the error and skips the tile).
+__device__ __forceinline__ bool bar_wait(unsigned long long *bar, unsigned int parity)
+{
+   const unsigned int a = smem_addr(bar);
+   for (unsigned int it = 0; it < SF_WAIT_LIMIT; it++) {
+      unsigned int done;
+      asm volatile("{\n\t.reg .pred p;\n\t"
+                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                   "selp.u32 %0, 1, 0, p;\n\t}"
+                   : "=r"(done)
+                   : "r"(a), "r"(parity)
+                   : "memory");
+      if (done) return true;
+   }
+   return false;
+}
+
 __global__ void __launch_bounds__(128)
 k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nitems,
          const int4 *__restrict__ ph, const float2 *__restrict__ zp, int N, int chunk, int nk,
-         float2 *__restrict__ part)
+         float2 *__restrict__ part, int *__restrict__ err)
 {
-   __shared__ int4 sph[SF_TILE];
-   __shared__ __align__(16) float szp[SF_TILE * 2 * KI];
+   __shared__ __align__(128) float szp[2][SF_TILE32 * 2 * KI];
+   __shared__ __align__(16) int4 sph[2][SF_TILE32];
+   __shared__ __align__(8) unsigned long long bar[2];
    const int it = blockIdx.x * blockDim.x + threadIdx.x;
    const int4 hd = it < nitems ? item[it] : make_int4(0, 0, 0, 0);
    const int s0 = blockIdx.y * chunk, s1 = min(N, s0 + chunk);
+   const int ntiles = s1 > s0 ? (s1 - s0 + SF_TILE32 - 1) / SF_TILE32 : 0;
    f2x ac[KI / 2], as[KI / 2];   // (t, t+1) pairs of Re and Im S(k)
 #pragma unroll
    for (int j = 0; j < KI / 2; j++) ac[j] = as[j] = 0ull;
    const unsigned int H = (unsigned int)hd.x, K = (unsigned int)hd.y, L = (unsigned int)hd.z;
-   const float4 *zsrc = reinterpret_cast<const float4 *>(zp);
-   float4 *zdst = reinterpret_cast<float4 *>(szp);
-   for (int tb = s0; tb < s1; tb += SF_TILE) {
-      const int nt = min(SF_TILE, s1 - tb);
-      __syncthreads();
-      for (int q = threadIdx.x; q < nt; q += blockDim.x) sph[q] = ph[tb + q];
-      for (int q = threadIdx.x; q < nt * (KI / 2); q += blockDim.x) zdst[q] = zsrc[(size_t)tb * (KI / 2) + q];
-      __syncthreads();
-      const int nq4 = (hd.w + 3) >> 2;   // k quads of this item (uniform over a warp but at group edges)
-      for (int q = 0; q < nt; q++) {
-         const int4 v = sph[q];
-         const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
-         float sn, cs;
-         sincos_poly(p, &sn, &cs);
-         const float qv = __int_as_float(v.w);
-         cs *= qv;
-         sn *= qv;
-         const f2x c2 = pk2(cs, cs), s2 = pk2(sn, sn), ns2 = neg2(s2);
-         const ulonglong2 *zc = reinterpret_cast<const ulonglong2 *>(szp + q * 2 * KI);
-         const ulonglong2 *zs = zc + KI / 4;
+   // one thread issues the copies: a tile's records and its z tables
+   auto issue = [&](int j) {
+      const int b = j & 1, tb = s0 + j * SF_TILE32, nt = min(SF_TILE32, s1 - tb);
+      const unsigned int bytes = (unsigned int)nt * (16u + 8u * KI);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                   :
+                   : "r"(smem_addr(&bar[b])), "r"(bytes)
+                   : "memory");
+      bulk_load(sph[b], ph + tb, (unsigned int)nt * 16u, &bar[b]);
+      bulk_load(szp[b], zp + (size_t)tb * KI, (unsigned int)nt * 8u * KI, &bar[b]);
+   };
+   if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(smem_addr(&bar[0])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(smem_addr(&bar[1])) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" : : : "memory");
+   }
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      if (ntiles > 0) issue(0);
+      if (ntiles > 1) issue(1);
+   }
+   const int nq4 = (hd.w + 3) >> 2;   // k quads of this item (uniform over a warp but at group edges)
+   for (int j = 0; j < ntiles; j++) {
+      const int b = j & 1, tb = s0 + j * SF_TILE32, nt = min(SF_TILE32, s1 - tb);
+      if (bar_wait(&bar[b], (unsigned int)(j >> 1) & 1u)) {
+         const float *zb = szp[b];
+         for (int q = 0; q < nt; q++) {
+            const int4 v = sph[b][q];
+            const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
+            float sn, cs;
+            sincos_poly(p, &sn, &cs);
+            const float qv = __int_as_float(v.w);
+            cs *= qv;
+            sn *= qv;
+            const f2x c2 = pk2(cs, cs), s2 = pk2(sn, sn), ns2 = neg2(s2);
+            const ulonglong2 *zc = reinterpret_cast<const ulonglong2 *>(zb + q * 2 * KI);
+            const ulonglong2 *zs = zc + KI / 4;
 #pragma unroll
-         for (int j = 0; j < KI / 4; j++) {
-            if (j < nq4) {
-               const ulonglong2 c = zc[j], sv = zs[j];
-               ac[2 * j] = fma2(c2, c.x, fma2(ns2, sv.x, ac[2 * j]));
-               as[2 * j] = fma2(s2, c.x, fma2(c2, sv.x, as[2 * j]));
-               ac[2 * j + 1] = fma2(c2, c.y, fma2(ns2, sv.y, ac[2 * j + 1]));
-               as[2 * j + 1] = fma2(s2, c.y, fma2(c2, sv.y, as[2 * j + 1]));
+            for (int jj = 0; jj < KI / 4; jj++) {
+               if (jj < nq4) {
+                  const ulonglong2 c = zc[jj], sv = zs[jj];
+                  ac[2 * jj] = fma2(c2, c.x, fma2(ns2, sv.x, ac[2 * jj]));
+                  as[2 * jj] = fma2(s2, c.x, fma2(c2, sv.x, as[2 * jj]));
+                  ac[2 * jj + 1] = fma2(c2, c.y, fma2(ns2, sv.y, ac[2 * jj + 1]));
+                  as[2 * jj + 1] = fma2(s2, c.y, fma2(c2, sv.y, as[2 * jj + 1]));
+               }
             }
          }
+      } else if (threadIdx.x == 0) {
+         atomicOr(err, 4);
       }
+      __syncthreads();   // every thread is done with buffer b
+      if (threadIdx.x == 0 && j + 2 < ntiles) issue(j + 2);
    }
    if (it < nitems) {
       const int k0 = item_k0[it];
@@ -777,11 +840,12 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    const dim3 gs((ni + 127) / 128, sh.chunks);
    if (mixed) {
       CK(d.part32.ensure((size_t)sh.chunks * nk));
-      k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, N, sh.chunk, nk, d.part32.p);
+      k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, N, sh.chunk, nk, d.part32.p,
+                                   &out->err);
       if (nf > 0) {
          CK(d.partf32.ensure((size_t)sh.chunks * nk));
          k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.phf32.p, d.zp32.p, N, sh.chunk, nk,
-                                      d.partf32.p);
+                                      d.partf32.p, &out->err);
       }
    } else {
       CK(d.part64.ensure((size_t)sh.chunks * nk));

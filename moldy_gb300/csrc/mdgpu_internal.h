@@ -103,7 +103,8 @@ struct DevOut {
    double pe_k;           // sum of k-space energies (before self/sheet)
    double st_k[6];
    double vir_in[6];      // sum x_i (x) f_in_i, reference-semantics calls only
-   int err;               // bit 0: co-ordinate out of range
+   int err;               // bit 0: co-ordinate out of range; bit 2: a
+                          // structure-factor tile copy timed out
    int n_too_close;
    int64_t npairs2;       // full-list pair evaluations (2x reference count)
    int too_close[MAX_TOO_CLOSE_REC][2];

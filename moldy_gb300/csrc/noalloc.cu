@@ -32,7 +32,7 @@ __global__ void k_prep(int N, const int *sorted, const double *site, const doubl
                        double hi7, double hi8, int mixed, int4 *ph32, float2 *z32, float2 *zp32,
                        ulonglong2 *ph64a, ulonglong2 *ph64b, double2 *z64);
 __global__ void k_sfac32(const int4 *item, const int *item_k0, int nitems, const int4 *ph,
-                         const float2 *zp, int N, int chunk, int nk, float2 *part);
+                         const float2 *zp, int N, int chunk, int nk, float2 *part, int *err);
 __global__ void k_kfinal(const double *blk, int nblocks, DevOut *out);
 __global__ void k_force32(const int4 *item, const int *item_k0, const float2 *item_kxy, int nitems,
                           int nk, int per_split, const float4 *kd, const int4 *ph, const float2 *zz,
@@ -129,7 +129,8 @@ __global__ void k_iota(int n, int *a)
 __global__ void k_add_energy(const DevOut *o, double *pe, double *stress)
 {
    if (threadIdx.x != 0) return;
-   *pe += o->pe_k;
+   // a structure-factor tile that never arrived leaves the energy undefined
+   *pe += (o->err & 4) ? __longlong_as_double(0x7ff8000000000000ll) : o->pe_k;
    stress[0] += o->st_k[0];
    stress[1] += o->st_k[1];
    stress[2] += o->st_k[2];
@@ -255,7 +256,7 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    if (chunks > MAX_CHUNKS) chunks = MAX_CHUNKS;
    const int chunk = ((N + chunks - 1) / chunks + 31) / 32 * 32;
    chunks = (N + chunk - 1) / chunk;
-   k_sfac32<<<dim3((ni + 127) / 128, chunks), 128, 0, st>>>(item, k0, ni, ph, zp, N, chunk, nk, part);
+   k_sfac32<<<dim3((ni + 127) / 128, chunks), 128, 0, st>>>(item, k0, ni, ph, zp, N, chunk, nk, part, &out->err);
    const int nbk = (nk + 255) / 256;
    k_kreduce_na<<<nbk, 256, 0, st>>>(nk, chunks, part, kvec, coef, coef2, kdat, blk);
    k_kfinal<<<1, 256, 0, st>>>(blk, nbk, out);
