@@ -218,6 +218,7 @@ mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl)
    inv3(h, hinvp);
    for (int i = 0; i < 9; i++) kl.hinv[i] = hinvp[i];
    for (int i = 0; i < 9; i++) hinvp[i] = 2 * PI * hinvp[i];
+   kl.dkz = hinvp[8];
    const double kcsq = kc * kc;
    kl.vol = det3(h);
    const double r4a = -1.0 / (4.0 * alpha * alpha);

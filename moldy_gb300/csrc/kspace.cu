@@ -398,15 +398,17 @@ __global__ void __launch_bounds__(FT_THREADS)
 k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
           const float2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
           const float4 *__restrict__ kd, const int4 *__restrict__ ph, const float2 *__restrict__ zz,
-          const double *__restrict__ chg, const int *__restrict__ sorted, int N, int obase,
+          const double *__restrict__ chg, const int *__restrict__ sorted, int N, int obase, float dkz,
           double *__restrict__ fpart)
 {
    __shared__ int4 s_it[FT_ITEMS];
    __shared__ float2 s_kxy[FT_ITEMS];
    __shared__ int s_k0[FT_ITEMS];
-   // per k, duplicated for the paired instructions: (A, A, -B, -B), (kz, kz)
+   __shared__ float s_kz0[FT_ITEMS];
+   // per k, duplicated for the paired instructions: (A, A, -B, -B).  Along
+   // an item kz is linear in t (kz = kz0 + t dkz, the k-list's l step), so
+   // the z force needs only sum f and sum t f per item: no kz per k.
    __shared__ ulonglong2 s_ab[FT_ITEMS * KI];
-   __shared__ unsigned long long s_kz[FT_ITEMS * KI];
    // two sites per thread, FT_THREADS apart: they share every load of the
    // per-k coefficients and the item bookkeeping, and run as the two lanes
    // of paired FP32 instructions (f32x2)
@@ -427,6 +429,7 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
       zc[t] = pk2(live0 ? za[t] : 1.f, live1 ? zb[t] : 1.f);
       zs[t] = pk2(live0 ? za[KI + t] : 0.f, live1 ? zb[KI + t] : 0.f);
    }
+   const f2x dkz2 = pk2(dkz, dkz);
    const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
    // compensated (Kahan) FP32 sums, taken every 4 items of plain FP32
    // partials: no FP64 instruction in the loop (on this part the FP64 pipe
@@ -444,11 +447,11 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
          s_it[q] = item[tb + q];
          s_kxy[q] = item_kxy[tb + q];
          s_k0[q] = item_k0[tb + q] - kb;
+         s_kz0[q] = kd[item_k0[tb + q]].z;
       }
       for (int q = threadIdx.x; q < ke - kb; q += blockDim.x) {
          const float4 k4 = kd[kb + q];
          s_ab[q] = make_ulonglong2(pk2(k4.x, k4.x), pk2(-k4.y, -k4.y));
-         s_kz[q] = pk2(k4.z, k4.z);
       }
       __syncthreads();
       for (int q = 0; q < nt; q++) {
@@ -463,9 +466,8 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
          sincos_poly(pa, &sa0, &ca0);
          sincos_poly(pb, &sb0, &cb0);
          const f2x c0 = pk2(ca0, cb0), s0 = pk2(sa0, sb0), ns0 = pk2(-sa0, -sb0);
-         f2x sf = 0ull, skz = 0ull;
+         f2x sf = 0ull, st = 0ull;   // sum f, sum t f
          const ulonglong2 *abq = s_ab + s_k0[q];
-         const unsigned long long *kzq = s_kz + s_k0[q];
          if (hd.w == KI) {   // full item (block-uniform): no per-k predicate
 #pragma unroll
             for (int t = 0; t < KI; t++) {
@@ -474,7 +476,7 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
                const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));    // sin of k.r
                const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));       // sin A - cos B
                sf = add2(sf, f);
-               skz = fma2(kzq[t], f, skz);
+               if (t > 0) st = fma2(pk2((float)t, (float)t), f, st);
             }
          } else {
 #pragma unroll
@@ -485,14 +487,15 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
                   const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));
                   const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));
                   sf = add2(sf, f);
-                  skz = fma2(kzq[t], f, skz);
+                  if (t > 0) st = fma2(pk2((float)t, (float)t), f, st);
                }
             }
          }
          const float2 kxy = s_kxy[q];
+         const float kz0 = s_kz0[q];
          px = fma2(pk2(kxy.x, kxy.x), sf, px);
          py = fma2(pk2(kxy.y, kxy.y), sf, py);
-         pz = add2(pz, skz);
+         pz = fma2(pk2(kz0, kz0), sf, fma2(dkz2, st, pz));   // sum (kz0 + t dkz) f
          if (++npart == 4) {
             float xa, xb, ya, yb, za, zb;
             upk2(px, xa, xb);
@@ -889,7 +892,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    if (mixed)
       k_force32<<<gf, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
                                            d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, c->rd.sorted.p, N, 0,
-                                           d.fpart.p);
+                                           (float)kl.dkz, d.fpart.p);
    else
       k_force64<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, sh.per_split,
                                     d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, c->rd.sorted.p, N, 0,
@@ -919,7 +922,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       if (mixed)
          k_force32<<<gff, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, shf.per_split,
                                                d.kdatf32.p, d.phc32.p, d.zpc32.p, c->rd.chg.p, d.sortedc.p, nf,
-                                               fw0, d.fpartf.p);
+                                               fw0, (float)kl.dkz, d.fpartf.p);
       else
          k_force64<<<gff, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, shf.per_split,
                                         d.kdatf64.p, d.pac64.p, d.pbc64.p, d.zc64.p, c->rd.chg.p, d.sortedc.p, nf,

@@ -47,6 +47,7 @@ struct KList {
    std::vector<int> item_k0;       // index of the item's first k-vector
    std::vector<double2> item_kxy;  // (kx, ky) of the item's (h,k) column
    std::vector<double> kz;         // per k-vector
+   double dkz = 0;                 // kz step from l to l + 1 (2 pi hinv[2][2])
    std::vector<double> coeff, coeff2;  // src/ewald.c:510-511
    double key[12];                 // h, k_cutoff, alpha
    double vol = 0;

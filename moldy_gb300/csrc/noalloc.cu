@@ -36,7 +36,7 @@ __global__ void k_sfac32(const int4 *item, const int *item_k0, int nitems, const
 __global__ void k_kfinal(const double *blk, int nblocks, DevOut *out);
 __global__ void k_force32(const int4 *item, const int *item_k0, const float2 *item_kxy, int nitems,
                           int nk, int per_split, const float4 *kd, const int4 *ph, const float2 *zz,
-                          const double *chg, const int *sorted, int N, int obase, double *fpart);
+                          const double *chg, const int *sorted, int N, int obase, float dkz, double *fpart);
 __global__ void k_fsum(int n3, int nsplit, const double *fpart, double *force, int accumulate);
 }  // namespace mdgpu
 
@@ -266,7 +266,7 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    const int per_split = (ni + splits - 1) / splits;
    splits = (ni + per_split - 1) / per_split;
    k_force32<<<dim3((N + 2 * FT_THREADS - 1) / (2 * FT_THREADS), splits), FT_THREADS, 0, st>>>(
-      item, k0, kxy, ni, nk, per_split, kdat, ph, zp, d_chg, sorted, N, 0, fpart);
+      item, k0, kxy, ni, nk, per_split, kdat, ph, zp, d_chg, sorted, N, 0, (float)hp[8], fpart);
    k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, splits, fpart, d_force, 1);
    k_add_energy<<<1, 32, 0, st>>>(out, d_pe, d_stress);
    e = cudaGetLastError();
