@@ -394,6 +394,25 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
    s = t;
 }
 
+static_assert(KI == 16, "k_force32 unrolls item counts 1..16");
+
+// One item's k-vectors for two sites (the two lanes): sum over t of
+// f = sin(k.r) A - cos(k.r) B and of t f, with exp(i k.r) = seed * zp[t].
+template <int W>
+__device__ __forceinline__ void item_force(const f2x *zc, const f2x *zs, f2x c0, f2x s0, f2x ns0,
+                                           const ulonglong2 *abq, f2x &sf, f2x &st)
+{
+#pragma unroll
+   for (int t = 0; t < W; t++) {
+      const ulonglong2 ab = abq[t];
+      const f2x cs = fma2(c0, zc[t], mul2(ns0, zs[t]));   // cos of k.r, both sites
+      const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));    // sin of k.r
+      const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));       // sin A - cos B
+      sf = add2(sf, f);
+      if (t > 0) st = fma2(pk2((float)t, (float)t), f, st);
+   }
+}
+
 __global__ void __launch_bounds__(FT_THREADS)
 k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
           const float2 *__restrict__ item_kxy, int nitems, int nk, int per_split,
@@ -468,28 +487,16 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
          const f2x c0 = pk2(ca0, cb0), s0 = pk2(sa0, sb0), ns0 = pk2(-sa0, -sb0);
          f2x sf = 0ull, st = 0ull;   // sum f, sum t f
          const ulonglong2 *abq = s_ab + s_k0[q];
-         if (hd.w == KI) {   // full item (block-uniform): no per-k predicate
-#pragma unroll
-            for (int t = 0; t < KI; t++) {
-               const ulonglong2 ab = abq[t];
-               const f2x cs = fma2(c0, zc[t], mul2(ns0, zs[t]));   // cos of k.r, both sites
-               const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));    // sin of k.r
-               const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));       // sin A - cos B
-               sf = add2(sf, f);
-               if (t > 0) st = fma2(pk2((float)t, (float)t), f, st);
-            }
-         } else {
-#pragma unroll
-            for (int t = 0; t < KI; t++) {
-               if (t < hd.w) {
-                  const ulonglong2 ab = abq[t];
-                  const f2x cs = fma2(c0, zc[t], mul2(ns0, zs[t]));
-                  const f2x sn = fma2(s0, zc[t], mul2(c0, zs[t]));
-                  const f2x f = fma2(sn, ab.x, mul2(cs, ab.y));
-                  sf = add2(sf, f);
-                  if (t > 0) st = fma2(pk2((float)t, (float)t), f, st);
-               }
-            }
+         // the item's count is block-uniform: a loop unrolled for each
+         // count, no per-k predicate
+         switch (hd.w) {
+#define MDGPU_ITEM(W) \
+         case W: item_force<W>(zc, zs, c0, s0, ns0, abq, sf, st); break;
+            MDGPU_ITEM(16) MDGPU_ITEM(15) MDGPU_ITEM(14) MDGPU_ITEM(13) MDGPU_ITEM(12) MDGPU_ITEM(11)
+            MDGPU_ITEM(10) MDGPU_ITEM(9) MDGPU_ITEM(8) MDGPU_ITEM(7) MDGPU_ITEM(6) MDGPU_ITEM(5)
+            MDGPU_ITEM(4) MDGPU_ITEM(3) MDGPU_ITEM(2) MDGPU_ITEM(1)
+#undef MDGPU_ITEM
+         default: break;
          }
          const float2 kxy = s_kxy[q];
          const float kz0 = s_kz0[q];
