@@ -450,7 +450,7 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    }
    const f2x dkz2 = pk2(dkz, dkz);
    const int a = blockIdx.y * per_split, b = min(nitems, a + per_split);
-   // compensated (Kahan) FP32 sums, taken every 4 items of plain FP32
+   // compensated (Kahan) FP32 sums, taken every 8 items of plain FP32
    // partials: no FP64 instruction in the loop (on this part the FP64 pipe
    // retires two lanes per clock per SM; a periodic FP64 fold halved the rate)
    float fxa = 0.f, fya = 0.f, fza = 0.f, exa = 0.f, eya = 0.f, eza = 0.f;
@@ -503,7 +503,7 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
          px = fma2(pk2(kxy.x, kxy.x), sf, px);
          py = fma2(pk2(kxy.y, kxy.y), sf, py);
          pz = fma2(pk2(kz0, kz0), sf, fma2(dkz2, st, pz));   // sum (kz0 + t dkz) f
-         if (++npart == 4) {
+         if (++npart == 8) {
             float xa, xb, ya, yb, za, zb;
             upk2(px, xa, xb);
             upk2(py, ya, yb);
