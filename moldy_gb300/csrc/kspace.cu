@@ -201,6 +201,7 @@ k_sfac32(const int4 *__restrict__ item, const int *__restrict__ item_k0, int nit
       const int b = j & 1, tb = s0 + j * SF_TILE32, nt = min(SF_TILE32, s1 - tb);
       if (bar_wait(&bar[b], (unsigned int)(j >> 1) & 1u)) {
          const float *zb = szp[b];
+#pragma unroll 2
          for (int q = 0; q < nt; q++) {
             const int4 v = sph[b][q];
             const unsigned int p = H * (unsigned int)v.x + K * (unsigned int)v.y + L * (unsigned int)v.z;
