@@ -260,8 +260,9 @@ mdgpu_status mdgpu_fm_loss_grad(mdgpu_ctx *ctx, const mdgpu_params *params, cons
  * reference's: c_of_m and mom [nmols][3] (fractional centres of mass and
  * scaled momenta h^T h m ds/dt), quat and amom [nmols_r][4] for the
  * molecules of rotating species in species order (amom[0] unused, [1..3]
- * principal angular momenta).  Framework species, thermostats and barostats
- * are not supported. */
+ * principal angular momenta).  A framework molecule (rdof 0) is held fixed
+ * as do_step holds it: its momentum is zeroed after the kicks
+ * (src/accel.c:748-755).  Thermostats and barostats are not supported. */
 typedef struct {
    const double *mass;          /* [nspecies] molecular mass, amu             */
    const double *inertia;       /* [nspecies][3] principal moments of inertia */

@@ -275,9 +275,12 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
                   if (S.inertia[k] > INERTIA_MIN) ker += 0.5 * L[k] * L[k] / S.inertia[k];
          }
       }
-      pm[0] = x[0];
-      pm[1] = x[1];
-      pm[2] = x[2];
+      // the framework constraint of do_step (src/accel.c:748-755): after the
+      // kicks (and after the kinetic energy at the half kick) a framework
+      // molecule's momentum is zero
+      pm[0] = S.framework ? 0.0 : x[0];
+      pm[1] = S.framework ? 0.0 : x[1];
+      pm[2] = S.framework ? 0.0 : x[2];
    }
    // fixed-shape block sums
    sh[0][threadIdx.x] = ket;
@@ -516,7 +519,6 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    if (!c->have_system || !c->have_control)
       return fail(c, MDGPU_E_ARG, "mdgpu_set_system and mdgpu_set_control come first");
    if (!(dyn->step > 0.0)) return fail(c, MDGPU_E_ARG, "the timestep must be positive");
-   if (c->fw_mol >= 0) return fail(c, MDGPU_E_UNSUPPORTED, "dynamics with a framework molecule are not supported");
    mdgpu_status s = ensure_ready(c, h, true, true);
    if (s) return s;
    MdHost &H = c->mdh;
@@ -549,6 +551,8 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
       }
       S.nsites = sp.nsites;
       S.pf0 = pf0;
+      S.framework = sp.framework ? 1 : 0;
+      if (S.framework && dyn->rdof[k] > 0) return fail(c, MDGPU_E_ARG, "a framework species cannot rotate");
       const double sc = H.half / S.mass;
       for (int i = 0; i < 9; i++) S.gdrift[i] = sc * Gi[i];
       const bool rot = dyn->rdof[k] > 0;

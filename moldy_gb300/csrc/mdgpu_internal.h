@@ -188,6 +188,7 @@ struct MdSpec {
    double inertia[3], rinertia[3];   // principal moments and their inverses
    double gdrift[9];                 // (dt/2 / mass) (h^T h)^-1, leapf_com's matrix
    int nsites, pf0;                  // sites per molecule, first principal-frame site
+   int framework;                    // fixed framework: momentum zeroed after the kicks
 };
 
 struct MdHost {

@@ -59,26 +59,30 @@ def species_dynamics(sysm: System, step: float, nosymmetric_rot: bool = False) -
         I = np.array([np.sum(m * (p[:, 1] ** 2 + p[:, 2] ** 2)), np.sum(m * (p[:, 0] ** 2 + p[:, 2] ** 2)),
                       np.sum(m * (p[:, 0] ** 2 + p[:, 1] ** 2))])
         off = np.array([np.sum(m * p[:, 0] * p[:, 1]), np.sum(m * p[:, 0] * p[:, 2]), np.sum(m * p[:, 1] * p[:, 2])])
-        if sp.nsites > 1 and np.max(np.abs(off)) > 1e-8 * max(I.max(), 1e-30):
+        # a framework does not rotate (src/startup.c:557-561): its sites stay
+        # as given, only centred on the centre of mass
+        if sp.nsites > 1 and not sp.framework and np.max(np.abs(off)) > 1e-8 * max(I.max(), 1e-30):
             raise ValueError(f"species {sp.name}: principal-frame sites are not on the principal axes")
         nz = sum(1 for i in range(3) if I[i] <= 1e-14 * (I[(i + 1) % 3] + I[(i + 2) % 3]))
         mass.append(M)
         inertia.append(I)
-        rdof.append(0 if sp.nsites == 1 else 3 - nz)
+        rdof.append(0 if sp.nsites == 1 or sp.framework else 3 - nz)
     return Dynamics(np.array(mass), np.array(inertia), np.array(rdof, np.int32), float(step), nosymmetric_rot)
 
 
 def thermal_state(sysm: System, dyn: Dynamics, temp: float, seed: int) -> MDState:
     """Seeded Maxwell-Boltzmann momenta at ``temp`` K with zero total linear
-    momentum; principal angular momenta L_i = I_i w_i with w_i Gaussian of
-    variance kT/I_i.  Orientations are the system's (identity if it has
-    none)."""
+    momentum (framework molecules at rest); principal angular momenta
+    L_i = I_i w_i with w_i Gaussian of variance kT/I_i.  Orientations are
+    the system's (identity if it has none)."""
     rng = np.random.default_rng(seed)
     h = np.asarray(sysm.h, np.float64)
     nm = sysm.nmols
     masses = np.concatenate([np.full(sp.nmols, dyn.mass[k]) for k, sp in enumerate(sysm.species)])
+    moving = np.concatenate([np.full(sp.nmols, not sp.framework) for sp in sysm.species])
     p = rng.normal(0.0, 1.0, (nm, 3)) * np.sqrt(KB * temp * masses)[:, None]
-    p -= p.sum(0) / nm
+    p[~moving] = 0.0                                # a framework is held fixed
+    p[moving] -= p[moving].sum(0) / max(int(moving.sum()), 1)
     mom = p @ h                                     # h^T p per molecule
     nq = int(sum(sp.nmols for k, sp in enumerate(sysm.species) if dyn.rdof[k] > 0))
     amom = np.zeros((nq, 4))

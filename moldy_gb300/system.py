@@ -284,6 +284,58 @@ def water(nside: int = 8, density_gcc: float = 1.0, seed: int = 2, alpha: float 
                   name=f"water{4 * nmols}", site_mass=np.array([0.0, 16.0, 1.0, 0.0]), quat=q)
 
 
+def water_on_framework(nside: int = 7, nlayers: int = 5, nwall: int = 8, spacing: float = 3.1,
+                       seed: int = 6, alpha: float = 0.3, cutoff: float = 9.0, accuracy: float = 1.0e-5,
+                       wall_charge: float = 0.4, strict: bool = False) -> System:
+    """Rigid water over a charged framework: a cubic box of side
+    nside*spacing; a framework molecule of nwall^2 sites on a square grid in
+    the plane z = 0 with charges +-``wall_charge`` e in a checkerboard
+    (neutral), mass 28 each; nside^2 * nlayers TIP4P-like molecules on a
+    lattice between z = 3.6 Å and the periodic image of the wall, seeded
+    random orientations.  LJ O-O as in :func:`water`, O-wall epsilon
+    0.5 kJ/mol, sigma 3.2 Å; framework-framework pairs are excluded by the
+    force path, as the reference excludes them.  Species order: water, then
+    the framework (frameworks last, src/input.c:95-117)."""
+    rng = np.random.default_rng(seed)
+    L = nside * spacing
+    if 3.6 + (nlayers - 1) * spacing > L - 3.6:
+        raise ValueError("the water layers do not fit between the wall and its image")
+    h = np.diag([L, L, L])
+    pf, _ = tip4p_geometry()
+    g = (np.arange(nside) + 0.5) / nside - 0.5
+    zl = (3.6 + spacing * np.arange(nlayers)) / L
+    com_frac = np.stack(np.meshgrid(g, g, zl, indexing="ij"), axis=-1).reshape(-1, 3)
+    com_frac[:, 2] -= np.floor(com_frac[:, 2] + 0.5)
+    nw = len(com_frac)
+    q = _random_quaternions(rng, nw)
+    R = _rotation_matrices(q)
+    xw = ((h @ com_frac.T).T[:, None, :] + np.einsum("mij,sj->msi", R, pf)).reshape(-1, 3)
+    # the framework: one molecule; its sites relative to its centre of mass
+    gw = (np.arange(nwall) + 0.25) / nwall - 0.5
+    wx, wy = np.meshgrid(gw, gw, indexing="ij")
+    wall = np.stack([wx.ravel() * L, wy.ravel() * L, np.zeros(nwall * nwall)], axis=1)
+    sign = ((np.arange(nwall)[:, None] + np.arange(nwall)[None, :]) % 2).ravel()
+    wcom = wall.mean(0)
+    wall_pf = wall - wcom
+    x = np.concatenate([xw, wall]).T
+    x = _wrap_sites(h, x.copy())
+    max_id = 6
+    potpar = _potpar(max_id)
+    _set_pot(potpar, max_id, 1, 1, [4.0 * 0.6485 / CONV_E, 3.154])
+    for wid in (4, 5):
+        _set_pot(potpar, max_id, 1, wid, [4.0 * 0.5 / CONV_E, 3.2])
+    site_charge = np.array([0.0, 0.0, 0.52, -1.04, wall_charge, -wall_charge]) / CONV_Q
+    spec_w = Species("Water", nw, np.array([1, 2, 2, 3], np.int32), pf)
+    spec_f = Species("Wall", 1, np.where(sign == 0, 4, 5).astype(np.int32), wall_pf, framework=True)
+    c_of_m = np.concatenate([com_frac, (np.linalg.inv(h) @ wcom)[None, :]])
+    return System(h=h, species=[spec_w, spec_f], ptype=LJPOT, potpar=potpar, site_charge=site_charge,
+                  site=x, c_of_m=c_of_m,
+                  control=Control(cutoff=cutoff, alpha=alpha, k_cutoff=ewald_k_cutoff(alpha, accuracy),
+                                  strict_cutoff=strict),
+                  name=f"waterwall{4 * nw + nwall * nwall}",
+                  site_mass=np.array([0.0, 16.0, 1.0, 0.0, 28.0, 28.0]), quat=q)
+
+
 def rock_salt(ncell: int = 16, a: float = 5.64, displacement: float = 0.1, seed: int = 3,
               alpha: float = 0.35, cutoff: float = 10.0, accuracy: float = 1.0e-5,
               k_cutoff: Optional[float] = None) -> System:

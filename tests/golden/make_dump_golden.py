@@ -8,7 +8,7 @@ file the reference wrote (raw bytes, key "file:<name>").  The reference is
 built without XDR (rpc/xdr.h is absent here), so these are native LP64
 files.
 
-usage: python tests/golden/make_dump_golden.py
+usage: python tests/golden/make_dump_golden.py [--only NAME]
 """
 import os
 import subprocess
@@ -29,6 +29,7 @@ CASES = [
     ("dump_water864", "md_water864", 30, 11, 5, 4, "rigid water, 216 molecules"),
     ("dump_argon500", "md_argon500", 50, 3, 10, 10, "argon fcc 500"),
     ("dump_rocksalt512", "md_rocksalt512", 30, 9, 10, 2, "rock salt 512"),
+    ("dump_waterwall", "md_waterwall", 30, 11, 10, 4, "water over a framework"),
 ]
 
 
@@ -41,7 +42,10 @@ def load_md(name):
 
 def main():
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     for name, src, steps, level, interval, ndumps, title in CASES:
+        if only is not None and name != only:
+            continue
         sysm, dyn, st0 = load_md(src)
         _, _, _, files = md.run(sysm, dyn, st0, steps, dump=("run%02d.dmp", level, interval, ndumps, title))
         arrs = {"file:" + k: np.frombuffer(v, np.uint8) for k, v in files.items()}

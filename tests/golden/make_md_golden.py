@@ -12,7 +12,11 @@ every step of a long run (10^4 steps of 2048-site water at 1 fs, lazy and
 strict cutoffs; 1000 steps of 500-atom argon at 10 fs) and its CPU time per
 step, for the energy-drift comparison.
 
-usage: python tests/golden/make_md_golden.py [--skip-drift]
+The framework fixture (md_waterwall) holds rigid water over a fixed,
+charged framework molecule: the reference zeroes the framework's momentum
+after each step's kicks (src/accel.c:748-755).
+
+usage: python tests/golden/make_md_golden.py [--skip-drift] [--only NAME]
 """
 import os
 import subprocess
@@ -50,6 +54,12 @@ def save(name, sysm, dyn, st, rec, fin, sec, temp, seed, **extra):
 
 def main():
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    ww = S.water_on_framework()
+    if only in (None, "md_waterwall"):
+        save("md_waterwall", ww, *case(ww, 0.001, 300.0, 9, 30), 300.0, 9)
+    if only is not None:
+        return
     w = S.water(nside=6, seed=3)
     save("md_water864", w, *case(w, 0.001, 300.0, 4, 30), 300.0, 4)
     ws = dataclasses.replace(w, control=dataclasses.replace(w.control, strict_cutoff=True))

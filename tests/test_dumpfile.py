@@ -10,7 +10,7 @@ import pytest
 
 from conftest import GOLDEN
 
-CASES = ["dump_water864", "dump_argon500", "dump_rocksalt512"]
+CASES = ["dump_water864", "dump_argon500", "dump_rocksalt512", "dump_waterwall"]
 
 
 def _fixture(name):

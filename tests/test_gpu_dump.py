@@ -11,7 +11,7 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["dump_water864", "dump_argon500", "dump_rocksalt512"]
+CASES = ["dump_water864", "dump_argon500", "dump_rocksalt512", "dump_waterwall"]
 
 
 def _setup(name, prec):

@@ -11,7 +11,7 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-SHORT = ["md_water864", "md_water864_strict_nosym", "md_water864_molpbc", "md_argon500", "md_rocksalt512"]
+SHORT = ["md_water864", "md_water864_strict_nosym", "md_water864_molpbc", "md_argon500", "md_rocksalt512", "md_waterwall"]
 
 
 def _load(name):
