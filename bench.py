@@ -20,9 +20,14 @@ Default arm (--impl gb300):
              forces against the FP64 ones on the same configuration;
   nve        constant-energy runs (10^4 mixed steps, 300 FP64 steps by
              default): steps/s, ns/day, drift of the conserved quantity;
-  e2e        steps/s through the drop-in force call (mdgpu_forces) with
-             pinned host buffers: the H2D copy of the site co-ordinates and
-             the D2H copy of forces, energies and stress inside every step;
+  e2e        MD steps/s through the public C API with the dynamic state in
+             pinned host memory: every step uploads it (mdgpu_md_set_state),
+             runs one step (mdgpu_md_run) and downloads it with the step's
+             energies (mdgpu_md_get_state);
+  e2e_force_call  force evaluations/s through the drop-in force call
+             (mdgpu_forces), as a host-side integrator would make it: the H2D
+             copy of the site co-ordinates and the D2H copy of forces,
+             energies and stress inside every call;
   roofline   the dominant kernel's algorithmic FLOP/s (reference op counts)
              against the FP32 FMA peak measured on this GPU;
   cpu_baseline  the reference algorithm's C restatement (oracle/port),
@@ -345,7 +350,36 @@ def run_gpu(args):
     for i in range(args.steps):
         e2e_step(i)
     barrier()
+    force_call_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
+
+    # the MD step through the public C API with the dynamic state in pinned
+    # host memory: upload the state, one step, download the state and the
+    # step's energies -- every step
+    md_h = MolecularDynamics(ff, dyn, state0)
+    nq = md_h.nq
+    h_cm = torch.from_numpy(np.ascontiguousarray(state0.c_of_m, np.float64)).pin_memory()
+    h_mom = torch.from_numpy(np.ascontiguousarray(state0.mom, np.float64)).pin_memory()
+    h_q = torch.from_numpy(np.ascontiguousarray(state0.quat, np.float64).reshape(-1)).pin_memory()
+    h_am = torch.from_numpy(np.ascontiguousarray(state0.amom, np.float64).reshape(-1)).pin_memory()
+    h_en = torch.zeros(4, dtype=torch.float64).pin_memory()
+    pt = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_double))  # noqa: E731
+
+    def md_e2e_step(i):
+        for st in (L.mdgpu_md_set_state(ff.ctx, pt(h_cm), pt(h_mom), pt(h_q), pt(h_am)),
+                   L.mdgpu_md_run(ff.ctx, 1, pt(h_en)),
+                   L.mdgpu_md_get_state(ff.ctx, pt(h_cm), pt(h_mom), pt(h_q), pt(h_am))):
+            if st != 0:
+                raise RuntimeError(L.mdgpu_last_error(ff.ctx).decode())
+
+    for i in range(args.warmup):
+        md_e2e_step(i)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        md_e2e_step(i)
+    barrier()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    state_bytes = 8 * (6 * sysA.nmols + 8 * nq)
     info = ff.info()
 
     # ---- roofline of the dominant kernel ---------------------------------------
@@ -389,9 +423,14 @@ def run_gpu(args):
                        "mixed_over_fp64": ms_force_fp64 / ms_force_mixed},
         "accuracy": {"force_rel_rms_mixed_vs_fp64": ferr, "energy_rel_mixed_vs_fp64": e_err},
         "nve": nve,
-        "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 3 * n * 8,
-                "d2h_bytes_per_step": 3 * n * 8 + 11 * 8 + 512,
-                "path": "mdgpu_forces (the drop-in force call) on host arrays each step"},
+        "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes + 4 * 8,
+                "path": "mdgpu_md_set_state + mdgpu_md_run(1) + mdgpu_md_get_state on pinned host "
+                        "arrays each step (centres of mass, momenta, quaternions, angular momenta)"},
+        "e2e_force_call": {"value": world / force_call_s, "unit": "force evaluations/s",
+                           "h2d_bytes_per_step": 3 * n * 8, "d2h_bytes_per_step": 3 * n * 8 + 11 * 8 + 512,
+                           "path": "mdgpu_forces (the drop-in force call of a host integrator) on pinned "
+                                   "host arrays each step"},
         "gpu_launches": int(launches_timed),
         "phases_ms": phases,
         "roofline": {"kernel": kernel_names[dom], "bound": "fp32", "achieved": achieved,

@@ -285,6 +285,12 @@ mdgpu_status mdgpu_md_init(mdgpu_ctx *ctx, const mdgpu_dynamics *dyn, const doub
  * cell or a quaternion lost its normalisation (QNORM2). */
 mdgpu_status mdgpu_md_run(mdgpu_ctx *ctx, int nsteps, double *energies);
 
+/* Replaces the dynamic state (same layout as mdgpu_md_init; any pointer may
+ * be NULL to keep that part), e.g. after a host-side velocity rescaling.
+ * Cheaper than mdgpu_md_init: the tables and the captured step stay. */
+mdgpu_status mdgpu_md_set_state(mdgpu_ctx *ctx, const double *c_of_m, const double *mom,
+                                const double *quat, const double *amom);
+
 /* Copies the current state back (any pointer may be NULL). */
 mdgpu_status mdgpu_md_get_state(mdgpu_ctx *ctx, double *c_of_m, double *mom, double *quat,
                                 double *amom);

@@ -805,6 +805,23 @@ extern "C" int mdgpu_dump_size(int level, int nmols, int nmols_r)
    return dump_layout(level, nmols, nmols_r, L);
 }
 
+extern "C" mdgpu_status mdgpu_md_set_state(mdgpu_ctx *c, const double *c_of_m, const double *mom,
+                                           const double *quat, const double *amom)
+{
+   if (!c) return MDGPU_E_ARG;
+   if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
+   MdDev &D = c->md;
+   cudaStream_t st = c->stream;
+   const size_t M = c->nmols, Q = c->mdh.nmols_r;
+   // into the buffers a captured step reads: the capture stays valid
+   if (c_of_m) CK(cudaMemcpyAsync(D.cofm.p, c_of_m, 3 * M * sizeof(double), cudaMemcpyHostToDevice, st));
+   if (mom) CK(cudaMemcpyAsync(D.mom.p, mom, 3 * M * sizeof(double), cudaMemcpyHostToDevice, st));
+   if (quat && Q) CK(cudaMemcpyAsync(D.quat.p, quat, 4 * Q * sizeof(double), cudaMemcpyHostToDevice, st));
+   if (amom && Q) CK(cudaMemcpyAsync(D.amom.p, amom, 4 * Q * sizeof(double), cudaMemcpyHostToDevice, st));
+   CK(cudaStreamSynchronize(st));
+   return MDGPU_OK;
+}
+
 extern "C" mdgpu_status mdgpu_md_get_state(mdgpu_ctx *c, double *c_of_m, double *mom, double *quat,
                                            double *amom)
 {

@@ -147,6 +147,15 @@ class MolecularDynamics:
                                                 _dp(e), rec.ctypes.data_as(C.POINTER(C.c_float))))
         return e[:nsteps], rec[:nrec]
 
+    def set_state(self, state: MDState) -> None:
+        """Replaces the dynamic state on the GPU (mdgpu_md_set_state)."""
+        cm = np.ascontiguousarray(state.c_of_m, np.float64)
+        mo = np.ascontiguousarray(state.mom, np.float64)
+        qu = np.ascontiguousarray(state.quat, np.float64)
+        am = np.ascontiguousarray(state.amom, np.float64)
+        self.ff._check(self.L.mdgpu_md_set_state(self.ff.ctx, _dp(cm), _dp(mo), _dp(qu) if self.nq else None,
+                                                 _dp(am) if self.nq else None))
+
     def state(self) -> MDState:
         sysm = self.ff.sysm
         cm, mo = np.zeros((sysm.nmols, 3)), np.zeros((sysm.nmols, 3))

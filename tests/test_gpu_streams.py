@@ -49,3 +49,25 @@ def test_single_step_calls_match_one_run():
     np.testing.assert_array_equal(s1.mom, s2.mom)
     np.testing.assert_array_equal(s1.quat, s2.quat)
     np.testing.assert_array_equal(s1.amom, s2.amom)
+
+
+def test_set_state_replays_the_same_trajectory():
+    """mdgpu_md_set_state puts a saved state back into the buffers the
+    captured step reads: the run from it repeats bit for bit."""
+    from moldy_gb300 import ForceField, system
+    from moldy_gb300.dynamics import MolecularDynamics, species_dynamics, thermal_state
+    sysm = system.water(nside=6, seed=3)
+    dyn = species_dynamics(sysm, 0.001)
+    ff = ForceField(sysm, precision="mixed")
+    md = MolecularDynamics(ff, dyn, thermal_state(sysm, dyn, 300.0, seed=4))
+    md.run(5)
+    s5 = md.state()
+    e1 = md.run(6)
+    s11 = md.state()
+    md.set_state(s5)
+    e2 = md.run(6)
+    s11b = md.state()
+    ff.close()
+    np.testing.assert_array_equal(e1, e2)
+    np.testing.assert_array_equal(s11.c_of_m, s11b.c_of_m)
+    np.testing.assert_array_equal(s11.amom, s11b.amom)
