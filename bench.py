@@ -179,6 +179,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def reduce_max(x, dist=None, device="cpu"):
+    """The maximum of x over the ranks of the default process group (x itself
+    without one): the slowest replica's time, which the job's rate uses."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def traffic_from_profiles():
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
@@ -250,10 +260,7 @@ def run_gpu(args):
         return sum(ms) / nsteps, wall
 
     def max_over_ranks(x):
-        t = torch.tensor([x], device=dev)
-        if dist is not None:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, dist, dev)
 
     # ---- the headline: MD steps on the GPU, mixed form ----------------------
     md = MolecularDynamics(ff, dyn, state0)
