@@ -795,20 +795,24 @@ mdgpu_status ks_prepare(mdgpu_ctx *c)
 
 // Chunks of the structure-factor pass and k-splits of the force pass, sized
 // for about two waves of resident threads; ipt items per thread in the
-// former, spt sites per thread in the latter.
+// former, spt sites per thread in the latter.  Chunks hold 64 sites or more
+// (their FP32 partial sums stay short: a crystal's near-cancelling
+// structure factor lost accuracy with 256-site chunks), splits 32 items or
+// more (below that the per-block set-up, tables and staging, outweighs the
+// extra parallelism).
 KsShape ks_shape(int N, int nitems, int ipt, int spt)
 {
    KsShape s;
    const long long target = 152LL * 2048;          // resident threads on a full GB300
    const long long sf_threads = (nitems + ipt - 1) / ipt, f_threads = (N + spt - 1) / spt;
    long long ch = target / (sf_threads > 0 ? sf_threads : 1);
-   long long max_ch = (N + 63) / 64;
+   long long max_ch = (N + 63) / 64;                // chunks of at least 64 sites
    if (ch < 1) ch = 1;
    if (ch > max_ch) ch = max_ch;
    s.chunk = (int)(((N + ch - 1) / ch + 31) / 32 * 32);
    s.chunks = (N + s.chunk - 1) / s.chunk;
    long long sp = (2 * target) / (f_threads > 0 ? f_threads : 1);
-   long long max_sp = (nitems + 7) / 8;
+   long long max_sp = (nitems + 31) / 32;           // at least 32 items per block
    if (sp < 1) sp = 1;
    if (sp > max_sp) sp = max_sp;
    if (sp < 1) sp = 1;
