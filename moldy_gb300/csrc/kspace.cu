@@ -314,28 +314,47 @@ __device__ __forceinline__ double bsum(double v, double *sh)
    return s;
 }
 
+// Per k: S(k) over the structure-factor chunks, then the energy, stress and
+// force coefficients.  A block takes KR_K consecutive k (one per lane) and
+// spreads the chunks over its KR_W warps (chunks w, w + KR_W, ... in warp w:
+// coalesced rows), whose sums warp 0 adds in warp order.
+constexpr int KR_K = 32, KR_W = 8;
+
 template <bool MIXED>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(KR_K * KR_W)
 k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__restrict__ p64,
           const double *__restrict__ kvec /*[3][nk]*/, const double *__restrict__ coeff,
           const double *__restrict__ coeff2, float4 *__restrict__ kd32, double4 *__restrict__ kd64,
           double *__restrict__ blk)
 {
-   __shared__ double red[32];
-   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+   __shared__ double sC[KR_W][KR_K], sS[KR_W][KR_K];
+   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+   const int k = blockIdx.x * KR_K + lane;
+   {
+      double C = 0.0, S = 0.0;
+      if (k < nk)
+         for (int c = w; c < nchunks; c += KR_W) {
+            if (MIXED) {
+               const float2 v = p32[(size_t)c * nk + k];
+               C += (double)v.x;
+               S += (double)v.y;
+            } else {
+               const double2 v = p64[(size_t)c * nk + k];
+               C += v.x;
+               S += v.y;
+            }
+         }
+      sC[w][lane] = C;
+      sS[w][lane] = S;
+   }
+   __syncthreads();
+   if (w != 0) return;
    double pek = 0, st[6] = {0, 0, 0, 0, 0, 0};
    if (k < nk) {
       double C = 0.0, S = 0.0;
-      for (int c = 0; c < nchunks; c++) {
-         if (MIXED) {
-            const float2 v = p32[(size_t)c * nk + k];
-            C += (double)v.x;
-            S += (double)v.y;
-         } else {
-            const double2 v = p64[(size_t)c * nk + k];
-            C += v.x;
-            S += v.y;
-         }
+      for (int i = 0; i < KR_W; i++) {
+         C += sC[i][lane];
+         S += sS[i][lane];
       }
       const double kx = kvec[k], ky = kvec[nk + k], kz = kvec[2 * nk + k];
       const double cf = coeff[k], cf2 = coeff2[k];
@@ -352,11 +371,16 @@ k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__
       else
          kd64[k] = make_double4(A, B, kz, 0.0);
    }
-   double s = bsum(pek, red);
-   if (threadIdx.x == 0) blk[blockIdx.x * 8] = s;
-   for (int i = 0; i < 6; i++) {
-      s = bsum(st[i], red);
-      if (threadIdx.x == 0) blk[blockIdx.x * 8 + 1 + i] = s;
+   // the block's energy and stress: warp 0 holds them all
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) {
+      pek += __shfl_down_sync(0xffffffffu, pek, o);
+#pragma unroll
+      for (int i = 0; i < 6; i++) st[i] += __shfl_down_sync(0xffffffffu, st[i], o);
+   }
+   if (lane == 0) {
+      blk[blockIdx.x * 8] = pek;
+      for (int i = 0; i < 6; i++) blk[blockIdx.x * 8 + 1 + i] = st[i];
    }
 }
 
@@ -873,7 +897,8 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       }
    }
    CK(cudaGetLastError());
-   const int nbk = (nk + 255) / 256;
+   // blocks of the per-k reduction: KR_K k each (the framework form: 256)
+   const int nbk = nf > 0 ? (nk + 255) / 256 : (nk + KR_K - 1) / KR_K;
    CK(d.blk.ensure((size_t)nbk * 8));
    phase_mark(c, MDGPU_PH_KREDUCE);
    if (nf > 0) {
@@ -890,10 +915,10 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       }
       c->launches += 2;
    } else if (mixed) {
-      k_kreduce<true><<<nbk, 256, 0, st>>>(nk, sh.chunks, d.part32.p, nullptr, d.kz64.p, d.coeff.p,
+      k_kreduce<true><<<nbk, KR_K * KR_W, 0, st>>>(nk, sh.chunks, d.part32.p, nullptr, d.kz64.p, d.coeff.p,
                                            d.coeff2.p, d.kdat32.p, nullptr, d.blk.p);
    } else {
-      k_kreduce<false><<<nbk, 256, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
+      k_kreduce<false><<<nbk, KR_K * KR_W, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
                                             d.coeff2.p, nullptr, d.kdat64.p, d.blk.p);
    }
    k_kfinal<<<1, 256, 0, st>>>(d.blk.p, nbk, out);
