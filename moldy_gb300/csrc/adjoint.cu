@@ -483,7 +483,9 @@ static mdgpu_status run_adjoint(mdgpu_ctx *c, const mdgpu_params *prm, const dou
    CK(cudaMemsetAsync(a.scal.p, 0, 4 * sizeof(double), st));
    // forward: forces and energies, leaving the binned sites, the phases and
    // the structure-factor partials in place for the backward passes
+   c->ks_all_sites = true;   // the backward passes read every site's phases
    s = mdgpu_forces_device(c, h, c->site.p, c->cofm_in.p, c->force.p, c->small.p, c->small.p + 2);
+   c->ks_all_sites = false;
    if (s) return s;
    const bool mixed = c->prec == MDGPU_MIXED;
    if (mixed) CK(a.res32.ensure(N)); else CK(a.res64.ensure(N));

@@ -46,11 +46,12 @@ __device__ __forceinline__ unsigned long long to_fixed64(double s)
 __device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c);
 
 // Per-site records are written in link-cell order (slot i holds site
-// sorted[i]): the structure-factor chunks are then compact regions of the
-// cell, close to neutral, so their FP32 partial sums stay small even where
-// the full sum cancels (an ionic crystal listed species by species would
-// otherwise give chunks of a single charge sign).
-__global__ void k_prep(int N, const int *__restrict__ sorted, const double *__restrict__ site,
+// sorted[i]; ns is the stride of the site array): the structure-factor
+// chunks are then compact regions of the cell, close to neutral, so their
+// FP32 partial sums stay small even where the full sum cancels (an ionic
+// crystal listed species by species would otherwise give chunks of a
+// single charge sign).
+__global__ void k_prep(int N, int ns, const int *__restrict__ sorted, const double *__restrict__ site,
                        const double *__restrict__ chg, double hi0, double hi1, double hi2,
                        double hi3, double hi4, double hi5, double hi6, double hi7, double hi8,
                        int mixed, int4 *__restrict__ ph32, float2 *__restrict__ z32,
@@ -60,7 +61,7 @@ __global__ void k_prep(int N, const int *__restrict__ sorted, const double *__re
    const int i = blockIdx.x * blockDim.x + threadIdx.x;   // slot
    if (i >= N) return;
    const int si = sorted[i];                                // site
-   double x = site[si], y = site[N + si], z = site[2 * N + si];
+   double x = site[si], y = site[ns + si], z = site[2 * (size_t)ns + si];
    double s0 = hi0 * x + hi1 * y + hi2 * z;
    double s1 = hi3 * x + hi4 * y + hi5 * z;
    double s2 = hi6 * x + hi7 * y + hi8 * z;
@@ -558,20 +559,23 @@ k_force32(const int4 *__restrict__ item, const int *__restrict__ item_k0,
    }
    // site oi's partial goes to row oi - obase of [3][N] (obase = 0 except
    // for a subset of sites held compactly)
+   // rows by slot (obase < 0) or by site - obase
    double *dst = fpart + (size_t)blockIdx.y * 3 * N;
    if (live0) {
       const int oi = sorted[i0];   // slot i0 holds site oi
       const double q = chg[oi];
-      dst[oi - obase] = q * ((double)fxa - (double)exa);
-      dst[N + oi - obase] = q * ((double)fya - (double)eya);
-      dst[2 * N + oi - obase] = q * ((double)fza - (double)eza);
+      const int r = obase < 0 ? i0 : oi - obase;
+      dst[r] = q * ((double)fxa - (double)exa);
+      dst[N + r] = q * ((double)fya - (double)eya);
+      dst[2 * N + r] = q * ((double)fza - (double)eza);
    }
    if (live1) {
       const int oi = sorted[i1];
       const double q = chg[oi];
-      dst[oi - obase] = q * ((double)fxb - (double)exb);
-      dst[N + oi - obase] = q * ((double)fyb - (double)eyb);
-      dst[2 * N + oi - obase] = q * ((double)fzb - (double)ezb);
+      const int r = obase < 0 ? i1 : oi - obase;
+      dst[r] = q * ((double)fxb - (double)exb);
+      dst[N + r] = q * ((double)fyb - (double)eyb);
+      dst[2 * N + r] = q * ((double)fzb - (double)ezb);
    }
 }
 
@@ -634,9 +638,10 @@ k_force64(const int4 *__restrict__ item, const int *__restrict__ item_k0,
       const int oi = sorted[i];   // slot i holds site oi
       const double q = chg[oi];
       double *dst = fpart + (size_t)blockIdx.y * 3 * N;
-      dst[oi - obase] = q * Fx;
-      dst[N + oi - obase] = q * Fy;
-      dst[2 * N + oi - obase] = q * Fz;
+      const int r = obase < 0 ? i : oi - obase;   // rows by slot (obase < 0) or by site - obase
+      dst[r] = q * Fx;
+      dst[N + r] = q * Fy;
+      dst[2 * N + r] = q * Fz;
    }
 }
 
@@ -768,6 +773,85 @@ __global__ void k_fsum(int n3, int nsplit, const double *__restrict__ fpart, dou
    force[i] = accumulate ? force[i] + s : s;
 }
 
+// force[comp][slots[j]] += sum over splits of fpart[split][comp][j], j < n
+// (partials by slot of the charged-site list; the other sites get nothing)
+__global__ void k_fsum_slots(int n, int N, int nsplit, const double *__restrict__ fpart,
+                             const int *__restrict__ slots, double *__restrict__ force)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= 3 * n) return;
+   const int comp = i / n, j = i - comp * n;
+   double s = 0.0;
+   for (int k = 0; k < nsplit; k++) s += fpart[(size_t)k * 3 * n + i];
+   force[(size_t)comp * N + slots[j]] += s;
+}
+
+// Compaction of the link-cell order to the charged sites: per block of
+// 1024 slots an exclusive scan of the flags (charge != 0), the block totals
+// scanned by one block, then each charged slot's site written to its place.
+__device__ __forceinline__ int block_scan_1024(int v, int *sh)   // exclusive, blockDim 1024
+{
+   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+   int x = v;
+#pragma unroll
+   for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+   }
+   if (lane == 31) sh[w] = x;
+   __syncthreads();
+   if (w == 0) {
+      int t = sh[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+         const int y = __shfl_up_sync(0xffffffffu, t, o);
+         if (lane >= o) t += y;
+      }
+      sh[lane] = t;   // inclusive over warps
+   }
+   __syncthreads();
+   return x - v + (w > 0 ? sh[w - 1] : 0);
+}
+
+__global__ void __launch_bounds__(1024) k_kflag_scan(int N, const int *__restrict__ sorted,
+                                                     const double *__restrict__ chg, int *__restrict__ ex,
+                                                     int *__restrict__ bsum)
+{
+   __shared__ int sh[32];
+   const int i = blockIdx.x * 1024 + threadIdx.x;
+   const int f = (i < N && chg[sorted[i]] != 0.0) ? 1 : 0;
+   const int e = block_scan_1024(f, sh);
+   if (i < N) ex[i] = e;
+   if (threadIdx.x == 1023) bsum[blockIdx.x] = e + f;
+}
+
+__global__ void __launch_bounds__(1024) k_kbsum_scan(int nb, int *__restrict__ bsum)
+{
+   __shared__ int sh[32];
+   __shared__ int carry;
+   if (threadIdx.x == 0) carry = 0;
+   __syncthreads();
+   for (int b0 = 0; b0 < nb; b0 += 1024) {
+      const int i = b0 + threadIdx.x;
+      const int v = i < nb ? bsum[i] : 0;
+      const int e = block_scan_1024(v, sh);
+      const int c0 = carry;
+      __syncthreads();
+      if (i < nb) bsum[i] = c0 + e;
+      if (threadIdx.x == 1023) carry = c0 + e + v;
+      __syncthreads();
+   }
+}
+
+__global__ void k_kcompact(int N, const int *__restrict__ sorted, const double *__restrict__ chg,
+                           const int *__restrict__ ex, const int *__restrict__ bsum, int *__restrict__ slots)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= N) return;
+   const int si = sorted[i];
+   if (chg[si] != 0.0) slots[bsum[i >> 10] + ex[i]] = si;
+}
+
 // -------------------------------------------------------------- host side
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
 
@@ -861,13 +945,45 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    }
    double hinv[9];
    memcpy(hinv, kl.hinv, sizeof hinv);
-   phase_mark(c, MDGPU_PH_KPREP);
-   k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, c->rd.sorted.p, d_site, c->rd.chg.p, hinv[0], hinv[1], hinv[2], hinv[3],
-                                           hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], mixed ? 1 : 0,
-                                           d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
-   CK(cudaGetLastError());
-   KsShape sh = mixed ? ks_shape(N, ni, 1, 2) : ks_shape(N, ni, 1, 1);
    const int fw0 = c->fw_site0, nf = N - fw0;   // framework sites, if any
+   phase_mark(c, MDGPU_PH_KPREP);
+   // The passes run over the charged sites only (a site without charge adds
+   // nothing to S(k) and has no k-space force; rigid water's O sites are a
+   // quarter of the work), kept in link-cell order -- except with a
+   // framework molecule and under the adjoint, which read every site.
+   const bool compact = nf <= 0 && !c->ks_all_sites;
+   int Nk = N;
+   const int *slots = c->rd.sorted.p;
+   if (compact) {
+      if (c->ncharged_gen != c->gen) {
+         int n = 0;
+         for (double q : c->chg) n += q != 0.0;
+         c->ncharged = n;
+         c->ncharged_gen = c->gen;
+      }
+      Nk = c->ncharged;
+      if (Nk == 0) {
+         if (join) CK(cudaStreamWaitEvent(st, join, 0));
+         if (!accumulate) CK(cudaMemsetAsync(d_force, 0, 3 * (size_t)N * sizeof(double), st));
+         return MDGPU_OK;
+      }
+      const int nb = (N + 1023) / 1024;
+      CK(d.kslots.ensure(N));   // room for every site whatever the device-side count
+      CK(d.kscan.ensure(N));
+      CK(d.kbsum.ensure(nb));
+      k_kflag_scan<<<nb, 1024, 0, st>>>(N, c->rd.sorted.p, c->rd.chg.p, d.kscan.p, d.kbsum.p);
+      k_kbsum_scan<<<1, 1024, 0, st>>>(nb, d.kbsum.p);
+      k_kcompact<<<(N + 255) / 256, 256, 0, st>>>(N, c->rd.sorted.p, c->rd.chg.p, d.kscan.p, d.kbsum.p,
+                                                  d.kslots.p);
+      CK(cudaGetLastError());
+      c->launches += 3;
+      slots = d.kslots.p;
+   }
+   k_prep<<<(Nk + 255) / 256, 256, 0, st>>>(Nk, N, slots, d_site, c->rd.chg.p, hinv[0], hinv[1], hinv[2],
+                                            hinv[3], hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], mixed ? 1 : 0,
+                                            d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
+   CK(cudaGetLastError());
+   KsShape sh = mixed ? ks_shape(Nk, ni, 1, 2) : ks_shape(Nk, ni, 1, 1);
    if (nf > 0) {
       CK(d.fslot.ensure(nf));
       if (mixed) CK(d.phf32.ensure(N)); else CK(d.phf64b.ensure(N));
@@ -879,7 +995,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    const dim3 gs((ni + 127) / 128, sh.chunks);
    if (mixed) {
       CK(d.part32.ensure((size_t)sh.chunks * nk));
-      k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, N, sh.chunk, nk, d.part32.p,
+      k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, Nk, sh.chunk, nk, d.part32.p,
                                    &out->err);
       if (nf > 0) {
          CK(d.partf32.ensure((size_t)sh.chunks * nk));
@@ -888,7 +1004,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       }
    } else {
       CK(d.part64.ensure((size_t)sh.chunks * nk));
-      k_sfac64<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, d.ph64b.p, d.z64.p, N, sh.chunk,
+      k_sfac64<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, d.ph64b.p, d.z64.p, Nk, sh.chunk,
                                    nk, d.part64.p);
       if (nf > 0) {
          CK(d.partf64.ensure((size_t)sh.chunks * nk));
@@ -923,21 +1039,27 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    }
    k_kfinal<<<1, 256, 0, st>>>(d.blk.p, nbk, out);
    CK(cudaGetLastError());
-   CK(d.fpart.ensure((size_t)sh.splits * 3 * N));
+   CK(d.fpart.ensure((size_t)sh.splits * 3 * Nk));
    phase_mark(c, MDGPU_PH_KFORCE);
-   dim3 gf((N + 255) / 256, sh.splits);
+   dim3 gf((Nk + 255) / 256, sh.splits);
+   const int obase = compact ? -1 : 0;   // partial rows by slot of the charged list, or by site
    if (mixed)
       k_force32<<<gf, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
-                                           d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, c->rd.sorted.p, N, 0,
+                                           d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, slots, Nk, obase,
                                            (float)kl.dkz, d.fpart.p);
    else
       k_force64<<<gf, 256, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, sh.per_split,
-                                    d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, c->rd.sorted.p, N, 0,
+                                    d.kdat64.p, d.ph64a.p, d.ph64b.p, d.z64.p, c->rd.chg.p, slots, Nk, obase,
                                     d.fpart.p);
    CK(cudaGetLastError());
    phase_mark(c, MDGPU_PH_FINAL);
    if (join) CK(cudaStreamWaitEvent(st, join, 0));
-   k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, sh.splits, d.fpart.p, d_force, accumulate ? 1 : 0);
+   if (compact) {
+      if (!accumulate) CK(cudaMemsetAsync(d_force, 0, 3 * (size_t)N * sizeof(double), st));
+      k_fsum_slots<<<(3 * Nk + 255) / 256, 256, 0, st>>>(Nk, N, sh.splits, d.fpart.p, slots, d_force);
+   } else {
+      k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, sh.splits, d.fpart.p, d_force, accumulate ? 1 : 0);
+   }
    CK(cudaGetLastError());
    if (nf > 0) {
       // the framework sites' framework-framework k-space forces, taken off

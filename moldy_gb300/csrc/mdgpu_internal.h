@@ -159,6 +159,9 @@ struct KsDev {
    DBuf<float4> kdatf32;
    DBuf<double4> kdatf64;
    DBuf<double> fpartf;
+   // charged sites only (a site without charge adds nothing to S(k) and
+   // gets no k-space force): their slots in link-cell order
+   DBuf<int> kslots, kscan, kbsum;
 };
 
 // Buffers of the adjoint (parameter-gradient) passes.
@@ -270,6 +273,11 @@ struct mdgpu_ctx {
    mdgpu_info info{};
    int64_t launches = 0;
    bool timing = false;
+   // the k-space passes run over every site, not only the charged ones
+   // (the adjoint's backward passes read every site's phases)
+   bool ks_all_sites = false;
+   uint64_t ncharged_gen = 0;       // configuration the count below is for
+   int ncharged = 0;                // sites with a nonzero charge
    cudaEvent_t ev[MDGPU_NPHASES + 1] = {};
    // second (high-priority) stream: the k-space passes run on it beside
    // the pair kernel

@@ -27,7 +27,7 @@
 
 namespace mdgpu {
 // kernels of the reciprocal-space pass (kspace.cu)
-__global__ void k_prep(int N, const int *sorted, const double *site, const double *chg, double hi0,
+__global__ void k_prep(int N, int ns, const int *sorted, const double *site, const double *chg, double hi0,
                        double hi1, double hi2, double hi3, double hi4, double hi5, double hi6,
                        double hi7, double hi8, int mixed, int4 *ph32, float2 *z32, float2 *zp32,
                        ulonglong2 *ph64a, ulonglong2 *ph64b, double2 *z64);
@@ -249,7 +249,7 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    const int N = nsites;
    // site order: as given (no link-cell binning in this variant)
    k_iota<<<(N + 255) / 256, 256, 0, st>>>(N, sorted);
-   k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, sorted, d_site, d_chg, hinv[0], hinv[1], hinv[2], hinv[3],
+   k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, N, sorted, d_site, d_chg, hinv[0], hinv[1], hinv[2], hinv[3],
                                            hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], 1, ph, z, zp,
                                            nullptr, nullptr, nullptr);
    int chunks = (N + 63) / 64;

@@ -16,7 +16,7 @@ The framework fixture (md_waterwall) holds rigid water over a fixed,
 charged framework molecule: the reference zeroes the framework's momentum
 after each step's kicks (src/accel.c:748-755).
 
-usage: python tests/golden/make_md_golden.py [--skip-drift] [--only NAME]
+usage: python tests/golden/make_md_golden.py [--skip-drift] [--only NAME | --only drift-extra]
 """
 import os
 import subprocess
@@ -58,6 +58,17 @@ def main():
     ww = S.water_on_framework()
     if only in (None, "md_waterwall"):
         save("md_waterwall", ww, *case(ww, 0.001, 300.0, 9, 30), 300.0, 9)
+    if only == "drift-extra":
+        # two more independent thermal starts of each drift run: the drift of
+        # a 10^4-step run is a noisy quantity, compared as a mean over starts
+        w2 = S.water(nside=8, seed=11)
+        for strict in (False, True):
+            s = dataclasses.replace(w2, control=dataclasses.replace(w2.control, strict_cutoff=strict))
+            for tag, seed in (("b", 22), ("c", 32)):
+                dyn, st, rec, fin, sec = case(s, 0.001, 300.0, seed, 10000)
+                save("md_drift_water2048" + ("_strict" if strict else "") + "_" + tag, s, dyn, st, rec, fin, sec,
+                     300.0, seed)
+        return
     if only is not None:
         return
     w = S.water(nside=6, seed=3)

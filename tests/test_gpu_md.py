@@ -80,36 +80,46 @@ def test_md_run_needs_init():
     ff.close()
 
 
-DRIFT = ["md_drift_water2048", "md_drift_water2048_strict", "md_drift_argon500"]
+DRIFT = {
+    "water2048": ["md_drift_water2048", "md_drift_water2048_b", "md_drift_water2048_c"],
+    "water2048_strict": ["md_drift_water2048_strict", "md_drift_water2048_strict_b", "md_drift_water2048_strict_c"],
+    "argon500": ["md_drift_argon500"],
+}
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", DRIFT)
-def test_energy_drift_no_worse_than_reference(name, prec):
-    """The whole reference run (10^4 steps of water, 10^3 of argon) on the
-    GPU from the same start: the least-squares drift of the conserved
-    quantity and its fluctuation about the trend are no larger than the
-    reference's own, within a margin for two chaotic trajectories of the
-    same dynamics.  The trajectories part within a few hundred steps, after
-    which each run's drift is one sample of the same random process (in
-    lazy link-cell mode, pairs beyond the cutoff enter and leave the
-    evaluated set at random; measured: the FP64 GPU run, the reference's own
-    arithmetic, drifts 2.2x the reference's figure on the lazy water run and
-    2.1x on the strict one), hence a factor 3."""
-    if not os.path.exists(os.path.join(GOLDEN, name + ".npz")):
-        pytest.skip("drift fixture not generated")
+@pytest.mark.parametrize("case", sorted(DRIFT))
+def test_energy_drift_no_worse_than_reference(case, prec):
+    """Whole reference runs (10^4 steps of water from three thermal starts,
+    10^3 of argon) on the GPU from the same starts: the least-squares drift
+    of the conserved quantity and its fluctuation about the trend, averaged
+    over the starts, are no larger than the reference's own, within a
+    margin.  The trajectories part within a few hundred steps, after which
+    each run's drift is one sample of a noisy quantity (in lazy link-cell
+    mode pairs beyond the cutoff enter and leave the evaluated set at
+    random; with strict cut-offs the slope of a 10^4-step run is dominated
+    by slow fluctuations of the conserved quantity): single runs of the
+    reference's own arithmetic (the FP64 GPU form) measured 2.1-2.2x the
+    reference's figure, hence the average over starts and a factor 2.5."""
     from moldy_gb300.dynamics import drift_per_ns
-    sysm, z, e, st, st1 = _run(name, prec)
-    rec = z["ref_rec"]
-    dt = float(z["md_step"])
-    H_ref, H = rec[:, 0], e.sum(1)
-    d_ref = drift_per_ns(np.stack([H_ref, 0 * H_ref, 0 * H_ref, 0 * H_ref], 1), dt)
-    d_gpu = drift_per_ns(e, dt)
-    t = np.arange(len(H))
-    fl_ref = np.std(H_ref - np.polyval(np.polyfit(t, H_ref, 1), t))
-    fl_gpu = np.std(H - np.polyval(np.polyfit(t, H, 1), t))
-    ke = float(np.mean(e[:, 2] + e[:, 3]))
-    # margin: 3x the reference's figure plus 1e-5 of the kinetic energy
+    names = [n for n in DRIFT[case] if os.path.exists(os.path.join(GOLDEN, n + ".npz"))]
+    if not names:
+        pytest.skip("drift fixtures not generated")
+    d_ref, d_gpu, fl_ref, fl_gpu, kes, span = [], [], [], [], [], 0.0
+    for name in names:
+        sysm, z, e, st, st1 = _run(name, prec)
+        rec = z["ref_rec"]
+        dt = float(z["md_step"])
+        H_ref, H = rec[:, 0], e.sum(1)
+        d_ref.append(abs(drift_per_ns(np.stack([H_ref, 0 * H_ref, 0 * H_ref, 0 * H_ref], 1), dt)))
+        d_gpu.append(abs(drift_per_ns(e, dt)))
+        t = np.arange(len(H))
+        fl_ref.append(np.std(H_ref - np.polyval(np.polyfit(t, H_ref, 1), t)))
+        fl_gpu.append(np.std(H - np.polyval(np.polyfit(t, H, 1), t)))
+        kes.append(float(np.mean(e[:, 2] + e[:, 3])))
+        span = len(H) * dt * 1e-3
+    ke = float(np.mean(kes))
+    # margin: 2.5x the reference's mean plus 1e-5 of the kinetic energy
     # over the run
-    assert abs(d_gpu) <= 3.0 * abs(d_ref) + 1e-5 * ke / (len(H) * dt * 1e-3), (d_gpu, d_ref)
-    assert fl_gpu <= 3.0 * fl_ref + 1e-6 * ke, (fl_gpu, fl_ref)
+    assert np.mean(d_gpu) <= 2.5 * np.mean(d_ref) + 1e-5 * ke / span, (d_gpu, d_ref)
+    assert np.mean(fl_gpu) <= 2.5 * np.mean(fl_ref) + 1e-6 * ke, (fl_gpu, fl_ref)
