@@ -385,25 +385,30 @@ k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__
    }
 }
 
-// Per-block energy/stress partials summed in a fixed order by one block of
-// 256 threads (launch with 256): thread t takes blocks t, t+256, ..., then a
-// fixed-shape tree.
-__global__ void __launch_bounds__(256) k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *out)
+// Per-block energy/stress partials summed in a fixed order by one block
+// (any multiple of 32 threads up to 1024): thread t takes blocks t, t + T,
+// ..., then fixed-shape warp and cross-warp trees.
+__global__ void __launch_bounds__(1024) k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *out)
 {
-   __shared__ double sh[7][256];
-   const int t = threadIdx.x;
+   __shared__ double sh[32][8];
+   const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
    double v[7] = {0, 0, 0, 0, 0, 0, 0};
    for (int b = t; b < nblocks; b += blockDim.x)
       for (int k = 0; k < 7; k++) v[k] += blk[b * 8 + k];
-   for (int k = 0; k < 7; k++) sh[k][t] = v[k];
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+      for (int k = 0; k < 7; k++) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+   if (lane == 0)
+      for (int k = 0; k < 7; k++) sh[w][k] = v[k];
    __syncthreads();
-   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (t < w)
-         for (int k = 0; k < 7; k++) sh[k][t] += sh[k][t + w];
-      __syncthreads();
-   }
-   if (t < 7) {
-      if (t == 0) out->pe_k = sh[0][0]; else out->st_k[t - 1] = sh[t][0];
+   if (w != 0) return;
+   for (int k = 0; k < 7; k++) v[k] = lane < nw ? sh[lane][k] : 0.0;
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+      for (int k = 0; k < 7; k++) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+   if (lane == 0) {
+      out->pe_k = v[0];
+      for (int k = 1; k < 7; k++) out->st_k[k - 1] = v[k];
    }
 }
 
@@ -1037,7 +1042,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       k_kreduce<false><<<nbk, KR_K * KR_W, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
                                             d.coeff2.p, nullptr, d.kdat64.p, d.blk.p);
    }
-   k_kfinal<<<1, 256, 0, st>>>(d.blk.p, nbk, out);
+   k_kfinal<<<1, 1024, 0, st>>>(d.blk.p, nbk, out);
    CK(cudaGetLastError());
    CK(d.fpart.ensure((size_t)sh.splits * 3 * Nk));
    phase_mark(c, MDGPU_PH_KFORCE);
