@@ -360,16 +360,24 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh)
 
 constexpr int PAIR_WARPS = 8;   // warps per block
 
-// Per-warp shared rows of the stencil walk.
+// Per-warp shared rows of the stencil walk (32 WALK_E entries), and the
+// stencil's cell-offset vectors (global, read by entry).
+constexpr int WALK_E = 4;   // stencil entries per lane in one pass of the walk
+
 struct WalkRows {
    int *inc, *jb, *info;
-   float4 *oh, *ol;
+   const float4 *oh, *ol;
 };
 
 // Walks the full stencil of home slot p (in cell c) with one warp and calls
-// visit(j, k, kimg) for every candidate slot j, the home site itself
-// excluded: k is the lane whose stencil entry j belongs to (its cell-offset
-// vectors are rows.oh[k], rows.ol[k]) and kimg the periodic image code.
+// visit(j, e, kimg) for every candidate slot j, the home site itself
+// excluded: e is the stencil entry j belongs to (its cell-offset vectors are
+// rows.oh[e], rows.ol[e]) and kimg the periodic image code.  A pass takes
+// 32 WALK_E stencil entries (WALK_E consecutive ones per lane), lays their
+// cells' slot ranges end to end by a warp prefix sum, and deals the
+// candidates out 32 at a time; each lane finds its candidate's entry by
+// binary search over the scanned counts.  With a few sites per cell, wider
+// passes keep the lanes busier (fewer, fuller rounds).
 template <bool MIXED, class Visit>
 __device__ __forceinline__ void walk_stencil(const RsParams &P, int p, int c, int lane,
                                              const int *__restrict__ cell_start,
@@ -378,39 +386,42 @@ __device__ __forceinline__ void walk_stencil(const RsParams &P, int p, int c, in
                                              const float4 *__restrict__ off_lo, const WalkRows &rows,
                                              Visit &&visit)
 {
+   (void)off_hi;
+   (void)off_lo;
    const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
-   for (int base = 0; base < P.nfull; base += 32) {
-      // lane `lane` takes stencil entry base + lane
-      const int e = base + lane;
-      int cnt = 0, jb = 0, info = 0;
-      float4 oh = make_float4(0, 0, 0, 0), ol = oh;
-      if (e < P.nfull) {
-         const int4 d = __ldg(&full[e]);
-         int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
-         const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
-         const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
-         const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
-         bx -= ix * P.nx;
-         by -= iy * P.ny;
-         bz -= iz * P.nz;
-         const int cb = bz + P.nz * (by + P.ny * bx);
-         const int j0 = __ldg(&cell_start[cb]);
-         cnt = __ldg(&cell_start[cb + 1]) - j0;
-         jb = j0;
-         info = (9 * (ix + 1) + 3 * (iy + 1) + (iz + 1)) | (d.w << 8);
-         if (MIXED) {
-            oh = __ldg(&off_hi[e]);
-            ol = __ldg(&off_lo[e]);
+   for (int base = 0; base < P.nfull; base += 32 * WALK_E) {
+      int cnt[WALK_E], jb[WALK_E], info[WALK_E], tot = 0;
+#pragma unroll
+      for (int u = 0; u < WALK_E; u++) {
+         const int e = base + lane * WALK_E + u;
+         cnt[u] = jb[u] = info[u] = 0;
+         if (e < P.nfull) {
+            const int4 d = __ldg(&full[e]);
+            int bx = cx + d.x, by = cy + d.y, bz = cz + d.z;
+            const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
+            const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
+            const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
+            bx -= ix * P.nx;
+            by -= iy * P.ny;
+            bz -= iz * P.nz;
+            const int cb = bz + P.nz * (by + P.ny * bx);
+            const int j0 = __ldg(&cell_start[cb]);
+            cnt[u] = __ldg(&cell_start[cb + 1]) - j0;
+            jb[u] = j0;
+            info[u] = (9 * (ix + 1) + 3 * (iy + 1) + (iz + 1)) | (d.w << 8);
          }
+         tot += cnt[u];
       }
-      const int inc = warp_incl_scan(cnt);
-      const int T = __shfl_sync(0xffffffffu, inc, 31);
-      rows.inc[lane] = inc;
-      rows.jb[lane] = jb - (inc - cnt);     // slot = jb[k] + candidate index
-      rows.info[lane] = info;
-      if (MIXED) {
-         rows.oh[lane] = oh;
-         rows.ol[lane] = ol;
+      const int linc = warp_incl_scan(tot);
+      const int T = __shfl_sync(0xffffffffu, linc, 31);
+      int run = linc - tot;   // candidates before this lane's entries
+#pragma unroll
+      for (int u = 0; u < WALK_E; u++) {
+         const int q = lane * WALK_E + u;
+         rows.jb[q] = jb[u] - run;    // slot = jb[q] + candidate index
+         run += cnt[u];
+         rows.inc[q] = run;
+         rows.info[q] = info[u];
       }
       __syncwarp();
       for (int r = 0; r < T; r += 32) {
@@ -418,11 +429,11 @@ __device__ __forceinline__ void walk_stencil(const RsParams &P, int p, int c, in
          if (idx < T) {
             int k = 0;
 #pragma unroll
-            for (int s = 16; s >= 1; s >>= 1)
+            for (int s = 16 * WALK_E; s >= 1; s >>= 1)
                if (rows.inc[k + s - 1] <= idx) k += s;
             const int j = rows.jb[k] + idx;
             const int inf = rows.info[k];
-            if (!((inf >> 8) && j == p)) visit(j, k, inf & 255);
+            if (!((inf >> 8) && j == p)) visit(j, base + k, inf & 255);
          }
       }
       __syncwarp();
@@ -442,7 +453,7 @@ __device__ __forceinline__ void pair_sep(const RsParams &P, int j, int k, int ki
 {
    if (MIXED) {
       const float4 xj = __ldg(&pos32[j]);
-      const float4 h4 = rows.oh[k], l4 = rows.ol[k];
+      const float4 h4 = __ldg(&rows.oh[k]), l4 = __ldg(&rows.ol[k]);
       rx = (h4.x + (xj.x - xi32.x)) + l4.x;
       ry = (h4.y + (xj.y - xi32.y)) + l4.y;
       rz = (h4.z + (xj.z - xi32.z)) + l4.z;
@@ -515,8 +526,7 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
    typedef typename std::conditional<MIXED, float, double>::type R;
    constexpr int NP = NPar<PT>::v;
    extern __shared__ __align__(16) unsigned char smem_raw[];
-   __shared__ int s_inc[PAIR_WARPS][32], s_jb[PAIR_WARPS][32], s_info[PAIR_WARPS][32];
-   __shared__ float4 s_oh[PAIR_WARPS][32], s_ol[PAIR_WARPS][32];
+   __shared__ int s_inc[PAIR_WARPS][32 * WALK_E], s_jb[PAIR_WARPS][32 * WALK_E], s_info[PAIR_WARPS][32 * WALK_E];
    R *pot_s = reinterpret_cast<R *>(smem_raw);
    const int npot = P.max_id * P.max_id;
    const R *potg = MIXED ? (const R *)(const void *)potg32 : (const R *)(const void *)potg64;
@@ -528,7 +538,7 @@ k_pairs(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ 
    const int N = P.nsites;
    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
    const int p = blockIdx.x * PAIR_WARPS + w;   // home slot of this warp
-   const WalkRows rows{s_inc[w], s_jb[w], s_info[w], s_oh[w], s_ol[w]};
+   const WalkRows rows{s_inc[w], s_jb[w], s_info[w], off_hi, off_lo};
    // per-lane partial sums: few terms each, then a warp tree reduction
    R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
    int nev = 0;                                  // evaluations by this lane
@@ -829,14 +839,13 @@ k_pairs_adj(RsParams P, AdjParams A, const int *__restrict__ cell_start,
    typedef typename std::conditional<MIXED, float, double>::type R;
    constexpr int NP = NPar<PT>::v;
    extern __shared__ double s_acc[];
-   __shared__ int s_inc[PAIR_WARPS][32], s_jb[PAIR_WARPS][32], s_info[PAIR_WARPS][32];
-   __shared__ float4 s_oh[PAIR_WARPS][32], s_ol[PAIR_WARPS][32];
+   __shared__ int s_inc[PAIR_WARPS][32 * WALK_E], s_jb[PAIR_WARPS][32 * WALK_E], s_info[PAIR_WARPS][32 * WALK_E];
    for (int q = threadIdx.x; q < A.nslot; q += blockDim.x) s_acc[q] = 0.0;
    __syncthreads();
    const R *pot = MIXED ? (const R *)(const void *)potg32 : (const R *)(const void *)potg64;
    const int N = P.nsites, T = P.max_id * P.max_id * NP;
    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-   const WalkRows rows{s_inc[w], s_jb[w], s_info[w], s_oh[w], s_ol[w]};
+   const WalkRows rows{s_inc[w], s_jb[w], s_info[w], off_hi, off_lo};
    const R alpha = MIXED ? (R)P.alphaf : (R)P.alpha, norm = MIXED ? (R)P.normf : (R)P.norm;
    const R cut100 = (R)P.cut100;
    for (int p0 = blockIdx.x * PAIR_WARPS; p0 < N; p0 += gridDim.x * PAIR_WARPS) {
@@ -956,7 +965,7 @@ k_rdf(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ sl
       const double *__restrict__ site, double rbin, int nbins, unsigned long long *__restrict__ counts)
 {
    __shared__ unsigned int hist[HIST_SMEM];
-   __shared__ int s_inc[PAIR_WARPS][32], s_jb[PAIR_WARPS][32], s_info[PAIR_WARPS][32];
+   __shared__ int s_inc[PAIR_WARPS][32 * WALK_E], s_jb[PAIR_WARPS][32 * WALK_E], s_info[PAIR_WARPS][32 * WALK_E];
    const int nh = P.max_id * P.max_id * nbins;
    const bool in_smem = nh <= HIST_SMEM;
    if (in_smem)
