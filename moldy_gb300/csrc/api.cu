@@ -472,11 +472,13 @@ mdgpu_status mdgpu_forces_device(mdgpu_ctx *c, const double *h, const double *d_
    // so their blocks fill the SMs as pair blocks retire; the k-space force
    // sum waits for the pair kernel's forces.  Phase timing keeps the order.
    const bool overlap = ew && !c->timing;
-   s = rs_launch(c, d_site, d_cofm, d_force, overlap, nullptr, 0, nullptr);
+   // overlap: the fork event is recorded as soon as the link-cell order is
+   // complete, so the per-slot records of the pair kernel are built beside
+   // the first k-space passes
+   s = rs_launch(c, d_site, d_cofm, d_force, overlap, nullptr, 0, overlap ? c->ev_fork : nullptr);
    if (s) return s;
    if (overlap) {
       cudaStream_t main = c->stream;
-      CKR(cudaEventRecord(c->ev_fork, main));
       CKR(cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
       s = rs_pairs(c, d_force, nullptr, 0);
       if (s) return s;

@@ -296,9 +296,11 @@ namespace mdgpu {
 mdgpu_status rs_prepare(mdgpu_ctx *c);   // upload geometry/system tables
 // cells_only: bin and order the sites (the k-space passes stream them in
 // link-cell order) without the pair kernel.
+// sorted_ready (or null): recorded on the stream once the link-cell order
+// (c->rd.sorted) is complete, before the per-slot records.
 mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
                        double *d_force, bool cells_only, unsigned long long *d_keys,
-                       int64_t key_cap, int64_t *d_keycount);
+                       int64_t key_cap, cudaEvent_t sorted_ready = nullptr);
 // Real-space adjoint over the slots binned by the last rs_launch: gradients
 // into c->ad.gq ([2][N], written) and c->ad.slots; residual weights from
 // c->ad.res64/res32 when loss.

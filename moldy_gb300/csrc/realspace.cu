@@ -1228,9 +1228,8 @@ mdgpu_status rs_rdf(mdgpu_ctx *c, double limit, int nbins)
 
 mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm, double *d_force,
                        bool cells_only, unsigned long long *d_keys, int64_t key_cap,
-                       int64_t *unused)
+                       cudaEvent_t sorted_ready)
 {
-   (void)unused;
    RsDev &d = c->rd;
    const RsGeom &g = c->rs;
    cudaStream_t st = c->stream;
@@ -1250,6 +1249,8 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
    CK(cudaMemsetAsync(d.cell_count.p, 0, (g.ncells + 1) * sizeof(int), st));
    k_scatter<<<(N + 255) / 256, 256, 0, st>>>(N, d.cell_of.p, d.cell_start.p, d.cell_count.p, d.sorted.p);
    k_cellsort<<<(g.ncells + 255) / 256, 256, 0, st>>>(g.ncells, d.cell_start.p, d.sorted.p);
+   // the link-cell order is all the k-space passes need from here
+   if (sorted_ready) CK(cudaEventRecord(sorted_ready, st));
    const bool mixed = c->prec == MDGPU_MIXED && d_keys == nullptr;
    k_gather<<<(N + 255) / 256, 256, 0, st>>>(P, d_site, d.chg.p, d.siteid.p, d.molmap.p, d.sorted.p,
                                              d.cell_of.p, mixed ? nullptr : d.pos64.p,
