@@ -1042,7 +1042,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       k_kreduce<false><<<nbk, KR_K * KR_W, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
                                             d.coeff2.p, nullptr, d.kdat64.p, d.blk.p);
    }
-   k_kfinal<<<1, 1024, 0, st>>>(d.blk.p, nbk, out);
+   k_kfinal<<<1, 512, 0, st>>>(d.blk.p, nbk, out);
    CK(cudaGetLastError());
    CK(d.fpart.ensure((size_t)sh.splits * 3 * Nk));
    phase_mark(c, MDGPU_PH_KFORCE);
