@@ -369,6 +369,15 @@ void mdgpu_dump_close(mdgpu_dumpfile *df);
  * bound is the FMA pipe.  No counterpart in the reference. */
 mdgpu_status mdgpu_fma_peak(int device, int fp64, double *tflops);
 
+/* Tensor-core operand probe: one 128 x n x 16 bf16 MMA pair, D = A0 B0^T
+ * then (unless flags & 4) D += A1 B1^T (A1 negated if flags & 2), FP32
+ * accumulation, in the operand layout the reciprocal-space tensor-core
+ * kernels use (flags & 1 exchanges the descriptor's two offset fields).
+ * a0, a1: 128 x 16 bf16 bit patterns, row-major; b0, b1: n x 16; d: 128 x n.
+ * n a multiple of 16 in 16..128.  No counterpart in the reference. */
+mdgpu_status mdgpu_tc_probe(int device, const unsigned short *a0, const unsigned short *b0,
+                            const unsigned short *a1, const unsigned short *b1, int n, int flags, float *d);
+
 /* Potential at one distance (poteval, src/force.c:632-650): reference-site
  * charge 1, neighbour charge chgsq, Ewald alpha as given. */
 double mdgpu_poteval(const double *potpar, double r, int ptype, double chgsq, double alpha);

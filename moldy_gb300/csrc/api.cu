@@ -221,6 +221,10 @@ mdgpu_status mdgpu::sync_out(mdgpu_ctx *c)
       return fail(c, MDGPU_E_RANGE, "Co-ordinate out of range in BIN (fill_cells)");
    if (c->h_out->err & 4)
       return fail(c, MDGPU_E_CUDA, "a structure-factor tile copy did not complete (bounded wait expired)");
+   if (c->h_out->err & 8)
+      return fail(c, MDGPU_E_CUDA, "a tensor-core structure-factor stage did not complete (bounded wait expired)");
+   if (c->h_out->err & 16)
+      return fail(c, MDGPU_E_CUDA, "a tensor-core force-pass stage did not complete (bounded wait expired)");
    return MDGPU_OK;
 }
 
@@ -258,6 +262,7 @@ mdgpu_status mdgpu_create(mdgpu_ctx **out, int device, mdgpu_precision precision
    int lo_pri = 0, hi_pri = 0;
    c->device = device;
    c->prec = precision;
+   if (const char *v = getenv("MDGPU_KSPACE_TC")) c->tc_sfac = atoi(v) != 0;
    if (cudaSetDevice(device) != cudaSuccess ||
        cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
        cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri) != cudaSuccess ||

@@ -230,6 +230,9 @@ mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl)
    kl.coeff.clear();
    kl.coeff2.clear();
    int nk = 0;
+   std::vector<int4> cols;         // (h, k, l0, count) of each column
+   std::vector<int> col_item;      // its first item (before the sort)
+   std::vector<float2> col_kxy;
    for (int hh = 0; hh <= kl.hmax; hh++)
       for (int k = (hh == 0 ? 0 : -kl.kmax); k <= kl.kmax; k++) {
          double kx = hh * hinvp[0] + k * hinvp[3];
@@ -245,6 +248,11 @@ mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl)
                if (extend)
                   kl.item.back().w++;
                else {
+                  if (prev_l != l - 1) {   // a new column
+                     cols.push_back(make_int4(hh, k, l, 0));
+                     col_item.push_back((int)kl.item.size());
+                     col_kxy.push_back(make_float2((float)kx, (float)ky));
+                  }
                   kl.item.push_back(make_int4(hh, k, l, 1));
                   kl.item_k0.push_back(nk);
                   kl.item_kxy.push_back(make_double2(kx, ky));
@@ -269,9 +277,12 @@ mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl)
    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return kl.item[a].w > kl.item[b].w; });
    KList o;
    o.item.reserve(kl.nitems);
+   std::vector<int> new_k0(kl.nitems), pre_w(kl.nitems);
+   for (int i = 0; i < kl.nitems; i++) pre_w[i] = kl.item[i].w;
    int k0 = 0;
    for (int i : order) {
       const int4 it = kl.item[i];
+      new_k0[i] = k0;
       o.item.push_back(it);
       o.item_k0.push_back(k0);
       o.item_kxy.push_back(kl.item_kxy[i]);
@@ -289,6 +300,47 @@ mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl)
    kl.kz.swap(o.kz);
    kl.coeff.swap(o.coeff);
    kl.coeff2.swap(o.coeff2);
+   // Tensor-core items: each column cut into runs of KT from its first l,
+   // so run r holds the column's KI items 4r .. 4r+3 (contiguous k each).
+   kl.tc_item.clear();
+   kl.tc_k0.clear();
+   kl.tc_kxy.clear();
+   for (size_t c = 0; c < cols.size(); c++) {
+      const int f = col_item[c], e = c + 1 < cols.size() ? col_item[c + 1] : kl.nitems;
+      int total = 0;
+      for (int i = f; i < e; i++) total += pre_w[i];
+      for (int r = 0; r * KT < total; r++) {
+         int ki[4];
+         for (int j = 0; j < 4; j++) {
+            const int run = 4 * r + j;
+            ki[j] = run * KI < total ? new_k0[f + run] : -1;
+         }
+         kl.tc_item.push_back(make_int4(cols[c].x, cols[c].y, cols[c].z + r * KT, std::min(KT, total - r * KT)));
+         kl.tc_k0.push_back(make_int4(ki[0], ki[1], ki[2], ki[3]));
+         kl.tc_kxy.push_back(col_kxy[c]);
+      }
+   }
+   kl.tc_nitems = (int)kl.tc_item.size();
+   {
+      std::vector<int> ord(kl.tc_nitems);
+      for (int i = 0; i < kl.tc_nitems; i++) ord[i] = i;
+      std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return kl.tc_item[a].w > kl.tc_item[b].w; });
+      std::vector<int4> it2, k02;
+      std::vector<float2> kxy2;
+      for (int i : ord) {
+         it2.push_back(kl.tc_item[i]);
+         k02.push_back(kl.tc_k0[i]);
+         kxy2.push_back(kl.tc_kxy[i]);
+      }
+      while (it2.size() % 128) {
+         it2.push_back(make_int4(0, 0, 0, 0));
+         k02.push_back(make_int4(-1, -1, -1, -1));
+         kxy2.push_back(make_float2(0.f, 0.f));
+      }
+      kl.tc_item.swap(it2);
+      kl.tc_k0.swap(k02);
+      kl.tc_kxy.swap(kxy2);
+   }
    return MDGPU_OK;
 }
 

@@ -43,8 +43,6 @@ __device__ __forceinline__ unsigned long long to_fixed64(double s)
    return (unsigned long long)t << 2;
 }
 
-__device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c);
-
 // Per-site records are written in link-cell order (slot i holds site
 // sorted[i]; ns is the stride of the site array): the structure-factor
 // chunks are then compact regions of the cell, close to neutral, so their
@@ -92,17 +90,6 @@ __global__ void k_prep(int N, int ns, const int *__restrict__ sorted, const doub
    }
 }
 
-// exp(2 pi i p / 2^32) for a 32-bit phase p, to about 1 FP32 ulp: the top 24
-// bits go exactly into sincospif, the low 8 bits (< 2^-23 revolution) are
-// added to first order.
-__device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c)
-{
-   float s0, c0;
-   sincospif((float)(int)(p & 0xFFFFFF00u) * 4.656612873077393e-10f, &s0, &c0);   // 2^-31
-   const float d = (float)(p & 0xFFu) * 1.4629180792671596e-09f;                  // 2 pi / 2^32
-   *c = fmaf(-s0, d, c0);
-   *s = fmaf(c0, d, s0);
-}
 
 
 // ---------------------------------------------------------------- S(k)
@@ -894,10 +881,24 @@ mdgpu_status ks_prepare(mdgpu_ctx *c)
       CK(cudaMemcpyAsync(d.kz64.p, kv.data(), kv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(d.coeff.p, kl.coeff.data(), nk * sizeof(double), cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(d.coeff2.p, kl.coeff2.data(), nk * sizeof(double), cudaMemcpyHostToDevice, st));
+      const size_t nt = kl.tc_item.size();
+      CK(d.tc_item.ensure(nt));
+      CK(d.tc_k0.ensure(nt));
+      CK(d.tc_kxy.ensure(nt));
+      CK(d.tc_coef.ensure(nt));
+      CK(cudaMemcpyAsync(d.tc_kxy.p, kl.tc_kxy.data(), nt * sizeof(float2), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.tc_item.p, kl.tc_item.data(), nt * sizeof(int4), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.tc_k0.p, kl.tc_k0.data(), nt * sizeof(int4), cudaMemcpyHostToDevice, st));
       CK(cudaStreamSynchronize(st));
       c->kl_uploaded = true;
    }
-   CK(d.ph32.ensure(N));
+   if (c->prec == MDGPU_MIXED && c->tc_sfac) {
+      CK(ks_tc_init(c->device));
+      CK(d.ztab.ensure(ks_tc_ztab_len(N)));
+      CK(d.zsite.ensure(ks_tc_zsite_len(N)));
+      CK(d.utab.ensure(ks_tc_utab_len((int)kl.tc_item.size())));
+   }
+   CK(d.ph32.ensure(N + 128));
    CK(d.z32.ensure(N));
    CK(d.zp32.ensure((size_t)N * KI));
    CK(d.ph64a.ensure(N));
@@ -962,8 +963,13 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    if (compact) {
       if (c->ncharged_gen != c->gen) {
          int n = 0;
-         for (double q : c->chg) n += q != 0.0;
+         double qm = 0;
+         for (double q : c->chg) {
+            n += q != 0.0;
+            qm = std::max(qm, std::fabs(q));
+         }
          c->ncharged = n;
+         c->qmax = qm;
          c->ncharged_gen = c->gen;
       }
       Nk = c->ncharged;
@@ -998,7 +1004,12 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    }
    phase_mark(c, MDGPU_PH_SFAC);
    const dim3 gs((ni + 127) / 128, sh.chunks);
-   if (mixed) {
+   if (mixed && compact && c->tc_sfac) {
+      CK(d.part32.ensure((size_t)ks_tc_chunks(Nk) * nk));
+      CK(d.ztab.ensure(ks_tc_ztab_len(Nk)));
+      sh.chunks = ks_sfac_tc(st, Nk, nk, d, (int)(kl.tc_item.size() / 128), c->qmax, &out->err);
+      c->launches += 1;
+   } else if (mixed) {
       CK(d.part32.ensure((size_t)sh.chunks * nk));
       k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, Nk, sh.chunk, nk, d.part32.p,
                                    &out->err);
@@ -1044,11 +1055,18 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    }
    k_kfinal<<<1, 512, 0, st>>>(d.blk.p, nbk, out);
    CK(cudaGetLastError());
+   const bool tcf = mixed && compact && c->tc_sfac;
+   if (tcf) sh.splits = ks_force_tc_splits(Nk);
    CK(d.fpart.ensure((size_t)sh.splits * 3 * Nk));
    phase_mark(c, MDGPU_PH_KFORCE);
    dim3 gf((Nk + 255) / 256, sh.splits);
    const int obase = compact ? -1 : 0;   // partial rows by slot of the charged list, or by site
-   if (mixed)
+   if (tcf) {
+      CK(d.zsite.ensure(ks_tc_zsite_len(Nk)));
+      CK(d.utab.ensure(ks_tc_utab_len((int)kl.tc_item.size())));
+      ks_force_tc(st, Nk, d, (int)kl.tc_item.size(), c->rd.chg.p, slots, (float)kl.dkz, d.fpart.p, &out->err);
+      c->launches += 2;
+   } else if (mixed)
       k_force32<<<gf, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
                                            d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, slots, Nk, obase,
                                            (float)kl.dkz, d.fpart.p);

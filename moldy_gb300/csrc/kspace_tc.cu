@@ -1,0 +1,655 @@
+// Structure factor of the mixed form on the tensor cores (tcgen05): the
+// S(k) pass of ewald() (src/ewald.c:124-141, the sums of q cos(k.r) and
+// q sin(k.r) over sites, 523-533) as a complex matrix product.
+//
+// A tensor-core item is a run of up to KT = 64 consecutive l values of one
+// (h,k) column.  For item i, site j and offset t,
+//     exp(i k.r_j) = seed_ij z_j(t),  seed_ij = exp(2 pi i (h u_x + k u_y + l0 u_z)),
+//     z_j(t) = exp(2 pi i t u_z)
+// with the 32-bit fixed-point phases u of the FP32 path, so
+//     S(i, t) = sum_j (q_j seed_ij) z_j(t)
+// is a product of an items x sites matrix (computed per stage on the CUDA
+// cores: one polynomial sine/cosine per item and site, amortised over up to
+// 64 k-vectors) and a sites x t matrix (the per-site z tables, built once
+// per evaluation).  Complex arithmetic as real MMAs: Re S = Ar Zr - Ai Zi,
+// Im S = Ar Zi + Ai Zr, the minus sign by the instruction's A negation.
+//
+// Precision.  Charges are scaled by a power of two to |q| <= 1, and every
+// FP32 operand is split into three bf16 terms on fixed grids (tc.cuh): the
+// hi*hi products go to one tensor-memory accumulator, where their sums are
+// exact (multiples of 2^-14 below 2^10: a 512-site partial of terms of
+// magnitude <= 1), so the accumulator's round-toward-zero never acts on
+// them; hm, mh, hl, lh and mm go to a second accumulator, 2^-8 smaller.  The
+// terms left out and the splitting are within 2^-24 of each operand, as for
+// the FP32 path.  Each CTA sums 512 sites and writes one partial per k; the
+// partials are added in FP64 by the per-k reduction.
+//
+// CTA roles (192 threads): warps 0-3 build the A operand of each stage (one
+// item row per thread) and, at the end, read the accumulators back (a
+// warp reaches tensor-memory lanes 32 (w % 4) ..); warp 4 streams each
+// stage's z tables and site records by bulk copy; warp 5 owns the tensor
+// memory and issues the MMAs.  Stages are triple-buffered on mbarriers;
+// every wait is bounded and sets bit 3 of the error word when it expires.
+#include <cmath>
+
+#include "mdgpu_internal.h"
+#include "phase.cuh"
+#include "tc.cuh"
+
+namespace mdgpu {
+
+constexpr int TC_KS = 16;                          // sites per stage (the K of one MMA)
+constexpr int TC_NS = 3;                           // stages in flight
+constexpr int TC_TERM = 128 * TC_KS * 2;           // one 128-row bf16 operand of a stage: 4096 bytes
+constexpr int TC_ABYTES = 6 * TC_TERM;             // Ar, Ai x (hi, mid, lo)
+constexpr int TC_BBYTES = 3 * TC_TERM;             // [Zr | Zi] x (hi, mid, lo)
+constexpr int TC_PBYTES = TC_KS * 16;              // site records (u_x, u_y, u_z, q)
+constexpr int TC_STAGE = TC_ABYTES + TC_BBYTES + TC_PBYTES;
+constexpr int TC_SMEM = TC_NS * TC_STAGE;
+constexpr int TC_CHUNK = 512;                      // sites per CTA (one partial per k)
+constexpr int TC_LBO = 16 * 128;                   // 8-column groups of a 128-row operand
+constexpr int TC_ERR = 8;                          // error-word bit: a stage wait expired
+
+static_assert(TC_STAGE % 16 == 0 && TC_ABYTES % 1024 == 0, "stage buffers stay 16-byte aligned");
+static_assert(TC_CHUNK % TC_KS == 0, "chunks hold whole stages");
+static_assert(KT == 4 * KI && KT <= 64, "an item is four KI runs, Zr and Zi fit 128 rows");
+
+// z tables of the padded site list (np a multiple of 16) as the MMA's B
+// operand, per 16-site stage: [term][column group (8 sites)][row group][8
+// rows][8 sites] bf16, rows 0..63 cos(2 pi t u_z) and 64..127 its sine.
+// One thread per (8 sites, row); also zeroes the site records past n so
+// padding sites have no charge.
+__global__ void k_ztab_tc(int n, int np, int4 *__restrict__ ph, uint4 *__restrict__ ztab)
+{
+   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+   if (idx >= (long long)(np / 8) * 128) return;
+   const int q8 = (int)(idx >> 7), row = (int)(idx & 127), t = row & 63;
+   float v[8];
+#pragma unroll
+   for (int s = 0; s < 8; s++) {
+      const int i = q8 * 8 + s;
+      const unsigned int uz = i < n ? (unsigned int)ph[i].z : 0u;
+      float sn, cs;
+      sincos_rev32((unsigned int)t * uz, &sn, &cs);
+      v[s] = row < 64 ? cs : sn;
+   }
+   unsigned int h[4], m[4], l[4];
+#pragma unroll
+   for (int j = 0; j < 4; j++) tc::split3(v[2 * j], v[2 * j + 1], h[j], m[j], l[j]);
+   const size_t base = (size_t)(q8 >> 1) * (TC_BBYTES / 16) + (q8 & 1) * (TC_LBO / 16) + (row >> 3) * 8 + (row & 7);
+   ztab[base] = make_uint4(h[0], h[1], h[2], h[3]);
+   ztab[base + TC_TERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
+   ztab[base + 2 * TC_TERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
+   if (row == 0)
+      for (int s = 0; s < 8; s++) {
+         const int i = q8 * 8 + s;
+         if (i >= n && i < np) ph[i] = make_int4(0, 0, 0, 0);
+      }
+}
+
+__device__ __forceinline__ void tc_abort(int *flag, int *err, int bit = TC_ERR)
+{
+   *(volatile int *)flag = 1;
+   atomicOr(err, bit);
+}
+
+__device__ __forceinline__ bool tc_aborted(const int *flag)
+{
+   return *(const volatile int *)flag != 0;
+}
+
+// Grid: (item tiles of 128, site chunks of TC_CHUNK).  part[chunk][k].
+__global__ void __launch_bounds__(192, 2)
+k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const int4 *__restrict__ ph,
+          const uint4 *__restrict__ ztab, int np, int nk, float qscale, float qunscale, float2 *__restrict__ part,
+          int *__restrict__ err)
+{
+   using namespace tc;
+   extern __shared__ __align__(1024) unsigned char sm[];
+   __shared__ __align__(8) uint64_t full_b[TC_NS], full_a[TC_NS], empty[TC_NS], accf;
+   __shared__ unsigned int tmem_s;
+   __shared__ int abort_s;
+   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+   const int tile = blockIdx.x, chunk = blockIdx.y;
+   const int s0 = chunk * TC_CHUNK;
+   const int nst = (min(np, s0 + TC_CHUNK) - s0) / TC_KS;
+   const int ncols = (item[tile * 128].w + 15) & ~15;   // the tile's largest count, rounded up
+   if (ncols == 0 || nst <= 0) return;                  // (uniform over the CTA)
+   if (tid == 0) {
+      for (int s = 0; s < TC_NS; s++) {
+         bar_init(&full_b[s], 1);
+         bar_init(&full_a[s], 4);
+         bar_init(&empty[s], 1);
+      }
+      bar_init(&accf, 1);
+      abort_s = 0;
+      bar_init_fence();
+   }
+   __syncwarp();
+   if (w == 5) tmem_alloc(&tmem_s, 256);   // [0,128): hh sums, [128,256): the smaller terms
+   fence_before_sync();
+   __syncthreads();
+   fence_after_sync();
+   const unsigned int tmem = tmem_s;
+
+   if (w == 4) {
+      // ---- bulk copies of each stage's z tables and site records
+      if (lane == 0) {
+         int issued = 0;
+         for (int st = 0; st < nst; st++) {
+            const int s = st % TC_NS;
+            if (st >= TC_NS && !bar_wait(&empty[s], (unsigned int)(st / TC_NS - 1) & 1u)) {
+               tc_abort(&abort_s, err);
+               break;
+            }
+            if (tc_aborted(&abort_s)) break;
+            unsigned char *sb = sm + s * TC_STAGE;
+            bar_expect_tx(&full_b[s], TC_BBYTES + TC_PBYTES);
+            bulk_load(sb + TC_ABYTES, ztab + (size_t)(s0 / TC_KS + st) * (TC_BBYTES / 16), TC_BBYTES, &full_b[s]);
+            bulk_load(sb + TC_ABYTES + TC_BBYTES, ph + s0 + st * TC_KS, TC_PBYTES, &full_b[s]);
+            issued = st + 1;
+         }
+         // copies still in flight complete before the CTA's shared memory goes
+         for (int st = issued > TC_NS ? issued - TC_NS : 0; st < issued; st++)
+            bar_wait(&full_b[st % TC_NS], (unsigned int)(st / TC_NS) & 1u);
+      }
+   } else if (w == 5) {
+      // ---- MMA issue
+      if (lane == 0) {
+         const unsigned int idn = idesc_bf16(128, ncols, false), idneg = idesc_bf16(128, ncols, true);
+         const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
+         for (int st = 0; st < nst; st++) {
+            const int s = st % TC_NS;
+            const unsigned int par = (unsigned int)(st / TC_NS) & 1u;
+            if (!bar_wait(&full_a[s], par) || !bar_wait(&full_b[s], par)) {
+               tc_abort(&abort_s, err);
+               break;
+            }
+            fence_after_sync();
+            const unsigned int a = saddr(sm + s * TC_STAGE), b = a + TC_ABYTES;
+#pragma unroll
+            for (int p = 0; p < 6; p++) {
+               const unsigned int d = tmem + (p == 0 ? 0u : 128u);
+               const bool acc = st > 0 || p > 1;
+               const uint64_t ar = sdesc(a + ta[p] * TC_TERM, TC_LBO, 128);
+               const uint64_t ai = sdesc(a + (3 + ta[p]) * TC_TERM, TC_LBO, 128);
+               const uint64_t zr = sdesc(b + tb[p] * TC_TERM, TC_LBO, 128);
+               const uint64_t zi = sdesc(b + tb[p] * TC_TERM + 8 * 128, TC_LBO, 128);
+               mma_bf16(d, ar, zr, idn, acc);          // Re += Ar Zr
+               mma_bf16(d + 64, ar, zi, idn, acc);     // Im += Ar Zi
+               mma_bf16(d, ai, zi, idneg, true);       // Re -= Ai Zi
+               mma_bf16(d + 64, ai, zr, idn, true);    // Im += Ai Zr
+            }
+            mma_commit(&empty[s]);
+         }
+         mma_commit(&accf);   // also after an abort: the readers wait on it
+      }
+   } else {
+      // ---- A operand: q_j seed_ij for this thread's item row
+      const int m = tid;
+      const int4 hd = item[tile * 128 + m];
+      const unsigned int H = (unsigned int)hd.x, K = (unsigned int)hd.y, L = (unsigned int)hd.z;
+      for (int st = 0; st < nst; st++) {
+         const int s = st % TC_NS;
+         if (tc_aborted(&abort_s)) break;
+         if (!bar_wait(&full_b[s], (unsigned int)(st / TC_NS) & 1u)) {
+            tc_abort(&abort_s, err);
+            break;
+         }
+         unsigned char *A = sm + s * TC_STAGE;
+         const int4 *P = reinterpret_cast<const int4 *>(A + TC_ABYTES + TC_BBYTES);
+#pragma unroll
+         for (int g = 0; g < 2; g++) {
+            unsigned int hr[4], mr[4], lr[4], hi[4], mi[4], li[4];
+#pragma unroll
+            for (int jp = 0; jp < 4; jp++) {
+               const int4 v0 = P[8 * g + 2 * jp], v1 = P[8 * g + 2 * jp + 1];
+               float s0v, c0v, s1v, c1v;
+               sincos_poly(H * (unsigned int)v0.x + K * (unsigned int)v0.y + L * (unsigned int)v0.z, &s0v, &c0v);
+               sincos_poly(H * (unsigned int)v1.x + K * (unsigned int)v1.y + L * (unsigned int)v1.z, &s1v, &c1v);
+               const float q0 = __int_as_float(v0.w) * qscale, q1 = __int_as_float(v1.w) * qscale;
+               split3(c0v * q0, c1v * q1, hr[jp], mr[jp], lr[jp]);
+               split3(s0v * q0, s1v * q1, hi[jp], mi[jp], li[jp]);
+            }
+            unsigned char *row = A + g * TC_LBO + (m >> 3) * 128 + (m & 7) * 16;
+            *reinterpret_cast<uint4 *>(row) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
+            *reinterpret_cast<uint4 *>(row + TC_TERM) = make_uint4(mr[0], mr[1], mr[2], mr[3]);
+            *reinterpret_cast<uint4 *>(row + 2 * TC_TERM) = make_uint4(lr[0], lr[1], lr[2], lr[3]);
+            *reinterpret_cast<uint4 *>(row + 3 * TC_TERM) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<uint4 *>(row + 4 * TC_TERM) = make_uint4(mi[0], mi[1], mi[2], mi[3]);
+            *reinterpret_cast<uint4 *>(row + 5 * TC_TERM) = make_uint4(li[0], li[1], li[2], li[3]);
+         }
+         fence_async_smem();
+         __syncwarp();
+         if (lane == 0) bar_arrive(&full_a[s]);
+      }
+      // ---- read back: row m of the tile, columns t (Re) and 64 + t (Im)
+      const bool done = bar_wait(&accf, 0);
+      const bool ok = __all_sync(0xffffffffu, done && !tc_aborted(&abort_s));
+      if (!done && lane == 0) tc_abort(&abort_s, err);
+      fence_after_sync();
+      if (ok) {
+         const int4 k0 = item_k0[tile * 128 + m];
+         const unsigned int trow = tmem + ((unsigned int)(32 * w) << 16);
+         float2 *dst = part + (size_t)chunk * nk;
+         for (int t0 = 0; t0 < ncols; t0 += 16) {
+            float re[16], im[16], re2[16], im2[16];
+            tmem_ld16(trow + t0, re);
+            tmem_ld16(trow + 64 + t0, im);
+            tmem_ld16(trow + 128 + t0, re2);
+            tmem_ld16(trow + 192 + t0, im2);
+            tmem_wait2(re, im);
+            tmem_wait2(re2, im2);
+            const int kr = t0 == 0 ? k0.x : t0 == 16 ? k0.y : t0 == 32 ? k0.z : k0.w;
+            if (kr >= 0)
+#pragma unroll
+               for (int j = 0; j < 16; j++)
+                  if (t0 + j < hd.w)
+                     dst[kr + j] = make_float2((re[j] + re2[j]) * qunscale, (im[j] + im2[j]) * qunscale);
+         }
+      }
+   }
+   fence_before_sync();
+   __syncthreads();
+   if (w == 5) {
+      __syncwarp();
+      fence_after_sync();
+      tmem_dealloc(tmem, 256);
+   }
+}
+
+// Host side: z tables, then the product.  Returns the number of site
+// chunks (rows of part).
+int ks_sfac_tc(cudaStream_t st, int nsites, int nk, const KsDev &d, int ntiles, double qmax, int *err)
+{
+   const int np = (nsites + TC_KS - 1) / TC_KS * TC_KS;
+   const long long nthr = (long long)(np / 8) * 128;
+   k_ztab_tc<<<(unsigned int)((nthr + 255) / 256), 256, 0, st>>>(nsites, np, d.ph32.p, d.ztab.p);
+   const int nchunks = (np + TC_CHUNK - 1) / TC_CHUNK;
+   // charges scaled by a power of two to |q| <= 1 (exact), undone on the partials
+   int e = 0;
+   std::frexp(qmax > 0 ? qmax : 1.0, &e);
+   const float qs = std::ldexp(1.0f, e);
+   k_sfac_tc<<<dim3(ntiles, nchunks), 192, TC_SMEM, st>>>(d.tc_item.p, d.tc_k0.p, d.ph32.p, d.ztab.p, np, nk,
+                                                          1.0f / qs, qs, d.part32.p, err);
+   return nchunks;
+}
+
+
+size_t ks_tc_ztab_len(int nsites)
+{
+   const size_t np = (size_t)(nsites + TC_KS - 1) / TC_KS * TC_KS;
+   return np / TC_KS * (TC_BBYTES / 16);
+}
+
+int ks_tc_chunks(int nsites)
+{
+   const int np = (nsites + TC_KS - 1) / TC_KS * TC_KS;
+   return (np + TC_CHUNK - 1) / TC_CHUNK;
+}
+
+
+// ------------------------------------------------------------- forces
+// The force pass of ewald() (src/ewald.c:557-566): for a charged site j,
+//     F_j = q_j sum_k k (sin(k.r_j) A_k - cos(k.r_j) B_k) = q_j sum_k k Im(e_jk U_k),
+// U_k = A_k - i B_k.  Over a tensor-core item (seed_ij, offsets t, k-vector
+// (kx, ky, kz0 + t dkz)):
+//     W1_ij = sum_t z_j(t) U_t,  W2_ij = sum_t t z_j(t) U_t,
+//     F_j += q_j (kx f1, ky f1, kz0 f1 + dkz f2),  f1,2 = Im(seed_ij W1,2_ij).
+// W is a product of the sites x t z tables (K = 128: the 64 cosines, then
+// the 64 sines) and four coefficient rows per item,
+//     W1re = [A | B],  W1im = [-B | A],  W2re = [tA | tB],  W2im = [-tB | tA],
+// each row scaled by a power of two to |v| <= 1 (the scale is folded into
+// the item's force coefficients).  A CTA holds one 128-site tile's z tables
+// (96 KB, loaded once) and streams the coefficient rows of 32 items (N =
+// 128) per tile of items, K-step by K-step (only the K-steps an item tile's
+// longest item needs); tensor memory holds two accumulator pairs, so the
+// epilogue of one item tile (8 warps: the seed sine/cosine per item and
+// site, the k-vector weights, Kahan-compensated FP32 force sums) overlaps
+// the MMAs of the next.
+constexpr int FTC_NI = 32;                         // items per item tile (4 rows each: N = 128)
+constexpr int FTC_NSB = 4;                         // coefficient stages in flight
+constexpr int FTC_ATERM = 128 * 128 * 2;           // one term of a site tile's z tables: 32 KB
+constexpr int FTC_ABYTES = 3 * FTC_ATERM;          // 96 KB
+constexpr int FTC_BTERM = 128 * 16 * 2;            // one term of a coefficient stage: 4 KB
+constexpr int FTC_BBYTES = 3 * FTC_BTERM;          // 12 KB
+constexpr int FTC_SMEM = FTC_ABYTES + FTC_NSB * FTC_BBYTES + 128 * 3 * 4 * 2;
+constexpr int FTC_THREADS = 320;                   // 8 epilogue warps, bulk-copy warp, MMA warp
+constexpr int FTC_SPLITS = 2;                      // item-tile ranges per site tile (grid.y)
+constexpr int FTC_ERR = 16;                        // error-word bit: a force-pass wait expired
+
+// Site tiles' z tables as the A operand: [tile][term][column group 16][row
+// group 16][8 rows][8 t] bf16; column groups 0..7 hold cos(2 pi t u_z), t =
+// 0..63, 8..15 the sines.  One thread per (site, column group).
+__global__ void k_zsite_tc(int n, int np128, const int4 *__restrict__ ph, uint4 *__restrict__ zsite)
+{
+   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+   if (idx >= (long long)np128 * 16) return;
+   const int r = (int)(idx & 127), g = (int)((idx >> 7) & 15), tile = (int)(idx >> 11);
+   const int i = tile * 128 + r;
+   const unsigned int uz = i < n ? (unsigned int)ph[i].z : 0u;
+   const int t0 = 8 * (g & 7);
+   float v[8];
+#pragma unroll
+   for (int e = 0; e < 8; e++) {
+      float sn, cs;
+      sincos_rev32((unsigned int)(t0 + e) * uz, &sn, &cs);
+      v[e] = g < 8 ? cs : sn;
+   }
+   unsigned int h[4], m[4], l[4];
+#pragma unroll
+   for (int j = 0; j < 4; j++) tc::split3(v[2 * j], v[2 * j + 1], h[j], m[j], l[j]);
+   const size_t base = (size_t)tile * (FTC_ABYTES / 16) + g * 128 + (r >> 3) * 8 + (r & 7);
+   zsite[base] = make_uint4(h[0], h[1], h[2], h[3]);
+   zsite[base + FTC_ATERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
+   zsite[base + 2 * FTC_ATERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// Coefficient rows of each item from the per-k (A, B, kz): one warp per
+// item.  Layout per (item tile, K-step of 16): [term][column group 2][row
+// group 16][8 rows][8 K] bf16, row 4 i + c for item i of the tile.
+__global__ void __launch_bounds__(256)
+k_utab_tc(int nitems, const int4 *__restrict__ item, const int4 *__restrict__ item_k0,
+          const float2 *__restrict__ kxy, const float4 *__restrict__ kd, float dkz, uint4 *__restrict__ utab,
+          float4 *__restrict__ coef)
+{
+   __shared__ float sv[8][64][4];
+   const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int i = blockIdx.x * 8 + wl;
+   if (i >= nitems) return;   // (warp-uniform)
+   const int4 hd = item[i], k0 = item_k0[i];
+   float a[2], b[2], kz0 = 0.f, m1 = 0.f, m2 = 0.f;
+#pragma unroll
+   for (int h = 0; h < 2; h++) {
+      const int t = lane + 32 * h;
+      a[h] = b[h] = 0.f;
+      if (t < hd.w) {
+         const int run = t >> 4;
+         const int kr = run == 0 ? k0.x : run == 1 ? k0.y : run == 2 ? k0.z : k0.w;
+         const float4 v = kd[kr + (t & 15)];
+         a[h] = v.x;
+         b[h] = v.y;
+         if (t == 0) kz0 = v.z;
+      }
+      m1 = fmaxf(m1, fmaxf(fabsf(a[h]), fabsf(b[h])));
+      m2 = fmaxf(m2, (float)t * fmaxf(fabsf(a[h]), fabsf(b[h])));
+   }
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) {
+      m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+      m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+   }
+   kz0 = __shfl_sync(0xffffffffu, kz0, 0);
+   // powers of two at or above the rows' largest magnitude
+   int e1 = 0, e2 = 0;
+   if (m1 > 0.f) frexpf(m1, &e1);
+   if (m2 > 0.f) frexpf(m2, &e2);
+   const float s1 = ldexpf(1.f, e1), s2 = ldexpf(1.f, e2), i1 = ldexpf(1.f, -e1), i2 = ldexpf(1.f, -e2);
+#pragma unroll
+   for (int h = 0; h < 2; h++) {
+      const int t = lane + 32 * h;
+      sv[wl][t][0] = a[h] * i1;
+      sv[wl][t][1] = b[h] * i1;
+      sv[wl][t][2] = (float)t * a[h] * i2;
+      sv[wl][t][3] = (float)t * b[h] * i2;
+   }
+   __syncwarp();
+   const int tile = i / FTC_NI, il = i % FTC_NI;
+#pragma unroll
+   for (int h = 0; h < 2; h++) {
+      const int id = lane + 32 * h, c = id & 3, g = id >> 2;   // row c of the item, column group g
+      const bool zi = g >= 8;                                  // the sine half of K
+      const int t0 = 8 * (g & 7);
+      // W1re = [A | B], W1im = [-B | A], W2re = [tA | tB], W2im = [-tB | tA]
+      const int src = (c & 2) + (zi ? ((c & 1) ? 0 : 1) : ((c & 1) ? 1 : 0));
+      const float sg = (!zi && (c & 1)) ? -1.f : 1.f;
+      float v[8];
+#pragma unroll
+      for (int e = 0; e < 8; e++) v[e] = sg * sv[wl][t0 + e][src];
+      unsigned int hh[4], mm[4], ll[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) tc::split3(v[2 * j], v[2 * j + 1], hh[j], mm[j], ll[j]);
+      const int n = 4 * il + c, ks = g >> 1, kg = g & 1;
+      const size_t base =
+          ((size_t)tile * 8 + ks) * (FTC_BBYTES / 16) + kg * 128 + (n >> 3) * 8 + (n & 7);
+      utab[base] = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+      utab[base + FTC_BTERM / 16] = make_uint4(mm[0], mm[1], mm[2], mm[3]);
+      utab[base + 2 * FTC_BTERM / 16] = make_uint4(ll[0], ll[1], ll[2], ll[3]);
+   }
+   if (lane == 0) {
+      const float2 k = kxy[i];
+      coef[i] = make_float4(k.x * s1, k.y * s1, kz0 * s1, dkz * s2);
+   }
+}
+
+__device__ __forceinline__ void kahan_add_tc(float &s, float &c, float x)
+{
+   const float y = x - c;
+   const float t = s + y;
+   c = (t - s) - y;
+   s = t;
+}
+
+// Grid: (site tiles of 128, FTC_SPLITS ranges of item tiles).
+__global__ void __launch_bounds__(FTC_THREADS, 1)
+k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int nitems,
+           const int4 *__restrict__ ph, const uint4 *__restrict__ zsite, const uint4 *__restrict__ utab,
+           const double *__restrict__ chg, const int *__restrict__ slots, int n, double *__restrict__ fpart,
+           int *__restrict__ err)
+{
+   using namespace tc;
+   extern __shared__ __align__(1024) unsigned char sm[];
+   __shared__ __align__(8) uint64_t full_a, full_b[FTC_NSB], empty_b[FTC_NSB], acc_full[2], acc_empty[2], done;
+   __shared__ unsigned int tmem_s;
+   __shared__ int abort_s;
+   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+   const int tile = blockIdx.x;
+   const int ntiles = nitems / FTC_NI;
+   const int per = (ntiles + gridDim.y - 1) / gridDim.y;
+   const int nt0 = blockIdx.y * per, nt1 = min(ntiles, nt0 + per);
+   unsigned char *A = sm, *Bs = sm + FTC_ABYTES;
+   float *red = reinterpret_cast<float *>(sm + FTC_ABYTES + FTC_NSB * FTC_BBYTES);   // [2][128][3] (sum, comp)
+   if (tid == 0) {
+      bar_init(&full_a, 1);
+      for (int s = 0; s < FTC_NSB; s++) {
+         bar_init(&full_b[s], 1);
+         bar_init(&empty_b[s], 1);
+      }
+      for (int b = 0; b < 2; b++) {
+         bar_init(&acc_full[b], 1);
+         bar_init(&acc_empty[b], 8);
+      }
+      bar_init(&done, 1);
+      abort_s = 0;
+      bar_init_fence();
+   }
+   __syncwarp();
+   if (w == 9) tmem_alloc(&tmem_s, 512);   // two buffers x (hh sums, smaller terms) x 128 columns
+   fence_before_sync();
+   __syncthreads();
+   fence_after_sync();
+   const unsigned int tmem = tmem_s;
+   // K-steps of an item tile: ceil(longest count / 16) in each half of K
+   auto khalf = [&](int nt) { return (item[nt * FTC_NI].w + 15) >> 4; };
+
+   if (w == 8) {
+      if (lane == 0) {
+         bar_expect_tx(&full_a, FTC_ABYTES);
+         bulk_load(A, zsite + (size_t)tile * (FTC_ABYTES / 16), FTC_ABYTES, &full_a);
+         int g = 0;
+         bool stop = false;
+         for (int nt = nt0; nt < nt1 && !stop; nt++) {
+            const int kh = khalf(nt);
+            for (int q = 0; q < 2 * kh; q++) {
+               const int ks = q < kh ? q : 4 + q - kh;
+               const int s = g % FTC_NSB;
+               if (g >= FTC_NSB && !bar_wait(&empty_b[s], (unsigned int)(g / FTC_NSB - 1) & 1u)) {
+                  tc_abort(&abort_s, err, FTC_ERR);
+                  stop = true;
+                  break;
+               }
+               if (tc_aborted(&abort_s)) {
+                  stop = true;
+                  break;
+               }
+               bar_expect_tx(&full_b[s], FTC_BBYTES);
+               bulk_load(Bs + s * FTC_BBYTES, utab + ((size_t)nt * 8 + ks) * (FTC_BBYTES / 16), FTC_BBYTES,
+                         &full_b[s]);
+               g++;
+            }
+         }
+         bar_wait(&full_a, 0);
+         for (int q = g > FTC_NSB ? g - FTC_NSB : 0; q < g; q++)
+            bar_wait(&full_b[q % FTC_NSB], (unsigned int)(q / FTC_NSB) & 1u);
+      }
+   } else if (w == 9) {
+      if (lane == 0) {
+         const unsigned int idn = idesc_bf16(128, 128, false);
+         const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
+         const unsigned int a0 = saddr(A), b0 = saddr(Bs);
+         bool ok = bar_wait(&full_a, 0);
+         if (!ok) tc_abort(&abort_s, err, FTC_ERR);
+         int g = 0;
+         for (int nt = nt0, j = 0; nt < nt1 && ok; nt++, j++) {
+            const int b = j & 1;
+            if (j >= 2 && !bar_wait(&acc_empty[b], (unsigned int)((j >> 1) - 1) & 1u)) {
+               tc_abort(&abort_s, err, FTC_ERR);
+               break;
+            }
+            fence_after_sync();
+            const int kh = khalf(nt);
+            for (int q = 0; q < 2 * kh; q++) {
+               const int ks = q < kh ? q : 4 + q - kh;
+               const int s = g % FTC_NSB;
+               if (!bar_wait(&full_b[s], (unsigned int)(g / FTC_NSB) & 1u)) {
+                  tc_abort(&abort_s, err, FTC_ERR);
+                  ok = false;
+                  break;
+               }
+               fence_after_sync();
+               const unsigned int bs = b0 + s * FTC_BBYTES;
+#pragma unroll
+               for (int p = 0; p < 6; p++) {
+                  const uint64_t ad = sdesc(a0 + ta[p] * FTC_ATERM + ks * 4096, 2048, 128);
+                  const uint64_t bd = sdesc(bs + tb[p] * FTC_BTERM, 2048, 128);
+                  mma_bf16(tmem + b * 256 + (p == 0 ? 0 : 128), ad, bd, idn, q > 0 || p > 1);
+               }
+               mma_commit(&empty_b[s]);
+               g++;
+            }
+            if (ok) mma_commit(&acc_full[b]);
+         }
+         mma_commit(&done);
+         bar_wait(&done, 0);   // every MMA complete before the tensor memory is released
+      }
+   } else {
+      // ---- epilogue: site row r, item half ih of each item tile
+      const int r = 32 * (w & 3) + lane, ih = w >> 2;
+      const int i = tile * 128 + r;
+      const int4 v = i < n ? ph[i] : make_int4(0, 0, 0, 0);
+      const unsigned int ux = (unsigned int)v.x, uy = (unsigned int)v.y, uz = (unsigned int)v.z;
+      const unsigned int trow = tmem + ((unsigned int)(32 * (w & 3)) << 16);
+      float Fx = 0.f, Fy = 0.f, Fz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
+      for (int nt = nt0, j = 0; nt < nt1; nt++, j++) {
+         const int b = j & 1;
+         const bool got = bar_wait(&acc_full[b], (unsigned int)(j >> 1) & 1u);
+         if (!__all_sync(0xffffffffu, got && !tc_aborted(&abort_s))) {
+            if (lane == 0) tc_abort(&abort_s, err, FTC_ERR);
+            break;
+         }
+         fence_after_sync();
+         float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll 1
+         for (int grp = 0; grp < 4; grp++) {
+            float mv[16], cv[16];
+            const unsigned int col = (unsigned int)(b * 256 + 64 * ih + 16 * grp);
+            tmem_ld16(trow + col, mv);
+            tmem_ld16(trow + col + 128, cv);
+            tmem_wait2(mv, cv);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+               const int it = nt * FTC_NI + 16 * ih + 4 * grp + e;
+               const int4 hd = item[it];
+               if (hd.w == 0) continue;   // (uniform: padding items)
+               const float4 cf = coef[it];
+               float sn, cs;
+               sincos_poly((unsigned int)hd.x * ux + (unsigned int)hd.y * uy + (unsigned int)hd.z * uz, &sn, &cs);
+               const float w1r = mv[4 * e] + cv[4 * e], w1i = mv[4 * e + 1] + cv[4 * e + 1];
+               const float w2r = mv[4 * e + 2] + cv[4 * e + 2], w2i = mv[4 * e + 3] + cv[4 * e + 3];
+               const float f1 = fmaf(cs, w1i, sn * w1r), f2 = fmaf(cs, w2i, sn * w2r);
+               fx = fmaf(cf.x, f1, fx);
+               fy = fmaf(cf.y, f1, fy);
+               fz = fmaf(cf.z, f1, fmaf(cf.w, f2, fz));
+            }
+         }
+         fence_before_sync();
+         __syncwarp();
+         if (lane == 0) bar_arrive(&acc_empty[b]);
+         kahan_add_tc(Fx, Cx, fx);
+         kahan_add_tc(Fy, Cy, fy);
+         kahan_add_tc(Fz, Cz, fz);
+      }
+      float *rr = red + ((size_t)ih * 128 + r) * 3;
+      rr[0] = Fx - Cx;
+      rr[1] = Fy - Cy;
+      rr[2] = Fz - Cz;
+   }
+   fence_before_sync();
+   __syncthreads();
+   if (w < 4) {
+      const int r = 32 * w + lane, i = tile * 128 + r;
+      if (i < n && !tc_aborted(&abort_s)) {
+         const double q = chg[slots[i]];
+         const float *r0 = red + (size_t)r * 3, *r1 = red + (size_t)(128 + r) * 3;
+         double *dst = fpart + (size_t)blockIdx.y * 3 * n;
+         dst[i] = q * ((double)r0[0] + (double)r1[0]);
+         dst[n + i] = q * ((double)r0[1] + (double)r1[1]);
+         dst[2 * (size_t)n + i] = q * ((double)r0[2] + (double)r1[2]);
+      }
+   }
+   if (w == 9) {
+      __syncwarp();
+      fence_after_sync();
+      tmem_dealloc(tmem, 512);
+   }
+}
+
+int ks_force_tc_splits(int) { return FTC_SPLITS; }
+
+int ks_force_tc(cudaStream_t st, int nsites, const KsDev &d, int nitems_padded, const double *chg,
+                const int *slots, float dkz, double *fpart, int *err)
+{
+   const int np128 = (nsites + 127) / 128 * 128;
+   k_zsite_tc<<<(unsigned int)(((long long)np128 * 16 + 255) / 256), 256, 0, st>>>(nsites, np128, d.ph32.p,
+                                                                                    d.zsite.p);
+   k_utab_tc<<<(nitems_padded + 7) / 8, 256, 0, st>>>(nitems_padded, d.tc_item.p, d.tc_k0.p, d.tc_kxy.p,
+                                                      d.kdat32.p, dkz, d.utab.p, d.tc_coef.p);
+   k_force_tc<<<dim3(np128 / 128, FTC_SPLITS), FTC_THREADS, FTC_SMEM, st>>>(
+       d.tc_item.p, d.tc_coef.p, nitems_padded, d.ph32.p, d.zsite.p, d.utab.p, chg, slots, nsites, fpart, err);
+   return FTC_SPLITS;
+}
+
+size_t ks_tc_zsite_len(int nsites)
+{
+   return (size_t)((nsites + 127) / 128) * (FTC_ABYTES / 16);
+}
+
+size_t ks_tc_utab_len(int nitems_padded)
+{
+   return (size_t)(nitems_padded / FTC_NI) * 8 * (FTC_BBYTES / 16);
+}
+
+// Shared-memory sizes of the tensor-core kernels, set once per device
+// outside any stream capture (from ks_prepare).
+cudaError_t ks_tc_init(int device)
+{
+   static unsigned long long done = 0;
+   if (device >= 0 && device < 64 && (done >> device) & 1ull) return cudaSuccess;
+   cudaError_t e = cudaFuncSetAttribute(k_sfac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+   if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_force_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, FTC_SMEM);
+   if (e == cudaSuccess && device >= 0 && device < 64) done |= 1ull << device;
+   return e;
+}
+
+}  // namespace mdgpu

@@ -14,6 +14,7 @@ namespace mdgpu {
 
 constexpr int NPOTP = 8;          // parameters per potential (src/defs.h:144)
 constexpr int KI = 16;            // k-vectors per k-space work item
+constexpr int KT = 64;            // k-vectors per tensor-core structure-factor item (4 KI runs)
 constexpr int FT_THREADS = 128;   // k_force32: threads per block, two sites each
 constexpr double PI = 3.14159265358979323846;
 constexpr double ALPHAMIN = 1e-7; // src/defs.h:181
@@ -52,6 +53,12 @@ struct KList {
    double key[12];                 // h, k_cutoff, alpha
    double vol = 0;
    double hinv[9];
+   // tensor-core structure factor: runs of up to KT l values of a column,
+   // largest count first, padded with empty runs to a multiple of 128
+   std::vector<int4> tc_item;      // (h, k, l0, count)
+   std::vector<int4> tc_k0;        // first k index of each KI run of the item (-1 past its end)
+   std::vector<float2> tc_kxy;     // (kx, ky) of the item's column
+   int tc_nitems = 0;              // before padding
 };
 
 mdgpu_status build_klist(const double *h, const mdgpu_control &ctl, KList &kl);
@@ -162,6 +169,14 @@ struct KsDev {
    // charged sites only (a site without charge adds nothing to S(k) and
    // gets no k-space force): their slots in link-cell order
    DBuf<int> kslots, kscan, kbsum;
+   // tensor-core structure factor: its items and the per-site z tables as
+   // split bf16 MMA operands (kspace_tc.cu)
+   DBuf<int4> tc_item, tc_k0;
+   DBuf<float2> tc_kxy;
+   DBuf<uint4> ztab;       // structure factor: z tables as the B operand, per 16 sites
+   DBuf<uint4> zsite;      // force pass: z tables as the A operand, per 128 sites
+   DBuf<uint4> utab;       // force pass: per-item coefficient rows (B operand)
+   DBuf<float4> tc_coef;   // per item: kx s1, ky s1, kz0 s1, dkz s2 (row scales s)
 };
 
 // Buffers of the adjoint (parameter-gradient) passes.
@@ -276,8 +291,12 @@ struct mdgpu_ctx {
    // the k-space passes run over every site, not only the charged ones
    // (the adjoint's backward passes read every site's phases)
    bool ks_all_sites = false;
+   // mixed form: structure factor on the tensor cores (MDGPU_KSPACE_TC=0
+   // at context creation selects the CUDA-core pass)
+   bool tc_sfac = true;
    uint64_t ncharged_gen = 0;       // configuration the count below is for
    int ncharged = 0;                // sites with a nonzero charge
+   double qmax = 0;                 // and their largest |q|
    cudaEvent_t ev[MDGPU_NPHASES + 1] = {};
    // second (high-priority) stream: the k-space passes run on it beside
    // the pair kernel
@@ -325,6 +344,20 @@ struct KsShape {
 // Chunks of the structure-factor pass and k-splits of a per-site pass
 // (ipt items per thread, spt sites per thread).
 KsShape ks_shape(int N, int nitems, int ipt, int spt);
+// Tensor-core structure factor (kspace_tc.cu): z tables + product into
+// part32 ([chunks][nk]); returns the number of chunks.
+int ks_sfac_tc(cudaStream_t st, int nsites, int nk, const KsDev &d, int ntiles, double qmax, int *err);
+// Tensor-core force pass over the charged slots: coefficient rows from the
+// per-k (A, B, kz), then F_slot * q into fpart[split][3][nsites]; returns the
+// number of splits.
+int ks_force_tc(cudaStream_t st, int nsites, const KsDev &d, int nitems_padded, const double *chg,
+                const int *slots, float dkz, double *fpart, int *err);
+int ks_force_tc_splits(int nsites);
+size_t ks_tc_zsite_len(int nsites);
+size_t ks_tc_utab_len(int nitems_padded);
+cudaError_t ks_tc_init(int device);
+size_t ks_tc_ztab_len(int nsites);
+int ks_tc_chunks(int nsites);
 // api.cu
 mdgpu_status fail(mdgpu_ctx *c, mdgpu_status s, const std::string &msg);
 mdgpu_status cuda_check(mdgpu_ctx *c, cudaError_t e, const char *what);

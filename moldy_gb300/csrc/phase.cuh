@@ -34,4 +34,16 @@ __device__ __forceinline__ void sincos_poly(unsigned int p, float *s, float *c)
    *c = cs;
 }
 
+// exp(2 pi i p / 2^32) for a 32-bit phase p, to about 1 FP32 ulp: the top 24
+// bits go exactly into sincospif, the low 8 bits (< 2^-23 revolution) are
+// added to first order.
+__device__ __forceinline__ void sincos_rev32(unsigned int p, float *s, float *c)
+{
+   float s0, c0;
+   sincospif((float)(int)(p & 0xFFFFFF00u) * 4.656612873077393e-10f, &s0, &c0);   // 2^-31
+   const float d = (float)(p & 0xFFu) * 1.4629180792671596e-09f;                  // 2 pi / 2^32
+   *c = fmaf(-s0, d, c0);
+   *s = fmaf(c0, d, s0);
+}
+
 }  // namespace mdgpu

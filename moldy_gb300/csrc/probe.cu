@@ -84,3 +84,109 @@ extern "C" mdgpu_status mdgpu_fma_peak(int device, int fp64, double *tflops)
    *tflops = flops / (best * 1e-3) / 1e12;
    return MDGPU_OK;
 }
+
+// ------------------------------------------------------- tensor-core probe
+// One CTA computes D = A0 B0^T and then (unless flags & 4) D += A1 B1^T,
+// negating A1 if flags & 2, with M = 128, N = n, K = 16 (bf16 operands, FP32
+// accumulation in tensor memory), operands in the K-major unswizzled layout
+// of tc.cuh.  flags & 1 exchanges the two offset fields of the operand
+// descriptors (the operand regions are sized so that both readings stay
+// inside them).  It checks the operand layout, the negation flag and the
+// rounding of the accumulator against a host computation.
+#include "tc.cuh"
+
+namespace mdgpu {
+
+constexpr int TCP_REGION = 32768;   // bytes per operand region
+
+__global__ void __launch_bounds__(128)
+k_tc_probe(const uint4 *__restrict__ a0, const uint4 *__restrict__ b0, const uint4 *__restrict__ a1,
+           const uint4 *__restrict__ b1, int n, int flags, float *__restrict__ d, int *__restrict__ err)
+{
+   using namespace tc;
+   extern __shared__ __align__(1024) unsigned char sm[];
+   __shared__ __align__(8) uint64_t bar;
+   __shared__ unsigned int taddr_s;
+   const int m = threadIdx.x, w = m >> 5;
+   unsigned char *A0 = sm, *A1 = sm + TCP_REGION, *B0 = sm + 2 * TCP_REGION, *B1 = sm + 3 * TCP_REGION;
+   for (int i = m; i < 4 * TCP_REGION / 16; i += 128) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
+   __syncthreads();
+   for (int g = 0; g < 2; g++) {
+      const int off = g * 2048 + (m >> 3) * 128 + (m & 7) * 16;
+      *reinterpret_cast<uint4 *>(A0 + off) = a0[m * 2 + g];
+      *reinterpret_cast<uint4 *>(A1 + off) = a1[m * 2 + g];
+      for (int r = m; r < n; r += 128) {
+         const int offb = g * (n / 8) * 128 + (r >> 3) * 128 + (r & 7) * 16;
+         *reinterpret_cast<uint4 *>(B0 + offb) = b0[r * 2 + g];
+         *reinterpret_cast<uint4 *>(B1 + offb) = b1[r * 2 + g];
+      }
+   }
+   fence_async_smem();
+   if (m == 0) {
+      bar_init(&bar, 1);
+      bar_init_fence();
+   }
+   __syncwarp();
+   if (w == 0) tmem_alloc(&taddr_s, 256);
+   fence_before_sync();
+   __syncthreads();
+   fence_after_sync();
+   const unsigned int tb = taddr_s;
+   if (m == 0) {
+      const bool swap = flags & 1;
+      auto desc = [&](const unsigned char *p, unsigned int lbo) {
+         return swap ? sdesc(saddr(p), 128u, lbo) : sdesc(saddr(p), lbo, 128u);
+      };
+      mma_bf16(tb, desc(A0, 2048u), desc(B0, 16u * n), idesc_bf16(128, n, false), false);
+      if (!(flags & 4)) mma_bf16(tb, desc(A1, 2048u), desc(B1, 16u * n), idesc_bf16(128, n, (flags & 2) != 0), true);
+      mma_commit(&bar);
+   }
+   __syncwarp();
+   const bool ok = __all_sync(0xffffffffu, bar_wait(&bar, 0));
+   if (!ok && (m & 31) == 0) atomicOr(err, 1);
+   fence_after_sync();
+   if (ok)
+      for (int c = 0; c < n; c += 16) {
+         float v[16];
+         tmem_ld16(tb + ((unsigned int)(32 * w) << 16) + (unsigned int)c, v);
+         tmem_wait(v);
+         for (int j = 0; j < 16; j++) d[m * n + c + j] = v[j];
+      }
+   fence_before_sync();
+   __syncthreads();
+   if (w == 0) tmem_dealloc(tb, 256);
+}
+
+}  // namespace mdgpu
+
+// a0, a1: 128 x 16 bf16 (row-major); b0, b1: n x 16; d: 128 x n FP32.
+// n a multiple of 16 in 16..128.
+extern "C" mdgpu_status mdgpu_tc_probe(int device, const unsigned short *a0, const unsigned short *b0,
+                                       const unsigned short *a1, const unsigned short *b1, int n, int flags,
+                                       float *d)
+{
+   using namespace mdgpu;
+   if (!a0 || !b0 || !a1 || !b1 || !d || n < 16 || n > 128 || n % 16) return MDGPU_E_ARG;
+   if (cudaSetDevice(device) != cudaSuccess) return MDGPU_E_CUDA;
+   const size_t sa = 128 * 16 * 2, sb = (size_t)n * 16 * 2, sd = 128 * (size_t)n * 4;
+   unsigned char *buf = nullptr;
+   if (cudaMalloc(&buf, 2 * sa + 2 * sb + sd + 16) != cudaSuccess) return MDGPU_E_NOMEM;
+   unsigned char *pa0 = buf, *pa1 = buf + sa, *pb0 = buf + 2 * sa, *pb1 = pb0 + sb, *pd = pb1 + sb;
+   int *perr = reinterpret_cast<int *>(pd + sd);
+   cudaMemcpy(pa0, a0, sa, cudaMemcpyHostToDevice);
+   cudaMemcpy(pa1, a1, sa, cudaMemcpyHostToDevice);
+   cudaMemcpy(pb0, b0, sb, cudaMemcpyHostToDevice);
+   cudaMemcpy(pb1, b1, sb, cudaMemcpyHostToDevice);
+   cudaMemset(perr, 0, sizeof(int));
+   cudaFuncSetAttribute(k_tc_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * TCP_REGION);
+   k_tc_probe<<<1, 128, 4 * TCP_REGION>>>(reinterpret_cast<const uint4 *>(pa0), reinterpret_cast<const uint4 *>(pb0),
+                                          reinterpret_cast<const uint4 *>(pa1), reinterpret_cast<const uint4 *>(pb1),
+                                          n, flags, reinterpret_cast<float *>(pd), perr);
+   cudaError_t e = cudaDeviceSynchronize();
+   int herr = 0;
+   if (e == cudaSuccess) e = cudaMemcpy(d, pd, sd, cudaMemcpyDeviceToHost);
+   if (e == cudaSuccess) e = cudaMemcpy(&herr, perr, sizeof(int), cudaMemcpyDeviceToHost);
+   cudaFree(buf);
+   if (e != cudaSuccess) return MDGPU_E_CUDA;
+   return herr ? MDGPU_E_CUDA : MDGPU_OK;
+}
