@@ -29,7 +29,10 @@ Default arm (--impl gb300):
              copy of the site co-ordinates and the D2H copy of forces,
              energies and stress inside every call;
   roofline   the dominant kernel's algorithmic FLOP/s (reference op counts)
-             against the FP32 FMA peak measured on this GPU;
+             against the bound of the pipe it runs on: the measured bf16
+             tensor peak (MEASURED_PEAKS.json, sustained) for the tensor-core
+             reciprocal-space kernels, with the MMA work they issue beside
+             it; the FP32 FMA peak measured on this GPU for the pair kernel;
   cpu_baseline  the reference algorithm's C restatement (oracle/port),
              -O2 -ffast-math, on all host cores, on a bounded sample of the
              force evaluation (the reference's integrator is under 1% of its
@@ -73,6 +76,50 @@ STEP_PS = 0.001                      # 1 fs
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks():
+    """The machine's measured HBM and bf16 tensor peaks (MEASURED_PEAKS.json at
+    the repository root), or the stated fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return {"hbm_gbs": float(m["hbm_gbs"]), "bf16": float(m["bf16_tflops"]),
+                "bf16_sustained": float(m["bf16_tflops_sustained"]), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16": 1900.0, "bf16_sustained": 1700.0, "source": "fallback"}
+
+
+def tc_mma_flops(sysm, nq):
+    """Tensor-core work the two reciprocal-space kernels issue per launch
+    (bf16 MMA flops, the split-operand term products and the padding of
+    items to 16-column multiples included), from the k-list columns exactly
+    as the library builds them: runs of up to 64 l values per (h,k) column,
+    largest count first, 128 per structure-factor tile, 32 per force tile."""
+    import math
+    h = np.asarray(sysm.h, np.float64).reshape(9)
+    kc = sysm.control.k_cutoff
+    hmax = int(math.floor(kc / (2 * math.pi) * h[0]))
+    kmax = int(math.floor(kc / (2 * math.pi) * math.sqrt(h[1] ** 2 + h[4] ** 2)))
+    lmax = int(math.floor(kc / (2 * math.pi) * math.sqrt(h[2] ** 2 + h[5] ** 2 + h[8] ** 2)))
+    hi = (2 * math.pi * np.linalg.inv(h.reshape(3, 3))).reshape(9)
+    counts = []
+    for hh in range(hmax + 1):
+        for k in range(0 if hh == 0 else -kmax, kmax + 1):
+            kx, ky, kzt = hh * hi[0] + k * hi[3], hh * hi[1] + k * hi[4], hh * hi[2] + k * hi[5]
+            ls = np.arange(1 if hh == 0 and k == 0 else -lmax, lmax + 1)
+            n = int(np.count_nonzero((kzt + ls * hi[8]) ** 2 + kx * kx + ky * ky < kc * kc))
+            while n > 0:
+                counts.append(min(n, 64))
+                n -= 64
+    counts = sorted(counts, reverse=True)
+    counts += [0] * (-len(counts) % 128)
+    np16 = (nq + 15) // 16 * 16
+    sfac = sum((np16 // 16) * 24 * 2 * 128 * 16 * ((counts[t] + 15) // 16 * 16)
+               for t in range(0, len(counts), 128))
+    force = ((nq + 127) // 128) * sum(12 * ((counts[t] + 15) // 16) * 2 * 128 * 128 * 16
+                                      for t in range(0, len(counts), 32))
+    return {"sfac": float(sfac), "kforce": float(force)}
 
 
 def make_workload(seed=7):
@@ -402,7 +449,25 @@ def run_gpu(args):
     dom = max(work, key=lambda k: phases.get(k, 0.0))
     achieved = work[dom] / (phases[dom] * 1e-3) / 1e12
     traffic = traffic_from_profiles().get(dom)
-    kernel_names = {"kforce": "k_force32", "sfac": "k_sfac32", "pairs": "k_pairs<LJ,erfc,mixed>"}
+    kernel_names = {"kforce": "k_force_tc", "sfac": "k_sfac_tc", "pairs": "k_pairs<LJ,erfc,mixed>"}
+    peaks = measured_peaks()
+    mma = tc_mma_flops(sysA, n_q)
+    if dom in mma:
+        # tensor-core kernels: the bound is the bf16 tensor pipe (sustained,
+        # as the kernel runs inside a long step); achieved counts the
+        # reference's own FP32 operations, the MMA work they expand to (three
+        # bf16 terms per operand, six term products, complex arithmetic as
+        # real products, padded columns) is reported beside it
+        peak, unit, bound = peaks["bf16_sustained"], "TFLOP/s", "tensor"
+        peak_source = (f"{peaks['source']} cuBLAS bf16 GEMM throughput, sustained "
+                       f"(MEASURED_PEAKS.json bf16_tflops_sustained)")
+        mma_rate = mma[dom] / (phases[dom] * 1e-3) / 1e12
+        mma_line = {"flops_per_launch": mma[dom], "tflops": mma_rate, "frac": mma_rate / peak,
+                    "expansion": mma[dom] / work[dom]}
+    else:
+        peak, unit, bound = tf32.value, "TFLOP/s", "fp32"
+        peak_source = "measured FP32 FMA throughput on this GPU (mdgpu_fma_peak)"
+        mma_line = None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -442,14 +507,15 @@ def run_gpu(args):
                                    "host arrays each step"},
         "gpu_launches": int(launches_timed),
         "phases_ms": phases,
-        "roofline": {"kernel": kernel_names[dom], "bound": "fp32", "achieved": achieved,
-                     "work": (f"{FLOPS_FORCE_PER_SITE_K} flops per (charged site, k): {n_q} sites x {nk} k"
-                              if dom == "kforce" else dom),
-                     "peak": tf32.value, "unit": "TFLOP/s", "frac": achieved / tf32.value,
-                     "traffic": traffic,
-                     "peak_source": "measured FP32 FMA throughput on this GPU (mdgpu_fma_peak), "
-                                    "MEASURED_PEAKS.json carries only HBM and bf16",
-                     "fp64_peak": tf64.value},
+        "roofline": {"kernel": kernel_names[dom], "bound": bound, "achieved": achieved,
+                     "work": ({"kforce": f"{FLOPS_FORCE_PER_SITE_K} flops per (charged site, k): "
+                                         f"{n_q} sites x {nk} k",
+                               "sfac": f"{FLOPS_SFAC_PER_SITE_K} flops per (charged site, k): "
+                                       f"{n_q} sites x {nk} k",
+                               "pairs": f"{FLOPS_PAIR_LJ_ERFC} flops per evaluated pair"}[dom]),
+                     "peak": peak, "unit": unit, "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_source, "mma": mma_line,
+                     "fp32_fma_peak": tf32.value, "fp64_fma_peak": tf64.value},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "wall_s_mixed_timed": wall_mixed,

@@ -994,6 +994,15 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
                                             hinv[3], hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], mixed ? 1 : 0,
                                             d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
    CK(cudaGetLastError());
+   // mixed form over the charged sites: both passes on the tensor cores
+   const bool tc = mixed && compact && c->tc_sfac;
+   if (tc) {
+      CK(d.ztab.ensure(ks_tc_ztab_len(Nk)));
+      CK(d.zsite.ensure(ks_tc_zsite_len(Nk)));
+      CK(d.utab.ensure(ks_tc_utab_len((int)kl.tc_item.size())));
+      ks_tables_tc(st, Nk, d);
+      c->launches += 2;
+   }
    KsShape sh = mixed ? ks_shape(Nk, ni, 1, 2) : ks_shape(Nk, ni, 1, 1);
    if (nf > 0) {
       CK(d.fslot.ensure(nf));
@@ -1004,11 +1013,9 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    }
    phase_mark(c, MDGPU_PH_SFAC);
    const dim3 gs((ni + 127) / 128, sh.chunks);
-   if (mixed && compact && c->tc_sfac) {
+   if (tc) {
       CK(d.part32.ensure((size_t)ks_tc_chunks(Nk) * nk));
-      CK(d.ztab.ensure(ks_tc_ztab_len(Nk)));
       sh.chunks = ks_sfac_tc(st, Nk, nk, d, (int)(kl.tc_item.size() / 128), c->qmax, &out->err);
-      c->launches += 1;
    } else if (mixed) {
       CK(d.part32.ensure((size_t)sh.chunks * nk));
       k_sfac32<<<gs, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph32.p, d.zp32.p, Nk, sh.chunk, nk, d.part32.p,
@@ -1055,17 +1062,17 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    }
    k_kfinal<<<1, 512, 0, st>>>(d.blk.p, nbk, out);
    CK(cudaGetLastError());
-   const bool tcf = mixed && compact && c->tc_sfac;
-   if (tcf) sh.splits = ks_force_tc_splits(Nk);
+   if (tc) {
+      sh.splits = ks_force_tc_splits(Nk);
+      ks_coef_tc(st, d, (int)kl.tc_item.size(), (float)kl.dkz);
+      c->launches += 1;
+   }
    CK(d.fpart.ensure((size_t)sh.splits * 3 * Nk));
    phase_mark(c, MDGPU_PH_KFORCE);
    dim3 gf((Nk + 255) / 256, sh.splits);
    const int obase = compact ? -1 : 0;   // partial rows by slot of the charged list, or by site
-   if (tcf) {
-      CK(d.zsite.ensure(ks_tc_zsite_len(Nk)));
-      CK(d.utab.ensure(ks_tc_utab_len((int)kl.tc_item.size())));
-      ks_force_tc(st, Nk, d, (int)kl.tc_item.size(), c->rd.chg.p, slots, (float)kl.dkz, d.fpart.p, &out->err);
-      c->launches += 2;
+   if (tc) {
+      ks_force_tc(st, Nk, d, (int)kl.tc_item.size(), c->rd.chg.p, slots, d.fpart.p, &out->err);
    } else if (mixed)
       k_force32<<<gf, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
                                            d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, slots, Nk, obase,

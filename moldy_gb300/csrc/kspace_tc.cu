@@ -258,13 +258,11 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
    }
 }
 
-// Host side: z tables, then the product.  Returns the number of site
-// chunks (rows of part).
+// The structure-factor product into part32 ([chunks][nk]); returns the
+// number of chunks.
 int ks_sfac_tc(cudaStream_t st, int nsites, int nk, const KsDev &d, int ntiles, double qmax, int *err)
 {
    const int np = (nsites + TC_KS - 1) / TC_KS * TC_KS;
-   const long long nthr = (long long)(np / 8) * 128;
-   k_ztab_tc<<<(unsigned int)((nthr + 255) / 256), 256, 0, st>>>(nsites, np, d.ph32.p, d.ztab.p);
    const int nchunks = (np + TC_CHUNK - 1) / TC_CHUNK;
    // charges scaled by a power of two to |q| <= 1 (exact), undone on the partials
    int e = 0;
@@ -274,7 +272,6 @@ int ks_sfac_tc(cudaStream_t st, int nsites, int nk, const KsDev &d, int ntiles, 
                                                           1.0f / qs, qs, d.part32.p, err);
    return nchunks;
 }
-
 
 size_t ks_tc_ztab_len(int nsites)
 {
@@ -616,14 +613,29 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
 
 int ks_force_tc_splits(int) { return FTC_SPLITS; }
 
-int ks_force_tc(cudaStream_t st, int nsites, const KsDev &d, int nitems_padded, const double *chg,
-                const int *slots, float dkz, double *fpart, int *err)
+// Host side.  Per-site operand tables (after k_prep): the z tables as the
+// structure factor's B operand and as the force pass's A operand.
+void ks_tables_tc(cudaStream_t st, int nsites, const KsDev &d)
 {
+   const int np = (nsites + TC_KS - 1) / TC_KS * TC_KS;
+   const long long nthr = (long long)(np / 8) * 128;
+   k_ztab_tc<<<(unsigned int)((nthr + 255) / 256), 256, 0, st>>>(nsites, np, d.ph32.p, d.ztab.p);
    const int np128 = (nsites + 127) / 128 * 128;
    k_zsite_tc<<<(unsigned int)(((long long)np128 * 16 + 255) / 256), 256, 0, st>>>(nsites, np128, d.ph32.p,
                                                                                     d.zsite.p);
+}
+
+// The force pass's coefficient rows (after the per-k reduction).
+void ks_coef_tc(cudaStream_t st, const KsDev &d, int nitems_padded, float dkz)
+{
    k_utab_tc<<<(nitems_padded + 7) / 8, 256, 0, st>>>(nitems_padded, d.tc_item.p, d.tc_k0.p, d.tc_kxy.p,
                                                       d.kdat32.p, dkz, d.utab.p, d.tc_coef.p);
+}
+
+int ks_force_tc(cudaStream_t st, int nsites, const KsDev &d, int nitems_padded, const double *chg,
+                const int *slots, double *fpart, int *err)
+{
+   const int np128 = (nsites + 127) / 128 * 128;
    k_force_tc<<<dim3(np128 / 128, FTC_SPLITS), FTC_THREADS, FTC_SMEM, st>>>(
        d.tc_item.p, d.tc_coef.p, nitems_padded, d.ph32.p, d.zsite.p, d.utab.p, chg, slots, nsites, fpart, err);
    return FTC_SPLITS;

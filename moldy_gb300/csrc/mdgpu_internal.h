@@ -344,15 +344,20 @@ struct KsShape {
 // Chunks of the structure-factor pass and k-splits of a per-site pass
 // (ipt items per thread, spt sites per thread).
 KsShape ks_shape(int N, int nitems, int ipt, int spt);
-// Tensor-core structure factor (kspace_tc.cu): z tables + product into
-// part32 ([chunks][nk]); returns the number of chunks.
+// Reciprocal-space passes on the tensor cores (kspace_tc.cu), mixed form:
+// per-site operand tables (after k_prep); the structure factor into part32
+// ([chunks][nk], returns the number of chunks); the force pass's per-item
+// coefficient rows (after the per-k reduction); the force pass, F_slot * q
+// into fpart[split][3][nsites] (returns the number of splits).
+void ks_tables_tc(cudaStream_t st, int nsites, const KsDev &d);
 int ks_sfac_tc(cudaStream_t st, int nsites, int nk, const KsDev &d, int ntiles, double qmax, int *err);
-// Tensor-core force pass over the charged slots: coefficient rows from the
-// per-k (A, B, kz), then F_slot * q into fpart[split][3][nsites]; returns the
-// number of splits.
+void ks_coef_tc(cudaStream_t st, const KsDev &d, int nitems_padded, float dkz);
 int ks_force_tc(cudaStream_t st, int nsites, const KsDev &d, int nitems_padded, const double *chg,
-                const int *slots, float dkz, double *fpart, int *err);
+                const int *slots, double *fpart, int *err);
 int ks_force_tc_splits(int nsites);
+cudaError_t ks_tc_init(int device);
+size_t ks_tc_ztab_len(int nsites);
+int ks_tc_chunks(int nsites);
 size_t ks_tc_zsite_len(int nsites);
 size_t ks_tc_utab_len(int nitems_padded);
 cudaError_t ks_tc_init(int device);
