@@ -377,6 +377,12 @@ mdgpu_status mdgpu_fma_peak(int device, int fp64, double *tflops);
  * n a multiple of 16 in 16..128.  No counterpart in the reference. */
 mdgpu_status mdgpu_tc_probe(int device, const unsigned short *a0, const unsigned short *b0,
                             const unsigned short *a1, const unsigned short *b1, int n, int flags, float *d);
+/* Tensor-core issue rate: in one CTA per SM (two if two_per_sm), issuers
+ * threads issue reps 128 x n x 16 bf16 MMAs in all over nacc accumulators
+ * each; bf16 TFLOP/s over the device.  n a multiple of 16 in 16..256,
+ * issuers 1..4, issuers * nacc * n <= 512 (256 with two CTAs per SM).  No
+ * counterpart in the reference. */
+mdgpu_status mdgpu_tc_rate(int device, int n, int reps, int nacc, int issuers, int two_per_sm, double *tflops);
 
 /* Potential at one distance (poteval, src/force.c:632-650): reference-site
  * charge 1, neighbour charge chgsq, Ewald alpha as given. */

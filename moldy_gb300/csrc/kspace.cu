@@ -302,6 +302,16 @@ __device__ __forceinline__ double bsum(double v, double *sh)
    return s;
 }
 
+// s += x with the rounding error carried in c (Kahan's compensated sum;
+// s - c is the running total).
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+   const float y = x - c;
+   const float t = s + y;
+   c = (t - s) - y;
+   s = t;
+}
+
 // Per k: S(k) over the structure-factor chunks, then the energy, stress and
 // force coefficients.  A block takes KR_K consecutive k (one per lane) and
 // spreads the chunks over its KR_W warps (chunks w, w + KR_W, ... in warp w:
@@ -320,18 +330,35 @@ k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__
    const int k = blockIdx.x * KR_K + lane;
    {
       double C = 0.0, S = 0.0;
-      if (k < nk)
-         for (int c = w; c < nchunks; c += KR_W) {
-            if (MIXED) {
+      if (k < nk) {
+         if (MIXED) {
+            // FP32 partials: two interleaved Kahan-compensated FP32 sums per
+            // lane (the FP64 pipe retires two lanes per clock per SM, a
+            // conversion and add per partial was the pass's bound), then FP64
+            float c0 = 0.f, e0 = 0.f, s0 = 0.f, f0 = 0.f, c1 = 0.f, e1 = 0.f, s1 = 0.f, f1 = 0.f;
+            int c = w;
+            for (; c + KR_W < nchunks; c += 2 * KR_W) {
+               const float2 v = p32[(size_t)c * nk + k], u = p32[(size_t)(c + KR_W) * nk + k];
+               kahan_add(c0, e0, v.x);
+               kahan_add(s0, f0, v.y);
+               kahan_add(c1, e1, u.x);
+               kahan_add(s1, f1, u.y);
+            }
+            if (c < nchunks) {
                const float2 v = p32[(size_t)c * nk + k];
-               C += (double)v.x;
-               S += (double)v.y;
-            } else {
+               kahan_add(c0, e0, v.x);
+               kahan_add(s0, f0, v.y);
+            }
+            C = ((double)c0 - (double)e0) + ((double)c1 - (double)e1);
+            S = ((double)s0 - (double)f0) + ((double)s1 - (double)f1);
+         } else {
+            for (int c = w; c < nchunks; c += KR_W) {
                const double2 v = p64[(size_t)c * nk + k];
                C += v.x;
                S += v.y;
             }
          }
+      }
       sC[w][lane] = C;
       sS[w][lane] = S;
    }
@@ -402,15 +429,6 @@ __global__ void __launch_bounds__(1024) k_kfinal(const double *__restrict__ blk,
 // ---------------------------------------------------------------- forces
 constexpr int FT_ITEMS = 64;
 
-// s += x with the rounding error carried in c (Kahan's compensated sum;
-// s - c is the running total).
-__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
-{
-   const float y = x - c;
-   const float t = s + y;
-   c = (t - s) - y;
-   s = t;
-}
 
 static_assert(KI == 16, "k_force32 unrolls item counts 1..16");
 

@@ -24,12 +24,14 @@
 // the FP32 path.  Each CTA sums 512 sites and writes one partial per k; the
 // partials are added in FP64 by the per-k reduction.
 //
-// CTA roles (192 threads): warps 0-3 build the A operand of each stage (one
-// item row per thread) and, at the end, read the accumulators back (a
-// warp reaches tensor-memory lanes 32 (w % 4) ..); warp 4 streams each
-// stage's z tables and site records by bulk copy; warp 5 owns the tensor
-// memory and issues the MMAs.  Stages are triple-buffered on mbarriers;
-// every wait is bounded and sets bit 3 of the error word when it expires.
+// CTA roles (320 threads): warps 0-7 build the A operand of each stage (one
+// item row and 8 of the stage's 16 sites per thread) and, at the end, read
+// the accumulators back (a warp reaches tensor-memory lanes 32 (w % 4) ..);
+// warp 8 copies the chunk's site records once and streams each stage's z
+// tables (bulk copies, four in flight); warp 9 owns the tensor memory and
+// issues the MMAs.  A operands are double-buffered, z tables quadruple-
+// buffered, on mbarriers; every wait is bounded and sets bit 3 of the error
+// word when it expires.
 #include <cmath>
 
 #include "mdgpu_internal.h"
@@ -39,18 +41,20 @@
 namespace mdgpu {
 
 constexpr int TC_KS = 16;                          // sites per stage (the K of one MMA)
-constexpr int TC_NS = 3;                           // stages in flight
+constexpr int TC_NSA = 2;                          // A-operand buffers
+constexpr int TC_NSB = 4;                          // z-table buffers (bulk copies in flight)
 constexpr int TC_TERM = 128 * TC_KS * 2;           // one 128-row bf16 operand of a stage: 4096 bytes
 constexpr int TC_ABYTES = 6 * TC_TERM;             // Ar, Ai x (hi, mid, lo)
 constexpr int TC_BBYTES = 3 * TC_TERM;             // [Zr | Zi] x (hi, mid, lo)
-constexpr int TC_PBYTES = TC_KS * 16;              // site records (u_x, u_y, u_z, q)
-constexpr int TC_STAGE = TC_ABYTES + TC_BBYTES + TC_PBYTES;
-constexpr int TC_SMEM = TC_NS * TC_STAGE;
 constexpr int TC_CHUNK = 512;                      // sites per CTA (one partial per k)
+constexpr int TC_PBYTES = TC_CHUNK * 16;           // the chunk's site records (u_x, u_y, u_z, q)
+constexpr int TC_AOFF = TC_PBYTES, TC_BOFF = TC_AOFF + TC_NSA * TC_ABYTES;
+constexpr int TC_SMEM = TC_BOFF + TC_NSB * TC_BBYTES;
 constexpr int TC_LBO = 16 * 128;                   // 8-column groups of a 128-row operand
 constexpr int TC_ERR = 8;                          // error-word bit: a stage wait expired
+constexpr int TC_THREADS = 320;                    // 8 operand/read-back warps, bulk-copy warp, MMA warp
 
-static_assert(TC_STAGE % 16 == 0 && TC_ABYTES % 1024 == 0, "stage buffers stay 16-byte aligned");
+static_assert(TC_AOFF % 1024 == 0 && TC_BOFF % 1024 == 0, "operand buffers stay aligned");
 static_assert(TC_CHUNK % TC_KS == 0, "chunks hold whole stages");
 static_assert(KT == 4 * KI && KT <= 64, "an item is four KI runs, Zr and Zi fit 128 rows");
 
@@ -99,14 +103,14 @@ __device__ __forceinline__ bool tc_aborted(const int *flag)
 }
 
 // Grid: (item tiles of 128, site chunks of TC_CHUNK).  part[chunk][k].
-__global__ void __launch_bounds__(192, 2)
+__global__ void __launch_bounds__(TC_THREADS, 2)
 k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const int4 *__restrict__ ph,
           const uint4 *__restrict__ ztab, int np, int nk, float qscale, float qunscale, float2 *__restrict__ part,
           int *__restrict__ err)
 {
    using namespace tc;
    extern __shared__ __align__(1024) unsigned char sm[];
-   __shared__ __align__(8) uint64_t full_b[TC_NS], full_a[TC_NS], empty[TC_NS], accf;
+   __shared__ __align__(8) uint64_t full_p, full_b[TC_NSB], empty_b[TC_NSB], full_a[TC_NSA], empty_a[TC_NSA], accf;
    __shared__ unsigned int tmem_s;
    __shared__ int abort_s;
    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -116,57 +120,64 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
    const int ncols = (item[tile * 128].w + 15) & ~15;   // the tile's largest count, rounded up
    if (ncols == 0 || nst <= 0) return;                  // (uniform over the CTA)
    if (tid == 0) {
-      for (int s = 0; s < TC_NS; s++) {
+      bar_init(&full_p, 1);
+      for (int s = 0; s < TC_NSB; s++) {
          bar_init(&full_b[s], 1);
-         bar_init(&full_a[s], 4);
-         bar_init(&empty[s], 1);
+         bar_init(&empty_b[s], 1);
+      }
+      for (int s = 0; s < TC_NSA; s++) {
+         bar_init(&full_a[s], 8);
+         bar_init(&empty_a[s], 1);
       }
       bar_init(&accf, 1);
       abort_s = 0;
       bar_init_fence();
    }
    __syncwarp();
-   if (w == 5) tmem_alloc(&tmem_s, 256);   // [0,128): hh sums, [128,256): the smaller terms
+   if (w == 9) tmem_alloc(&tmem_s, 256);   // [0,128): hh sums, [128,256): the smaller terms
    fence_before_sync();
    __syncthreads();
    fence_after_sync();
    const unsigned int tmem = tmem_s;
 
-   if (w == 4) {
-      // ---- bulk copies of each stage's z tables and site records
+   if (w == 8) {
+      // ---- bulk copies: the chunk's site records once, each stage's z tables
       if (lane == 0) {
+         bar_expect_tx(&full_p, (unsigned int)nst * TC_KS * 16);
+         bulk_load(sm, ph + s0, (unsigned int)nst * TC_KS * 16, &full_p);
          int issued = 0;
          for (int st = 0; st < nst; st++) {
-            const int s = st % TC_NS;
-            if (st >= TC_NS && !bar_wait(&empty[s], (unsigned int)(st / TC_NS - 1) & 1u)) {
+            const int s = st % TC_NSB;
+            if (st >= TC_NSB && !bar_wait(&empty_b[s], (unsigned int)(st / TC_NSB - 1) & 1u)) {
                tc_abort(&abort_s, err);
                break;
             }
             if (tc_aborted(&abort_s)) break;
-            unsigned char *sb = sm + s * TC_STAGE;
-            bar_expect_tx(&full_b[s], TC_BBYTES + TC_PBYTES);
-            bulk_load(sb + TC_ABYTES, ztab + (size_t)(s0 / TC_KS + st) * (TC_BBYTES / 16), TC_BBYTES, &full_b[s]);
-            bulk_load(sb + TC_ABYTES + TC_BBYTES, ph + s0 + st * TC_KS, TC_PBYTES, &full_b[s]);
+            bar_expect_tx(&full_b[s], TC_BBYTES);
+            bulk_load(sm + TC_BOFF + s * TC_BBYTES, ztab + (size_t)(s0 / TC_KS + st) * (TC_BBYTES / 16), TC_BBYTES,
+                      &full_b[s]);
             issued = st + 1;
          }
          // copies still in flight complete before the CTA's shared memory goes
-         for (int st = issued > TC_NS ? issued - TC_NS : 0; st < issued; st++)
-            bar_wait(&full_b[st % TC_NS], (unsigned int)(st / TC_NS) & 1u);
+         bar_wait(&full_p, 0);
+         for (int st = issued > TC_NSB ? issued - TC_NSB : 0; st < issued; st++)
+            bar_wait(&full_b[st % TC_NSB], (unsigned int)(st / TC_NSB) & 1u);
       }
-   } else if (w == 5) {
-      // ---- MMA issue
+   } else if (w == 9) {
+      // ---- MMA issue (the real and imaginary parts' MMAs alternate, so
+      // consecutive MMAs write different accumulators)
       if (lane == 0) {
          const unsigned int idn = idesc_bf16(128, ncols, false), idneg = idesc_bf16(128, ncols, true);
          const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
          for (int st = 0; st < nst; st++) {
-            const int s = st % TC_NS;
-            const unsigned int par = (unsigned int)(st / TC_NS) & 1u;
-            if (!bar_wait(&full_a[s], par) || !bar_wait(&full_b[s], par)) {
+            const int sa = st % TC_NSA, sb = st % TC_NSB;
+            if (!bar_wait(&full_a[sa], (unsigned int)(st / TC_NSA) & 1u) ||
+                !bar_wait(&full_b[sb], (unsigned int)(st / TC_NSB) & 1u)) {
                tc_abort(&abort_s, err);
                break;
             }
             fence_after_sync();
-            const unsigned int a = saddr(sm + s * TC_STAGE), b = a + TC_ABYTES;
+            const unsigned int a = saddr(sm + TC_AOFF + sa * TC_ABYTES), b = saddr(sm + TC_BOFF + sb * TC_BBYTES);
 #pragma unroll
             for (int p = 0; p < 6; p++) {
                const unsigned int d = tmem + (p == 0 ? 0u : 128u);
@@ -180,26 +191,28 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
                mma_bf16(d, ai, zi, idneg, true);       // Re -= Ai Zi
                mma_bf16(d + 64, ai, zr, idn, true);    // Im += Ai Zr
             }
-            mma_commit(&empty[s]);
+            mma_commit(&empty_a[sa]);
+            mma_commit(&empty_b[sb]);
          }
          mma_commit(&accf);   // also after an abort: the readers wait on it
       }
    } else {
-      // ---- A operand: q_j seed_ij for this thread's item row
-      const int m = tid;
+      // ---- A operand: q_j seed_ij for this thread's item row and the
+      // stage's sites 8 g .. 8 g + 7
+      const int m = tid & 127, g = tid >> 7;
       const int4 hd = item[tile * 128 + m];
       const unsigned int H = (unsigned int)hd.x, K = (unsigned int)hd.y, L = (unsigned int)hd.z;
+      if (!bar_wait(&full_p, 0)) tc_abort(&abort_s, err);
       for (int st = 0; st < nst; st++) {
-         const int s = st % TC_NS;
+         const int s = st % TC_NSA;
          if (tc_aborted(&abort_s)) break;
-         if (!bar_wait(&full_b[s], (unsigned int)(st / TC_NS) & 1u)) {
+         if (st >= TC_NSA && !bar_wait(&empty_a[s], (unsigned int)(st / TC_NSA - 1) & 1u)) {
             tc_abort(&abort_s, err);
             break;
          }
-         unsigned char *A = sm + s * TC_STAGE;
-         const int4 *P = reinterpret_cast<const int4 *>(A + TC_ABYTES + TC_BBYTES);
-#pragma unroll
-         for (int g = 0; g < 2; g++) {
+         unsigned char *A = sm + TC_AOFF + s * TC_ABYTES;
+         const int4 *P = reinterpret_cast<const int4 *>(sm) + st * TC_KS;
+         {
             unsigned int hr[4], mr[4], lr[4], hi[4], mi[4], li[4];
 #pragma unroll
             for (int jp = 0; jp < 4; jp++) {
@@ -223,16 +236,17 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
          __syncwarp();
          if (lane == 0) bar_arrive(&full_a[s]);
       }
-      // ---- read back: row m of the tile, columns t (Re) and 64 + t (Im)
+      // ---- read back: row m of the tile, columns t (Re) and 64 + t (Im),
+      // t in [32 g, 32 g + 32)
       const bool done = bar_wait(&accf, 0);
       const bool ok = __all_sync(0xffffffffu, done && !tc_aborted(&abort_s));
       if (!done && lane == 0) tc_abort(&abort_s, err);
       fence_after_sync();
       if (ok) {
          const int4 k0 = item_k0[tile * 128 + m];
-         const unsigned int trow = tmem + ((unsigned int)(32 * w) << 16);
+         const unsigned int trow = tmem + ((unsigned int)(32 * (w & 3)) << 16);
          float2 *dst = part + (size_t)chunk * nk;
-         for (int t0 = 0; t0 < ncols; t0 += 16) {
+         for (int t0 = 32 * g; t0 < min(ncols, 32 * g + 32); t0 += 16) {
             float re[16], im[16], re2[16], im2[16];
             tmem_ld16(trow + t0, re);
             tmem_ld16(trow + 64 + t0, im);
@@ -251,7 +265,7 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
    }
    fence_before_sync();
    __syncthreads();
-   if (w == 5) {
+   if (w == 9) {
       __syncwarp();
       fence_after_sync();
       tmem_dealloc(tmem, 256);
@@ -268,7 +282,7 @@ int ks_sfac_tc(cudaStream_t st, int nsites, int nk, const KsDev &d, int ntiles, 
    int e = 0;
    std::frexp(qmax > 0 ? qmax : 1.0, &e);
    const float qs = std::ldexp(1.0f, e);
-   k_sfac_tc<<<dim3(ntiles, nchunks), 192, TC_SMEM, st>>>(d.tc_item.p, d.tc_k0.p, d.ph32.p, d.ztab.p, np, nk,
+   k_sfac_tc<<<dim3(ntiles, nchunks), TC_THREADS, TC_SMEM, st>>>(d.tc_item.p, d.tc_k0.p, d.ph32.p, d.ztab.p, np, nk,
                                                           1.0f / qs, qs, d.part32.p, err);
    return nchunks;
 }
@@ -301,17 +315,21 @@ int ks_tc_chunks(int nsites)
 // (96 KB, loaded once) and streams the coefficient rows of 32 items (N =
 // 128) per tile of items, K-step by K-step (only the K-steps an item tile's
 // longest item needs); tensor memory holds two accumulator pairs, so the
-// epilogue of one item tile (8 warps: the seed sine/cosine per item and
-// site, the k-vector weights, Kahan-compensated FP32 force sums) overlaps
-// the MMAs of the next.
+// epilogue of one item tile (16 warps, four per tensor-memory lane quarter,
+// 8 items each: the seed sine/cosine per item and site, the k-vector
+// weights, Kahan-compensated FP32 force sums) overlaps the MMAs of the next.
 constexpr int FTC_NI = 32;                         // items per item tile (4 rows each: N = 128)
-constexpr int FTC_NSB = 4;                         // coefficient stages in flight
+constexpr int FTC_NSB = 4;                         // coefficient stages in flight per ring (two rings)
 constexpr int FTC_ATERM = 128 * 128 * 2;           // one term of a site tile's z tables: 32 KB
 constexpr int FTC_ABYTES = 3 * FTC_ATERM;          // 96 KB
 constexpr int FTC_BTERM = 128 * 16 * 2;            // one term of a coefficient stage: 4 KB
 constexpr int FTC_BBYTES = 3 * FTC_BTERM;          // 12 KB
-constexpr int FTC_SMEM = FTC_ABYTES + FTC_NSB * FTC_BBYTES + 128 * 3 * 4 * 2;
-constexpr int FTC_THREADS = 320;                   // 8 epilogue warps, bulk-copy warp, MMA warp
+constexpr int FTC_EG = 4;                          // epilogue warps per tensor-memory lane quarter
+constexpr int FTC_IPW = FTC_NI / FTC_EG;           // items of a tile per epilogue warp
+constexpr int FTC_EW = 4 * FTC_EG;                 // epilogue warps
+constexpr int FTC_SMEM = FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + FTC_EG * 128 * 3 * 4 + FTC_EW * FTC_IPW * 32;
+constexpr int FTC_THREADS = 32 * (FTC_EW + 4);     // epilogue warps, two bulk-copy warps, two MMA warps
+static_assert(FTC_IPW % 4 == 0, "an epilogue warp reads its items' columns 16 at a time");
 constexpr int FTC_SPLITS = 2;                      // item-tile ranges per site tile (grid.y)
 constexpr int FTC_ERR = 16;                        // error-word bit: a force-pass wait expired
 
@@ -436,7 +454,7 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
 {
    using namespace tc;
    extern __shared__ __align__(1024) unsigned char sm[];
-   __shared__ __align__(8) uint64_t full_a, full_b[FTC_NSB], empty_b[FTC_NSB], acc_full[2], acc_empty[2], done;
+   __shared__ __align__(8) uint64_t full_a, full_b[2][FTC_NSB], empty_b[2][FTC_NSB], acc_full[2], acc_empty[2], done[2];
    __shared__ unsigned int tmem_s;
    __shared__ int abort_s;
    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -445,23 +463,27 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
    const int per = (ntiles + gridDim.y - 1) / gridDim.y;
    const int nt0 = blockIdx.y * per, nt1 = min(ntiles, nt0 + per);
    unsigned char *A = sm, *Bs = sm + FTC_ABYTES;
-   float *red = reinterpret_cast<float *>(sm + FTC_ABYTES + FTC_NSB * FTC_BBYTES);   // [2][128][3] (sum, comp)
+   float *red = reinterpret_cast<float *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES);   // [FTC_EG][128][3]
+   // per epilogue warp: its items' (h, k, l0, count) and force coefficients
+   int4 *sitem = reinterpret_cast<int4 *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + FTC_EG * 128 * 3 * 4);
    if (tid == 0) {
       bar_init(&full_a, 1);
-      for (int s = 0; s < FTC_NSB; s++) {
-         bar_init(&full_b[s], 1);
-         bar_init(&empty_b[s], 1);
-      }
+      for (int p = 0; p < 2; p++)
+         for (int s = 0; s < FTC_NSB; s++) {
+            bar_init(&full_b[p][s], 1);
+            bar_init(&empty_b[p][s], 1);
+         }
       for (int b = 0; b < 2; b++) {
          bar_init(&acc_full[b], 1);
-         bar_init(&acc_empty[b], 8);
+         bar_init(&acc_empty[b], FTC_EW);
       }
-      bar_init(&done, 1);
+      bar_init(&done[0], 1);
+      bar_init(&done[1], 1);
       abort_s = 0;
       bar_init_fence();
    }
    __syncwarp();
-   if (w == 9) tmem_alloc(&tmem_s, 512);   // two buffers x (hh sums, smaller terms) x 128 columns
+   if (w == FTC_EW + 2) tmem_alloc(&tmem_s, 512);   // two buffers x (hh sums, smaller terms) x 128 columns
    fence_before_sync();
    __syncthreads();
    fence_after_sync();
@@ -469,18 +491,23 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
    // K-steps of an item tile: ceil(longest count / 16) in each half of K
    auto khalf = [&](int nt) { return (item[nt * FTC_NI].w + 15) >> 4; };
 
-   if (w == 8) {
+   if (w == FTC_EW || w == FTC_EW + 1) {
+      // ---- bulk copies: warp FTC_EW + p streams the coefficient rows of the
+      // item tiles j = p, p + 2, ... of this CTA's range into ring p
+      const int p = w - FTC_EW;
       if (lane == 0) {
-         bar_expect_tx(&full_a, FTC_ABYTES);
-         bulk_load(A, zsite + (size_t)tile * (FTC_ABYTES / 16), FTC_ABYTES, &full_a);
+         if (p == 0) {
+            bar_expect_tx(&full_a, FTC_ABYTES);
+            bulk_load(A, zsite + (size_t)tile * (FTC_ABYTES / 16), FTC_ABYTES, &full_a);
+         }
          int g = 0;
          bool stop = false;
-         for (int nt = nt0; nt < nt1 && !stop; nt++) {
+         for (int nt = nt0 + p; nt < nt1 && !stop; nt += 2) {
             const int kh = khalf(nt);
             for (int q = 0; q < 2 * kh; q++) {
                const int ks = q < kh ? q : 4 + q - kh;
                const int s = g % FTC_NSB;
-               if (g >= FTC_NSB && !bar_wait(&empty_b[s], (unsigned int)(g / FTC_NSB - 1) & 1u)) {
+               if (g >= FTC_NSB && !bar_wait(&empty_b[p][s], (unsigned int)(g / FTC_NSB - 1) & 1u)) {
                   tc_abort(&abort_s, err, FTC_ERR);
                   stop = true;
                   break;
@@ -489,27 +516,30 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
                   stop = true;
                   break;
                }
-               bar_expect_tx(&full_b[s], FTC_BBYTES);
-               bulk_load(Bs + s * FTC_BBYTES, utab + ((size_t)nt * 8 + ks) * (FTC_BBYTES / 16), FTC_BBYTES,
-                         &full_b[s]);
+               bar_expect_tx(&full_b[p][s], FTC_BBYTES);
+               bulk_load(Bs + (p * FTC_NSB + s) * FTC_BBYTES, utab + ((size_t)nt * 8 + ks) * (FTC_BBYTES / 16),
+                         FTC_BBYTES, &full_b[p][s]);
                g++;
             }
          }
-         bar_wait(&full_a, 0);
+         if (p == 0) bar_wait(&full_a, 0);
          for (int q = g > FTC_NSB ? g - FTC_NSB : 0; q < g; q++)
-            bar_wait(&full_b[q % FTC_NSB], (unsigned int)(q / FTC_NSB) & 1u);
+            bar_wait(&full_b[p][q % FTC_NSB], (unsigned int)(q / FTC_NSB) & 1u);
       }
-   } else if (w == 9) {
+   } else if (w == FTC_EW + 2 || w == FTC_EW + 3) {
+      // ---- MMA issue: warp FTC_EW + 2 + p takes the item tiles j = p, p + 2,
+      // ... into tensor-memory buffer p (one issuing thread sustains half the
+      // tensor pipe's rate at N = 128; two keep it busy)
+      const int p = w - FTC_EW - 2;
       if (lane == 0) {
          const unsigned int idn = idesc_bf16(128, 128, false);
          const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
-         const unsigned int a0 = saddr(A), b0 = saddr(Bs);
+         const unsigned int a0 = saddr(A), b0 = saddr(Bs + p * FTC_NSB * FTC_BBYTES);
          bool ok = bar_wait(&full_a, 0);
          if (!ok) tc_abort(&abort_s, err, FTC_ERR);
          int g = 0;
-         for (int nt = nt0, j = 0; nt < nt1 && ok; nt++, j++) {
-            const int b = j & 1;
-            if (j >= 2 && !bar_wait(&acc_empty[b], (unsigned int)((j >> 1) - 1) & 1u)) {
+         for (int nt = nt0 + p, jj = 0; nt < nt1 && ok; nt += 2, jj++) {
+            if (jj >= 1 && !bar_wait(&acc_empty[p], (unsigned int)(jj - 1) & 1u)) {
                tc_abort(&abort_s, err, FTC_ERR);
                break;
             }
@@ -518,7 +548,7 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
             for (int q = 0; q < 2 * kh; q++) {
                const int ks = q < kh ? q : 4 + q - kh;
                const int s = g % FTC_NSB;
-               if (!bar_wait(&full_b[s], (unsigned int)(g / FTC_NSB) & 1u)) {
+               if (!bar_wait(&full_b[p][s], (unsigned int)(g / FTC_NSB) & 1u)) {
                   tc_abort(&abort_s, err, FTC_ERR);
                   ok = false;
                   break;
@@ -526,29 +556,39 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
                fence_after_sync();
                const unsigned int bs = b0 + s * FTC_BBYTES;
 #pragma unroll
-               for (int p = 0; p < 6; p++) {
-                  const uint64_t ad = sdesc(a0 + ta[p] * FTC_ATERM + ks * 4096, 2048, 128);
-                  const uint64_t bd = sdesc(bs + tb[p] * FTC_BTERM, 2048, 128);
-                  mma_bf16(tmem + b * 256 + (p == 0 ? 0 : 128), ad, bd, idn, q > 0 || p > 1);
+               for (int t = 0; t < 6; t++) {
+                  const uint64_t ad = sdesc(a0 + ta[t] * FTC_ATERM + ks * 4096, 2048, 128);
+                  const uint64_t bd = sdesc(bs + tb[t] * FTC_BTERM, 2048, 128);
+                  mma_bf16(tmem + p * 256 + (t == 0 ? 0 : 128), ad, bd, idn, q > 0 || t > 1);
                }
-               mma_commit(&empty_b[s]);
+               mma_commit(&empty_b[p][s]);
                g++;
             }
-            if (ok) mma_commit(&acc_full[b]);
+            if (ok) mma_commit(&acc_full[p]);
          }
-         mma_commit(&done);
-         bar_wait(&done, 0);   // every MMA complete before the tensor memory is released
+         mma_commit(&done[p]);
+         bar_wait(&done[p], 0);   // every MMA complete before the tensor memory is released
       }
    } else {
-      // ---- epilogue: site row r, item half ih of each item tile
-      const int r = 32 * (w & 3) + lane, ih = w >> 2;
+      // ---- epilogue: site row r, items ig * FTC_IPW .. of each item tile
+      const int r = 32 * (w & 3) + lane, ig = w >> 2;
       const int i = tile * 128 + r;
       const int4 v = i < n ? ph[i] : make_int4(0, 0, 0, 0);
       const unsigned int ux = (unsigned int)v.x, uy = (unsigned int)v.y, uz = (unsigned int)v.z;
       const unsigned int trow = tmem + ((unsigned int)(32 * (w & 3)) << 16);
+      int4 *wi = sitem + w * 2 * FTC_IPW;   // [FTC_IPW] items, then [FTC_IPW] coefficients
+      const float4 *wc = reinterpret_cast<const float4 *>(wi + FTC_IPW);
       float Fx = 0.f, Fy = 0.f, Fz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
       for (int nt = nt0, j = 0; nt < nt1; nt++, j++) {
          const int b = j & 1;
+         const int it0 = nt * FTC_NI + ig * FTC_IPW;
+         // this tile's item records, fetched while its MMAs run
+         __syncwarp();
+         if (lane < FTC_IPW)
+            wi[lane] = item[it0 + lane];
+         else if (lane < 2 * FTC_IPW)
+            reinterpret_cast<float4 *>(wi)[lane] = coef[it0 + lane - FTC_IPW];
+         __syncwarp();
          const bool got = bar_wait(&acc_full[b], (unsigned int)(j >> 1) & 1u);
          if (!__all_sync(0xffffffffu, got && !tc_aborted(&abort_s))) {
             if (lane == 0) tc_abort(&abort_s, err, FTC_ERR);
@@ -557,18 +597,17 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
          fence_after_sync();
          float fx = 0.f, fy = 0.f, fz = 0.f;
 #pragma unroll 1
-         for (int grp = 0; grp < 4; grp++) {
+         for (int grp = 0; grp < FTC_IPW / 4; grp++) {
             float mv[16], cv[16];
-            const unsigned int col = (unsigned int)(b * 256 + 64 * ih + 16 * grp);
+            const unsigned int col = (unsigned int)(b * 256 + 4 * FTC_IPW * ig + 16 * grp);
             tmem_ld16(trow + col, mv);
             tmem_ld16(trow + col + 128, cv);
             tmem_wait2(mv, cv);
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-               const int it = nt * FTC_NI + 16 * ih + 4 * grp + e;
-               const int4 hd = item[it];
+               const int4 hd = wi[4 * grp + e];
                if (hd.w == 0) continue;   // (uniform: padding items)
-               const float4 cf = coef[it];
+               const float4 cf = wc[4 * grp + e];
                float sn, cs;
                sincos_poly((unsigned int)hd.x * ux + (unsigned int)hd.y * uy + (unsigned int)hd.z * uz, &sn, &cs);
                const float w1r = mv[4 * e] + cv[4 * e], w1i = mv[4 * e + 1] + cv[4 * e + 1];
@@ -586,7 +625,7 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
          kahan_add_tc(Fy, Cy, fy);
          kahan_add_tc(Fz, Cz, fz);
       }
-      float *rr = red + ((size_t)ih * 128 + r) * 3;
+      float *rr = red + ((size_t)ig * 128 + r) * 3;
       rr[0] = Fx - Cx;
       rr[1] = Fy - Cy;
       rr[2] = Fz - Cz;
@@ -597,14 +636,20 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
       const int r = 32 * w + lane, i = tile * 128 + r;
       if (i < n && !tc_aborted(&abort_s)) {
          const double q = chg[slots[i]];
-         const float *r0 = red + (size_t)r * 3, *r1 = red + (size_t)(128 + r) * 3;
+         double sx = 0.0, sy = 0.0, sz = 0.0;
+         for (int g = 0; g < FTC_EG; g++) {
+            const float *rg = red + ((size_t)g * 128 + r) * 3;
+            sx += (double)rg[0];
+            sy += (double)rg[1];
+            sz += (double)rg[2];
+         }
          double *dst = fpart + (size_t)blockIdx.y * 3 * n;
-         dst[i] = q * ((double)r0[0] + (double)r1[0]);
-         dst[n + i] = q * ((double)r0[1] + (double)r1[1]);
-         dst[2 * (size_t)n + i] = q * ((double)r0[2] + (double)r1[2]);
+         dst[i] = q * sx;
+         dst[n + i] = q * sy;
+         dst[2 * (size_t)n + i] = q * sz;
       }
    }
-   if (w == 9) {
+   if (w == FTC_EW + 2) {
       __syncwarp();
       fence_after_sync();
       tmem_dealloc(tmem, 512);

@@ -190,3 +190,96 @@ extern "C" mdgpu_status mdgpu_tc_probe(int device, const unsigned short *a0, con
    if (e != cudaSuccess) return MDGPU_E_CUDA;
    return herr ? MDGPU_E_CUDA : MDGPU_OK;
 }
+
+// ------------------------------------------------ tensor-core issue rate
+// One CTA per SM (the shared-memory request keeps it alone); its elected
+// thread issues reps MMAs of 128 x n x 16 (bf16, FP32 accumulation) from
+// zeroed operands, rotating over nacc accumulators of n columns, then waits
+// for their completion: the sustained MMA rate of one issuing thread at
+// this shape.
+namespace mdgpu {
+
+// issuers > 1: that many warps' lane 0 each issue reps / issuers MMAs into
+// their own accumulators (nacc per issuer); small selects 100 KB of shared
+// memory (two CTAs per SM, 256 tensor-memory columns each) instead of 200 KB.
+__global__ void __launch_bounds__(128, 1) k_tc_rate(int n, int reps, int nacc, int issuers, int ncols, int *__restrict__ err)
+{
+   using namespace tc;
+   extern __shared__ __align__(1024) unsigned char sm[];
+   __shared__ __align__(8) uint64_t bar[4];
+   __shared__ unsigned int taddr_s;
+   const int m = threadIdx.x, w = m >> 5;
+   for (int i = m; i < 32768 / 16; i += 128) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
+   fence_async_smem();
+   if (m == 0) {
+      for (int k = 0; k < 4; k++) bar_init(&bar[k], 1);
+      bar_init_fence();
+   }
+   __syncwarp();
+   if (w == 0) tmem_alloc(&taddr_s, (unsigned int)ncols);
+   fence_before_sync();
+   __syncthreads();
+   fence_after_sync();
+   const unsigned int tb = taddr_s;
+   if ((m & 31) == 0 && w < issuers) {
+      const unsigned int id = idesc_bf16(128, n, false);
+      const uint64_t ad = sdesc(saddr(sm), 2048u, 128u), bd = sdesc(saddr(sm + 8192), 16u * n, 128u);
+      const unsigned int base = tb + (unsigned int)(w * nacc * n);
+      for (int r = 0; r < reps / issuers; r++) mma_bf16(base + (unsigned int)((r % nacc) * n), ad, bd, id, r >= nacc);
+      mma_commit(&bar[w]);
+   }
+   __syncwarp();
+   bool ok = true;
+   for (int k = 0; k < issuers; k++) ok = ok && bar_wait(&bar[k], 0);
+   ok = __all_sync(0xffffffffu, ok);
+   if (!ok && (m & 31) == 0) atomicOr(err, 1);
+   fence_before_sync();
+   __syncthreads();
+   if (w == 0) tmem_dealloc(tb, (unsigned int)ncols);
+}
+
+}  // namespace mdgpu
+
+// n a multiple of 16 in 16..256, 1 <= issuers <= 4, issuers * nacc * n <=
+// 512 (256 with two CTAs per SM), reps >= issuers: bf16 MMA TFLOP/s over
+// all SMs (2 * 128 * n * 16 per MMA).
+extern "C" mdgpu_status mdgpu_tc_rate(int device, int n, int reps, int nacc, int issuers, int two_per_sm,
+                                      double *tflops)
+{
+   using namespace mdgpu;
+   const int ncols = two_per_sm ? 256 : 512;
+   if (!tflops || n < 16 || n > 256 || n % 16 || nacc < 1 || issuers < 1 || issuers > 4 ||
+       issuers * nacc * n > ncols || reps < issuers)
+      return MDGPU_E_ARG;
+   if (cudaSetDevice(device) != cudaSuccess) return MDGPU_E_CUDA;
+   int nsm = 0;
+   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+   int *perr = nullptr;
+   if (cudaMalloc(&perr, sizeof(int)) != cudaSuccess) return MDGPU_E_NOMEM;
+   cudaMemset(perr, 0, sizeof(int));
+   const int smem = two_per_sm ? 100 * 1024 : 200 * 1024;
+   cudaFuncSetAttribute(k_tc_rate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+   const int blocks = two_per_sm ? 2 * nsm : nsm;
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0);
+   cudaEventCreate(&e1);
+   float best = 1e30f;
+   for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0);
+      k_tc_rate<<<blocks, 128, smem>>>(n, reps, nacc, issuers, ncols, perr);
+      cudaEventRecord(e1);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0 && ms < best) best = ms;
+   }
+   int herr = 0;
+   cudaError_t e = cudaGetLastError();
+   if (e == cudaSuccess) e = cudaMemcpy(&herr, perr, sizeof(int), cudaMemcpyDeviceToHost);
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   cudaFree(perr);
+   if (e != cudaSuccess || herr) return MDGPU_E_CUDA;
+   *tflops = 2.0 * 128.0 * n * 16.0 * (double)(reps / issuers * issuers) * (double)blocks / (best * 1e-3) / 1e12;
+   return MDGPU_OK;
+}
