@@ -114,9 +114,9 @@ def tc_mma_flops(sysm, nq):
                 n -= 64
     counts = sorted(counts, reverse=True)
     counts += [0] * (-len(counts) % 128)
-    np16 = (nq + 15) // 16 * 16
-    sfac = sum((np16 // 16) * 24 * 2 * 128 * 16 * ((counts[t] + 15) // 16 * 16)
-               for t in range(0, len(counts), 128))
+    np32 = (nq + 31) // 32 * 32
+    # per 128-item tile and 16 sites: Ar and Ai times [Zr | Zi], six term products, N = 128
+    sfac = (len(counts) // 128) * (np32 // 16) * 12 * 2 * 128 * 128 * 16
     force = ((nq + 127) // 128) * sum(12 * ((counts[t] + 15) // 16) * 2 * 128 * 128 * 16
                                       for t in range(0, len(counts), 32))
     return {"sfac": float(sfac), "kforce": float(force)}

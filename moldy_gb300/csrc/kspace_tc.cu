@@ -11,27 +11,32 @@
 // is a product of an items x sites matrix (computed per stage on the CUDA
 // cores: one polynomial sine/cosine per item and site, amortised over up to
 // 64 k-vectors) and a sites x t matrix (the per-site z tables, built once
-// per evaluation).  Complex arithmetic as real MMAs: Re S = Ar Zr - Ai Zi,
-// Im S = Ar Zi + Ai Zr, the minus sign by the instruction's A negation.
+// per evaluation).  Complex arithmetic as real MMAs of N = 128: Ar and Ai
+// each times the whole z operand [Zr | Zi] (rows t, then 64 + t) into D1 =
+// (Ar Zr, Ar Zi) and D2 = (Ai Zr, Ai Zi), then Re S = Ar Zr - Ai Zi and
+// Im S = Ar Zi + Ai Zr in the read-back.  An MMA of 128 x N x 16 costs one
+// issuing thread the same time for any N up to 256 (measured:
+// mdgpu_tc_rate), so the products are kept wide and issued by two threads.
 //
-// Precision.  Charges are scaled by a power of two to |q| <= 1, and every
+// Precision.  Charges are scaled by a power of two to |q| < 1, and every
 // FP32 operand is split into three bf16 terms on fixed grids (tc.cuh): the
-// hi*hi products go to one tensor-memory accumulator, where their sums are
-// exact (multiples of 2^-14 below 2^10: a 512-site partial of terms of
-// magnitude <= 1), so the accumulator's round-toward-zero never acts on
-// them; hm, mh, hl, lh and mm go to a second accumulator, 2^-8 smaller.  The
-// terms left out and the splitting are within 2^-24 of each operand, as for
-// the FP32 path.  Each CTA sums 512 sites and writes one partial per k; the
-// partials are added in FP64 by the per-k reduction.
+// hi*hi products go to their own tensor-memory accumulators (D1, D2), where
+// their sums are exact (multiples of 2^-14 below 2^10: a 1024-site partial
+// of terms of magnitude < 1), so the accumulator's round-toward-zero never
+// acts on them; hm, mh, hl, lh and mm go to a second pair, 2^-8 smaller.
+// The terms left out and the splitting are within 2^-24 of each operand, as
+// for the FP32 path.  Each CTA sums 1024 sites and writes one partial per k;
+// the partials are added in compensated FP32 and FP64 by the per-k
+// reduction.
 //
-// CTA roles (320 threads): warps 0-7 build the A operand of each stage (one
-// item row and 8 of the stage's 16 sites per thread) and, at the end, read
-// the accumulators back (a warp reaches tensor-memory lanes 32 (w % 4) ..);
-// warp 8 copies the chunk's site records once and streams each stage's z
-// tables (bulk copies, four in flight); warp 9 owns the tensor memory and
-// issues the MMAs.  A operands are double-buffered, z tables quadruple-
-// buffered, on mbarriers; every wait is bounded and sets bit 3 of the error
-// word when it expires.
+// CTA roles (608 threads): warps 0-15 build the A operand of each 32-site
+// stage (one item row and 8 sites per thread) and, at the end, read the
+// accumulators back (a warp reaches tensor-memory lanes 32 (w % 4) ..);
+// warp 16 copies the chunk's site records once and streams each stage's z
+// tables (bulk copies, three in flight); warp 17 owns the tensor memory and
+// issues the Ar MMAs, warp 18 the Ai MMAs.  A operands are double-buffered,
+// z tables triple-buffered, on mbarriers; every wait is bounded and sets
+// bit 3 of the error word when it expires.
 #include <cmath>
 
 #include "mdgpu_internal.h"
@@ -40,26 +45,27 @@
 
 namespace mdgpu {
 
-constexpr int TC_KS = 16;                          // sites per stage (the K of one MMA)
+constexpr int TC_KS = 32;                          // sites per stage (two MMA K-steps of 16)
 constexpr int TC_NSA = 2;                          // A-operand buffers
-constexpr int TC_NSB = 4;                          // z-table buffers (bulk copies in flight)
-constexpr int TC_TERM = 128 * TC_KS * 2;           // one 128-row bf16 operand of a stage: 4096 bytes
+constexpr int TC_NSB = 3;                          // z-table buffers (bulk copies in flight)
+constexpr int TC_TERM = 128 * TC_KS * 2;           // one 128-row bf16 operand of a stage: 8 KB
 constexpr int TC_ABYTES = 6 * TC_TERM;             // Ar, Ai x (hi, mid, lo)
 constexpr int TC_BBYTES = 3 * TC_TERM;             // [Zr | Zi] x (hi, mid, lo)
-constexpr int TC_CHUNK = 512;                      // sites per CTA (one partial per k)
+constexpr int TC_CHUNK = 1024;                     // sites per CTA (one partial per k)
 constexpr int TC_PBYTES = TC_CHUNK * 16;           // the chunk's site records (u_x, u_y, u_z, q)
 constexpr int TC_AOFF = TC_PBYTES, TC_BOFF = TC_AOFF + TC_NSA * TC_ABYTES;
 constexpr int TC_SMEM = TC_BOFF + TC_NSB * TC_BBYTES;
 constexpr int TC_LBO = 16 * 128;                   // 8-column groups of a 128-row operand
 constexpr int TC_ERR = 8;                          // error-word bit: a stage wait expired
-constexpr int TC_THREADS = 320;                    // 8 operand/read-back warps, bulk-copy warp, MMA warp
+constexpr int TC_AW = 16;                          // operand / read-back warps
+constexpr int TC_THREADS = 32 * (TC_AW + 3);       // and a bulk-copy warp, two MMA warps
 
 static_assert(TC_AOFF % 1024 == 0 && TC_BOFF % 1024 == 0, "operand buffers stay aligned");
 static_assert(TC_CHUNK % TC_KS == 0, "chunks hold whole stages");
 static_assert(KT == 4 * KI && KT <= 64, "an item is four KI runs, Zr and Zi fit 128 rows");
 
-// z tables of the padded site list (np a multiple of 16) as the MMA's B
-// operand, per 16-site stage: [term][column group (8 sites)][row group][8
+// z tables of the padded site list (np a multiple of TC_KS) as the MMA's B
+// operand, per 32-site stage: [term][column group (8 sites)][row group][8
 // rows][8 sites] bf16, rows 0..63 cos(2 pi t u_z) and 64..127 its sine.
 // One thread per (8 sites, row); also zeroes the site records past n so
 // padding sites have no charge.
@@ -80,7 +86,8 @@ __global__ void k_ztab_tc(int n, int np, int4 *__restrict__ ph, uint4 *__restric
    unsigned int h[4], m[4], l[4];
 #pragma unroll
    for (int j = 0; j < 4; j++) tc::split3(v[2 * j], v[2 * j + 1], h[j], m[j], l[j]);
-   const size_t base = (size_t)(q8 >> 1) * (TC_BBYTES / 16) + (q8 & 1) * (TC_LBO / 16) + (row >> 3) * 8 + (row & 7);
+   constexpr int G = TC_KS / 8;   // column groups per stage
+   const size_t base = (size_t)(q8 / G) * (TC_BBYTES / 16) + (q8 % G) * (TC_LBO / 16) + (row >> 3) * 8 + (row & 7);
    ztab[base] = make_uint4(h[0], h[1], h[2], h[3]);
    ztab[base + TC_TERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
    ztab[base + 2 * TC_TERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
@@ -103,7 +110,7 @@ __device__ __forceinline__ bool tc_aborted(const int *flag)
 }
 
 // Grid: (item tiles of 128, site chunks of TC_CHUNK).  part[chunk][k].
-__global__ void __launch_bounds__(TC_THREADS, 2)
+__global__ void __launch_bounds__(TC_THREADS, 1)
 k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const int4 *__restrict__ ph,
           const uint4 *__restrict__ ztab, int np, int nk, float qscale, float qunscale, float2 *__restrict__ part,
           int *__restrict__ err)
@@ -123,24 +130,24 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
       bar_init(&full_p, 1);
       for (int s = 0; s < TC_NSB; s++) {
          bar_init(&full_b[s], 1);
-         bar_init(&empty_b[s], 1);
+         bar_init(&empty_b[s], 2);   // released by both MMA issuers
       }
       for (int s = 0; s < TC_NSA; s++) {
-         bar_init(&full_a[s], 8);
-         bar_init(&empty_a[s], 1);
+         bar_init(&full_a[s], TC_AW);
+         bar_init(&empty_a[s], 2);
       }
-      bar_init(&accf, 1);
+      bar_init(&accf, 2);
       abort_s = 0;
       bar_init_fence();
    }
    __syncwarp();
-   if (w == 9) tmem_alloc(&tmem_s, 256);   // [0,128): hh sums, [128,256): the smaller terms
+   if (w == TC_AW + 1) tmem_alloc(&tmem_s, 512);
    fence_before_sync();
    __syncthreads();
    fence_after_sync();
    const unsigned int tmem = tmem_s;
 
-   if (w == 8) {
+   if (w == TC_AW) {
       // ---- bulk copies: the chunk's site records once, each stage's z tables
       if (lane == 0) {
          bar_expect_tx(&full_p, (unsigned int)nst * TC_KS * 16);
@@ -163,11 +170,13 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
          for (int st = issued > TC_NSB ? issued - TC_NSB : 0; st < issued; st++)
             bar_wait(&full_b[st % TC_NSB], (unsigned int)(st / TC_NSB) & 1u);
       }
-   } else if (w == 9) {
-      // ---- MMA issue (the real and imaginary parts' MMAs alternate, so
-      // consecutive MMAs write different accumulators)
+   } else if (w == TC_AW + 1 || w == TC_AW + 2) {
+      // ---- MMA issue: warp TC_AW + 1 multiplies Ar, warp TC_AW + 2 Ai, by the
+      // whole z operand [Zr | Zi] (N = 128) into D1 = (Ar Zr, Ar Zi) and
+      // D2 = (Ai Zr, Ai Zi)
+      const int ic = w - TC_AW - 1;
       if (lane == 0) {
-         const unsigned int idn = idesc_bf16(128, ncols, false), idneg = idesc_bf16(128, ncols, true);
+         const unsigned int idn = idesc_bf16(128, 128, false);
          const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
          for (int st = 0; st < nst; st++) {
             const int sa = st % TC_NSA, sb = st % TC_NSB;
@@ -177,20 +186,15 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
                break;
             }
             fence_after_sync();
-            const unsigned int a = saddr(sm + TC_AOFF + sa * TC_ABYTES), b = saddr(sm + TC_BOFF + sb * TC_BBYTES);
+            const unsigned int a = saddr(sm + TC_AOFF + sa * TC_ABYTES) + 3 * ic * TC_TERM;
+            const unsigned int b = saddr(sm + TC_BOFF + sb * TC_BBYTES);
 #pragma unroll
-            for (int p = 0; p < 6; p++) {
-               const unsigned int d = tmem + (p == 0 ? 0u : 128u);
-               const bool acc = st > 0 || p > 1;
-               const uint64_t ar = sdesc(a + ta[p] * TC_TERM, TC_LBO, 128);
-               const uint64_t ai = sdesc(a + (3 + ta[p]) * TC_TERM, TC_LBO, 128);
-               const uint64_t zr = sdesc(b + tb[p] * TC_TERM, TC_LBO, 128);
-               const uint64_t zi = sdesc(b + tb[p] * TC_TERM + 8 * 128, TC_LBO, 128);
-               mma_bf16(d, ar, zr, idn, acc);          // Re += Ar Zr
-               mma_bf16(d + 64, ar, zi, idn, acc);     // Im += Ar Zi
-               mma_bf16(d, ai, zi, idneg, true);       // Re -= Ai Zi
-               mma_bf16(d + 64, ai, zr, idn, true);    // Im += Ai Zr
-            }
+            for (int ks = 0; ks < TC_KS / 16; ks++)
+#pragma unroll
+               for (int p = 0; p < 6; p++)
+                  mma_bf16(tmem + 128u * ic + (p == 0 ? 0u : 256u),
+                           sdesc(a + ta[p] * TC_TERM + ks * 2 * TC_LBO, TC_LBO, 128),
+                           sdesc(b + tb[p] * TC_TERM + ks * 2 * TC_LBO, TC_LBO, 128), idn, st > 0 || ks > 0 || p > 1);
             mma_commit(&empty_a[sa]);
             mma_commit(&empty_b[sb]);
          }
@@ -198,8 +202,8 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
       }
    } else {
       // ---- A operand: q_j seed_ij for this thread's item row and the
-      // stage's sites 8 g .. 8 g + 7
-      const int m = tid & 127, g = tid >> 7;
+      // stage's sites 8 qq .. 8 qq + 7 (one column group)
+      const int m = tid & 127, qq = tid >> 7;
       const int4 hd = item[tile * 128 + m];
       const unsigned int H = (unsigned int)hd.x, K = (unsigned int)hd.y, L = (unsigned int)hd.z;
       if (!bar_wait(&full_p, 0)) tc_abort(&abort_s, err);
@@ -211,64 +215,72 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
             break;
          }
          unsigned char *A = sm + TC_AOFF + s * TC_ABYTES;
-         const int4 *P = reinterpret_cast<const int4 *>(sm) + st * TC_KS;
-         {
-            unsigned int hr[4], mr[4], lr[4], hi[4], mi[4], li[4];
+         const int4 *P = reinterpret_cast<const int4 *>(sm) + st * TC_KS + 8 * qq;
+         unsigned int hr[4], mr[4], lr[4], hi[4], mi[4], li[4];
 #pragma unroll
-            for (int jp = 0; jp < 4; jp++) {
-               const int4 v0 = P[8 * g + 2 * jp], v1 = P[8 * g + 2 * jp + 1];
-               float s0v, c0v, s1v, c1v;
-               sincos_poly(H * (unsigned int)v0.x + K * (unsigned int)v0.y + L * (unsigned int)v0.z, &s0v, &c0v);
-               sincos_poly(H * (unsigned int)v1.x + K * (unsigned int)v1.y + L * (unsigned int)v1.z, &s1v, &c1v);
-               const float q0 = __int_as_float(v0.w) * qscale, q1 = __int_as_float(v1.w) * qscale;
-               split3(c0v * q0, c1v * q1, hr[jp], mr[jp], lr[jp]);
-               split3(s0v * q0, s1v * q1, hi[jp], mi[jp], li[jp]);
-            }
-            unsigned char *row = A + g * TC_LBO + (m >> 3) * 128 + (m & 7) * 16;
-            *reinterpret_cast<uint4 *>(row) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
-            *reinterpret_cast<uint4 *>(row + TC_TERM) = make_uint4(mr[0], mr[1], mr[2], mr[3]);
-            *reinterpret_cast<uint4 *>(row + 2 * TC_TERM) = make_uint4(lr[0], lr[1], lr[2], lr[3]);
-            *reinterpret_cast<uint4 *>(row + 3 * TC_TERM) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<uint4 *>(row + 4 * TC_TERM) = make_uint4(mi[0], mi[1], mi[2], mi[3]);
-            *reinterpret_cast<uint4 *>(row + 5 * TC_TERM) = make_uint4(li[0], li[1], li[2], li[3]);
+         for (int jp = 0; jp < 4; jp++) {
+            const int4 v0 = P[2 * jp], v1 = P[2 * jp + 1];
+            float s0v, c0v, s1v, c1v;
+            sincos_poly(H * (unsigned int)v0.x + K * (unsigned int)v0.y + L * (unsigned int)v0.z, &s0v, &c0v);
+            sincos_poly(H * (unsigned int)v1.x + K * (unsigned int)v1.y + L * (unsigned int)v1.z, &s1v, &c1v);
+            const float q0 = __int_as_float(v0.w) * qscale, q1 = __int_as_float(v1.w) * qscale;
+            split3(c0v * q0, c1v * q1, hr[jp], mr[jp], lr[jp]);
+            split3(s0v * q0, s1v * q1, hi[jp], mi[jp], li[jp]);
          }
+         unsigned char *row = A + qq * TC_LBO + (m >> 3) * 128 + (m & 7) * 16;
+         *reinterpret_cast<uint4 *>(row) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
+         *reinterpret_cast<uint4 *>(row + TC_TERM) = make_uint4(mr[0], mr[1], mr[2], mr[3]);
+         *reinterpret_cast<uint4 *>(row + 2 * TC_TERM) = make_uint4(lr[0], lr[1], lr[2], lr[3]);
+         *reinterpret_cast<uint4 *>(row + 3 * TC_TERM) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+         *reinterpret_cast<uint4 *>(row + 4 * TC_TERM) = make_uint4(mi[0], mi[1], mi[2], mi[3]);
+         *reinterpret_cast<uint4 *>(row + 5 * TC_TERM) = make_uint4(li[0], li[1], li[2], li[3]);
          fence_async_smem();
          __syncwarp();
          if (lane == 0) bar_arrive(&full_a[s]);
       }
-      // ---- read back: row m of the tile, columns t (Re) and 64 + t (Im),
-      // t in [32 g, 32 g + 32)
+      // ---- read back: item row m (lane quarter w % 4), t in [16 qq, 16 qq + 16):
+      // Re = Ar Zr - Ai Zi, Im = Ar Zi + Ai Zr, each the hh sums plus the rest
       const bool done = bar_wait(&accf, 0);
       const bool ok = __all_sync(0xffffffffu, done && !tc_aborted(&abort_s));
       if (!done && lane == 0) tc_abort(&abort_s, err);
       fence_after_sync();
-      if (ok) {
+      const int t0 = 16 * qq;
+      if (ok && t0 < ncols) {
          const int4 k0 = item_k0[tile * 128 + m];
-         const unsigned int trow = tmem + ((unsigned int)(32 * (w & 3)) << 16);
-         float2 *dst = part + (size_t)chunk * nk;
-         for (int t0 = 32 * g; t0 < min(ncols, 32 * g + 32); t0 += 16) {
-            float re[16], im[16], re2[16], im2[16];
-            tmem_ld16(trow + t0, re);
-            tmem_ld16(trow + 64 + t0, im);
-            tmem_ld16(trow + 128 + t0, re2);
-            tmem_ld16(trow + 192 + t0, im2);
-            tmem_wait2(re, im);
-            tmem_wait2(re2, im2);
-            const int kr = t0 == 0 ? k0.x : t0 == 16 ? k0.y : t0 == 32 ? k0.z : k0.w;
-            if (kr >= 0)
+         const unsigned int trow = tmem + ((unsigned int)(32 * (w & 3)) << 16) + (unsigned int)t0;
+         const int kr = qq == 0 ? k0.x : qq == 1 ? k0.y : qq == 2 ? k0.z : k0.w;
+         // column pairs (hh sums, the rest): Ar Zr at t, Ar Zi at 64 + t,
+         // Ai Zr at 128 + t, Ai Zi at 192 + t; the rest 256 further on
+         auto pair_sum = [&](unsigned int col, float (&out)[16]) {
+            float u[16], v[16];
+            tmem_ld16(trow + col, u);
+            tmem_ld16(trow + col + 256, v);
+            tmem_wait2(u, v);
 #pragma unroll
-               for (int j = 0; j < 16; j++)
-                  if (t0 + j < hd.w)
-                     dst[kr + j] = make_float2((re[j] + re2[j]) * qunscale, (im[j] + im2[j]) * qunscale);
-         }
+            for (int j = 0; j < 16; j++) out[j] = u[j] + v[j];
+         };
+         float re[16], im[16], x[16];
+         pair_sum(0, re);
+         pair_sum(192, x);
+#pragma unroll
+         for (int j = 0; j < 16; j++) re[j] -= x[j];
+         pair_sum(64, im);
+         pair_sum(128, x);
+#pragma unroll
+         for (int j = 0; j < 16; j++) im[j] += x[j];
+         float2 *dst = part + (size_t)chunk * nk;
+         if (kr >= 0)
+#pragma unroll
+            for (int j = 0; j < 16; j++)
+               if (t0 + j < hd.w) dst[kr + j] = make_float2(re[j] * qunscale, im[j] * qunscale);
       }
    }
    fence_before_sync();
    __syncthreads();
-   if (w == 9) {
+   if (w == TC_AW + 1) {
       __syncwarp();
       fence_after_sync();
-      tmem_dealloc(tmem, 256);
+      tmem_dealloc(tmem, 512);
    }
 }
 
