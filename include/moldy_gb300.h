@@ -369,11 +369,12 @@ void mdgpu_dump_close(mdgpu_dumpfile *df);
  * bound is the FMA pipe.  No counterpart in the reference. */
 mdgpu_status mdgpu_fma_peak(int device, int fp64, double *tflops);
 
-/* Tensor-core operand probe: one 128 x n x 16 bf16 MMA pair, D = A0 B0^T
- * then (unless flags & 4) D += A1 B1^T (A1 negated if flags & 2), FP32
- * accumulation, in the operand layout the reciprocal-space tensor-core
- * kernels use (flags & 1 exchanges the descriptor's two offset fields).
- * a0, a1: 128 x 16 bf16 bit patterns, row-major; b0, b1: n x 16; d: 128 x n.
+/* Tensor-core operand probe: one 128 x n x 16 MMA pair (bf16, or fp16 if
+ * flags & 8), D = A0 B0^T then (unless flags & 4) D += A1 B1^T (A1 negated
+ * if flags & 2), FP32 accumulation, in the operand layout the
+ * reciprocal-space tensor-core kernels use (flags & 1 exchanges the
+ * descriptor's two offset fields).  a0, a1: 128 x 16 16-bit patterns,
+ * row-major; b0, b1: n x 16; d: 128 x n.
  * n a multiple of 16 in 16..128.  No counterpart in the reference. */
 mdgpu_status mdgpu_tc_probe(int device, const unsigned short *a0, const unsigned short *b0,
                             const unsigned short *a1, const unsigned short *b1, int n, int flags, float *d);

@@ -192,7 +192,7 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
             for (int ks = 0; ks < TC_KS / 16; ks++)
 #pragma unroll
                for (int p = 0; p < 6; p++)
-                  mma_bf16(tmem + 128u * ic + (p == 0 ? 0u : 256u),
+                  mma_f16(tmem + 128u * ic + (p == 0 ? 0u : 256u),
                            sdesc(a + ta[p] * TC_TERM + ks * 2 * TC_LBO, TC_LBO, 128),
                            sdesc(b + tb[p] * TC_TERM + ks * 2 * TC_LBO, TC_LBO, 128), idn, st > 0 || ks > 0 || p > 1);
             mma_commit(&empty_a[sa]);
@@ -323,8 +323,12 @@ int ks_tc_chunks(int nsites)
 // the 64 sines) and four coefficient rows per item,
 //     W1re = [A | B],  W1im = [-B | A],  W2re = [tA | tB],  W2im = [-tB | tA],
 // each row scaled by a power of two to |v| <= 1 (the scale is folded into
-// the item's force coefficients).  A CTA holds one 128-site tile's z tables
-// (96 KB, loaded once) and streams the coefficient rows of 32 items (N =
+// the item's force coefficients).  Operands are three bf16 terms on fixed
+// grids as in the structure factor, six term products (hh into one
+// accumulator, the rest into another): the k-space force on a site is a
+// near-cancelling sum over k, and two fp16 terms (2^-22 per operand, three
+// products) raised the force error of the fixtures to 1.1e-5.  A CTA holds
+// one 128-site tile's z tables (96 KB, loaded once) and streams the coefficient rows of 32 items (N =
 // 128) per tile of items, K-step by K-step (only the K-steps an item tile's
 // longest item needs); tensor memory holds two accumulator pairs, so the
 // epilogue of one item tile (16 warps, four per tensor-memory lane quarter,
@@ -571,7 +575,7 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
                for (int t = 0; t < 6; t++) {
                   const uint64_t ad = sdesc(a0 + ta[t] * FTC_ATERM + ks * 4096, 2048, 128);
                   const uint64_t bd = sdesc(bs + tb[t] * FTC_BTERM, 2048, 128);
-                  mma_bf16(tmem + p * 256 + (t == 0 ? 0 : 128), ad, bd, idn, q > 0 || t > 1);
+                  mma_f16(tmem + p * 256 + (t == 0 ? 0 : 128), ad, bd, idn, q > 0 || t > 1);
                }
                mma_commit(&empty_b[p][s]);
                g++;

@@ -87,8 +87,9 @@ extern "C" mdgpu_status mdgpu_fma_peak(int device, int fp64, double *tflops)
 
 // ------------------------------------------------------- tensor-core probe
 // One CTA computes D = A0 B0^T and then (unless flags & 4) D += A1 B1^T,
-// negating A1 if flags & 2, with M = 128, N = n, K = 16 (bf16 operands, FP32
-// accumulation in tensor memory), operands in the K-major unswizzled layout
+// negating A1 if flags & 2, with M = 128, N = n, K = 16 (bf16 operands, or
+// fp16 if flags & 8; FP32 accumulation in tensor memory), operands in the
+// K-major unswizzled layout
 // of tc.cuh.  flags & 1 exchanges the two offset fields of the operand
 // descriptors (the operand regions are sized so that both readings stay
 // inside them).  It checks the operand layout, the negation flag and the
@@ -137,8 +138,12 @@ k_tc_probe(const uint4 *__restrict__ a0, const uint4 *__restrict__ b0, const uin
       auto desc = [&](const unsigned char *p, unsigned int lbo) {
          return swap ? sdesc(saddr(p), 128u, lbo) : sdesc(saddr(p), lbo, 128u);
       };
-      mma_bf16(tb, desc(A0, 2048u), desc(B0, 16u * n), idesc_bf16(128, n, false), false);
-      if (!(flags & 4)) mma_bf16(tb, desc(A1, 2048u), desc(B1, 16u * n), idesc_bf16(128, n, (flags & 2) != 0), true);
+      const bool h = (flags & 8) != 0;   // fp16 operands instead of bf16
+      mma_f16(tb, desc(A0, 2048u), desc(B0, 16u * n), h ? idesc_f16(128, n, false) : idesc_bf16(128, n, false),
+              false);
+      if (!(flags & 4))
+         mma_f16(tb, desc(A1, 2048u), desc(B1, 16u * n),
+                 h ? idesc_f16(128, n, (flags & 2) != 0) : idesc_bf16(128, n, (flags & 2) != 0), true);
       mma_commit(&bar);
    }
    __syncwarp();
@@ -225,7 +230,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_rate(int n, int reps, int nacc, i
       const unsigned int id = idesc_bf16(128, n, false);
       const uint64_t ad = sdesc(saddr(sm), 2048u, 128u), bd = sdesc(saddr(sm + 8192), 16u * n, 128u);
       const unsigned int base = tb + (unsigned int)(w * nacc * n);
-      for (int r = 0; r < reps / issuers; r++) mma_bf16(base + (unsigned int)((r % nacc) * n), ad, bd, id, r >= nacc);
+      for (int r = 0; r < reps / issuers; r++) mma_f16(base + (unsigned int)((r % nacc) * n), ad, bd, id, r >= nacc);
       mma_commit(&bar[w]);
    }
    __syncwarp();

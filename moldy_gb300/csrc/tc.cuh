@@ -115,8 +115,15 @@ __host__ __device__ constexpr unsigned int idesc_bf16(int M, int N, bool negA)
           ((unsigned int)(M >> 4) << 24);
 }
 
+// The same with fp16 A and B.
+__host__ __device__ constexpr unsigned int idesc_f16(int M, int N, bool negA)
+{
+   return (1u << 4) | ((negA ? 1u : 0u) << 13) | ((unsigned int)(N >> 3) << 17) | ((unsigned int)(M >> 4) << 24);
+}
+
 // D (tensor memory) = A B^T (+ D if acc), issued by one thread.
-__device__ __forceinline__ void mma_bf16(unsigned int d, uint64_t a, uint64_t b, unsigned int idesc, bool acc)
+// (kind::f16 takes bf16 or fp16 operands, the same type for A and B)
+__device__ __forceinline__ void mma_f16(unsigned int d, uint64_t a, uint64_t b, unsigned int idesc, bool acc)
 {
    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"

@@ -1,10 +1,11 @@
-"""Tensor-core (tcgen05) path of the mixed-form structure factor.
+"""Tensor-core (tcgen05) path of the mixed form's reciprocal space.
 
-The operand probe runs one 128 x n x 16 bf16 MMA pair in the operand layout
-the structure-factor kernel uses and compares it with the product computed
-on the host (small integers times powers of two: every sum is exact in FP32),
-with and without the A-negation flag.  The structure factor on the tensor
-cores is compared with the CUDA-core pass on the same configuration."""
+The operand probe runs one 128 x n x 16 MMA pair (bf16, the structure
+factor's operands, and fp16, the force pass's) in the operand layout the
+kernels use and compares it with the product computed on the host (small
+integers times powers of two: every sum is exact in FP32), with and without
+the A-negation flag.  The tensor-core passes (structure factor and forces)
+are compared with the CUDA-core passes on the same configurations."""
 import ctypes as C
 import os
 
@@ -44,6 +45,17 @@ def test_probe_layout_and_negation(n, neg):
     d = probe(a0, b0, a1, b1, 2 if neg else 0)
     A0, A1, B0, B1 = (bf16_value(v).astype(np.float64) for v in (a0, a1, b0, b1))
     ref = A0 @ B0.T + (-1.0 if neg else 1.0) * (A1 @ B1.T)
+    np.testing.assert_array_equal(d, ref.astype(np.float32))
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_probe_fp16_operands(n):
+    """The force pass's operand type: fp16 bit patterns, flags & 8."""
+    rng = np.random.default_rng(7 + n)
+    mk = lambda r: (rng.integers(-64, 65, size=(r, 16)).astype(np.float16) * np.float16(0.0625))
+    a0, a1, b0, b1 = mk(128), mk(128), mk(n), mk(n)
+    d = probe(*(v.view(np.uint16) for v in (a0, b0, a1, b1)), 8)
+    ref = a0.astype(np.float64) @ b0.astype(np.float64).T + a1.astype(np.float64) @ b1.astype(np.float64).T
     np.testing.assert_array_equal(d, ref.astype(np.float32))
 
 
