@@ -48,7 +48,9 @@ __device__ __forceinline__ unsigned long long to_fixed64(double s)
 // chunks are then compact regions of the cell, close to neutral, so their
 // FP32 partial sums stay small even where the full sum cancels (an ionic
 // crystal listed species by species would otherwise give chunks of a
-// single charge sign).
+// single charge sign).  mixed: 0 the FP64 records, 1 the FP32 records and
+// z tables, 2 the FP32 phases only (the tensor-core passes build their own
+// tables).
 __global__ void k_prep(int N, int ns, const int *__restrict__ sorted, const double *__restrict__ site,
                        const double *__restrict__ chg, double hi0, double hi1, double hi2,
                        double hi3, double hi4, double hi5, double hi6, double hi7, double hi8,
@@ -65,14 +67,15 @@ __global__ void k_prep(int N, int ns, const int *__restrict__ sorted, const doub
    double s2 = hi6 * x + hi7 * y + hi8 * z;
    unsigned long long ux = to_fixed64(s0), uy = to_fixed64(s1), uz = to_fixed64(s2);
    double q = chg[si];
-   double sz, cz;
-   sincospi(2.0 * ((double)(long long)uz * 5.421010862427522e-20), &sz, &cz);   // 2^-64
    if (mixed) {
       // round the 64-bit phases to 32 bits
       unsigned int ux32 = (unsigned int)((ux + 0x80000000ull) >> 32);
       unsigned int uy32 = (unsigned int)((uy + 0x80000000ull) >> 32);
       unsigned int uz32 = (unsigned int)((uz + 0x80000000ull) >> 32);
       ph32[i] = make_int4((int)ux32, (int)uy32, (int)uz32, __float_as_int((float)q));
+      if (mixed == 2) return;   // the tensor-core passes build their own z tables
+      double sz, cz;
+      sincospi(2.0 * ((double)(long long)uz * 5.421010862427522e-20), &sz, &cz);   // 2^-64
       z32[i] = make_float2((float)cz, (float)sz);
       // exp(2 pi i t s_z), t = 0..KI-1, each from its exact integer phase;
       // the site's KI cosines, then its KI sines
@@ -84,6 +87,8 @@ __global__ void k_prep(int N, int ns, const int *__restrict__ sorted, const doub
          zf[KI + t] = st;
       }
    } else {
+      double sz, cz;
+      sincospi(2.0 * ((double)(long long)uz * 5.421010862427522e-20), &sz, &cz);   // 2^-64
       ph64a[i] = make_ulonglong2(ux, uy);
       ph64b[i] = make_ulonglong2(uz, (unsigned long long)__double_as_longlong(q));
       z64[i] = make_double2(cz, sz);
@@ -1008,12 +1013,13 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       c->launches += 3;
       slots = d.kslots.p;
    }
-   k_prep<<<(Nk + 255) / 256, 256, 0, st>>>(Nk, N, slots, d_site, c->rd.chg.p, hinv[0], hinv[1], hinv[2],
-                                            hinv[3], hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], mixed ? 1 : 0,
-                                            d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p, d.ph64b.p, d.z64.p);
-   CK(cudaGetLastError());
    // mixed form over the charged sites: both passes on the tensor cores
    const bool tc = mixed && compact && c->tc_sfac;
+   k_prep<<<(Nk + 255) / 256, 256, 0, st>>>(Nk, N, slots, d_site, c->rd.chg.p, hinv[0], hinv[1], hinv[2],
+                                            hinv[3], hinv[4], hinv[5], hinv[6], hinv[7], hinv[8],
+                                            tc ? 2 : mixed ? 1 : 0, d.ph32.p, d.z32.p, d.zp32.p, d.ph64a.p,
+                                            d.ph64b.p, d.z64.p);
+   CK(cudaGetLastError());
    if (tc) {
       CK(d.ztab.ensure(ks_tc_ztab_len(Nk)));
       CK(d.zsite.ensure(ks_tc_zsite_len(Nk)));

@@ -220,12 +220,12 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
 #pragma unroll
          for (int jp = 0; jp < 4; jp++) {
             const int4 v0 = P[2 * jp], v1 = P[2 * jp + 1];
-            float s0v, c0v, s1v, c1v;
-            sincos_poly(H * (unsigned int)v0.x + K * (unsigned int)v0.y + L * (unsigned int)v0.z, &s0v, &c0v);
-            sincos_poly(H * (unsigned int)v1.x + K * (unsigned int)v1.y + L * (unsigned int)v1.z, &s1v, &c1v);
-            const float q0 = __int_as_float(v0.w) * qscale, q1 = __int_as_float(v1.w) * qscale;
-            split3(c0v * q0, c1v * q1, hr[jp], mr[jp], lr[jp]);
-            split3(s0v * q0, s1v * q1, hi[jp], mi[jp], li[jp]);
+            f2x sv, cv;   // the two sites as the lanes of paired FP32 instructions
+            sincos_poly2(H * (unsigned int)v0.x + K * (unsigned int)v0.y + L * (unsigned int)v0.z,
+                         H * (unsigned int)v1.x + K * (unsigned int)v1.y + L * (unsigned int)v1.z, sv, cv);
+            const f2x q = pk2(__int_as_float(v0.w) * qscale, __int_as_float(v1.w) * qscale);
+            split3(mul2(cv, q), hr[jp], mr[jp], lr[jp]);
+            split3(mul2(sv, q), hi[jp], mi[jp], li[jp]);
          }
          unsigned char *row = A + qq * TC_LBO + (m >> 3) * 128 + (m & 7) * 16;
          *reinterpret_cast<uint4 *>(row) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
@@ -449,7 +449,7 @@ k_utab_tc(int nitems, const int4 *__restrict__ item, const int4 *__restrict__ it
    }
    if (lane == 0) {
       const float2 k = kxy[i];
-      coef[i] = make_float4(k.x * s1, k.y * s1, kz0 * s1, dkz * s2);
+      coef[i] = hd.w > 0 ? make_float4(k.x * s1, k.y * s1, kz0 * s1, dkz * s2) : make_float4(0.f, 0.f, 0.f, 0.f);
    }
 }
 
@@ -622,7 +622,9 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                const int4 hd = wi[4 * grp + e];
-               if (hd.w == 0) continue;   // (uniform: padding items)
+               // padding items come last; a tile of padding only issues no
+               // MMAs, so its buffer holds an earlier tile's sums (uniform)
+               if (hd.w == 0) continue;
                const float4 cf = wc[4 * grp + e];
                float sn, cs;
                sincos_poly((unsigned int)hd.x * ux + (unsigned int)hd.y * uy + (unsigned int)hd.z * uz, &sn, &cs);

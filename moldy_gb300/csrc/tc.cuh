@@ -204,9 +204,9 @@ __device__ __forceinline__ f2x round_grid(f2x v, float c)
 {
    return add2(add2(v, pk2(c, c)), pk2(-c, -c));
 }
-__device__ __forceinline__ void split3(float a, float b, unsigned int &h, unsigned int &m, unsigned int &l)
+__device__ __forceinline__ void split3(f2x v, unsigned int &h, unsigned int &m, unsigned int &l)
 {
-   const f2x v = pk2(a, b), m1 = pk2(-1.f, -1.f);
+   const f2x m1 = pk2(-1.f, -1.f);
    const f2x vh = round_grid(v, 98304.f);            // 1.5 2^16: grid 2^-7
    const f2x r = fma2(vh, m1, v);                     // v - hi, exact
    const f2x vm = round_grid(r, 384.f);               // 1.5 2^8: grid 2^-15
@@ -215,6 +215,10 @@ __device__ __forceinline__ void split3(float a, float b, unsigned int &h, unsign
    h = pack_bf16(vh);
    m = pack_bf16(vm);
    l = pack_bf16(vl);
+}
+__device__ __forceinline__ void split3(float a, float b, unsigned int &h, unsigned int &m, unsigned int &l)
+{
+   split3(pk2(a, b), h, m, l);
 }
 
 }  // namespace tc
