@@ -90,12 +90,10 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16": 1900.0, "bf16_sustained": 1700.0, "source": "fallback"}
 
 
-def tc_mma_flops(sysm, nq):
-    """Tensor-core work the two reciprocal-space kernels issue per launch
-    (bf16 MMA flops, the split-operand term products and the padding of
-    items to 16-column multiples included), from the k-list columns exactly
-    as the library builds them: runs of up to 64 l values per (h,k) column,
-    largest count first, 128 per structure-factor tile, 32 per force tile."""
+def tc_item_counts(sysm):
+    """Counts of the tensor-core items (runs of up to 64 l values per (h,k)
+    column of the k-list), largest first, padded with empty items to a
+    multiple of 128 -- as the library builds them."""
     import math
     h = np.asarray(sysm.h, np.float64).reshape(9)
     kc = sysm.control.k_cutoff
@@ -113,7 +111,16 @@ def tc_mma_flops(sysm, nq):
                 counts.append(min(n, 64))
                 n -= 64
     counts = sorted(counts, reverse=True)
-    counts += [0] * (-len(counts) % 128)
+    return counts + [0] * (-len(counts) % 128)
+
+
+def tc_mma_flops(sysm, nq):
+    """Tensor-core work the two reciprocal-space kernels issue per launch
+    (bf16 MMA flops, the split-operand term products and the padding of
+    items to 16-column multiples included), from the k-list columns exactly
+    as the library builds them (tc_item_counts): 128 items per
+    structure-factor tile, 32 per force tile."""
+    counts = tc_item_counts(sysm)
     np32 = (nq + 31) // 32 * 32
     # per 128-item tile and 16 sites: Ar and Ai times [Zr | Zi], six term products, N = 128
     sfac = (len(counts) // 128) * (np32 // 16) * 12 * 2 * 128 * 128 * 16
