@@ -358,7 +358,7 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh)
    return s;   // valid in thread 0
 }
 
-constexpr int PAIR_WARPS = 8;   // warps per block
+constexpr int PAIR_WARPS = 4;   // warps per block (8k registers: a block fits beside a tensor-core CTA)
 
 // Per-warp shared rows of the stencil walk (32 WALK_E entries), and the
 // stencil's cell-offset vectors (global, read by entry).
