@@ -1,6 +1,7 @@
-// Structure factor of the mixed form on the tensor cores (tcgen05): the
-// S(k) pass of ewald() (src/ewald.c:124-141, the sums of q cos(k.r) and
-// q sin(k.r) over sites, 523-533) as a complex matrix product.
+// Reciprocal space of the mixed form on the tensor cores (tcgen05).  This
+// part: the S(k) pass of ewald() (src/ewald.c:124-141, the sums of q cos(k.r)
+// and q sin(k.r) over sites, 523-533) as a complex matrix product; the force
+// pass (src/ewald.c:557-566) follows further down.
 //
 // A tensor-core item is a run of up to KT = 64 consecutive l values of one
 // (h,k) column.  For item i, site j and offset t,
