@@ -38,6 +38,7 @@
 // issues the Ar MMAs, warp 18 the Ai MMAs.  A operands are double-buffered,
 // z tables triple-buffered, on mbarriers; every wait is bounded and sets
 // bit 3 of the error word when it expires.
+#include <atomic>
 #include <cmath>
 
 #include "mdgpu_internal.h"
@@ -717,14 +718,17 @@ size_t ks_tc_utab_len(int nitems_padded)
 
 // Shared-memory sizes of the tensor-core kernels, set once per device
 // outside any stream capture (from ks_prepare).
+// (contexts may be created from several host threads: the per-device flags
+// are atomic, and setting the attribute twice is harmless)
 cudaError_t ks_tc_init(int device)
 {
-   static unsigned long long done = 0;
-   if (device >= 0 && device < 64 && (done >> device) & 1ull) return cudaSuccess;
+   static std::atomic<unsigned long long> done{0};
+   const unsigned long long bit = device >= 0 && device < 64 ? 1ull << device : 0ull;
+   if (bit && (done.load() & bit)) return cudaSuccess;
    cudaError_t e = cudaFuncSetAttribute(k_sfac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
    if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_force_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, FTC_SMEM);
-   if (e == cudaSuccess && device >= 0 && device < 64) done |= 1ull << device;
+   if (e == cudaSuccess && bit) done.fetch_or(bit);
    return e;
 }
 
