@@ -389,6 +389,16 @@ mdgpu_status mdgpu_tc_rate(int device, int n, int reps, int nacc, int issuers, i
  * charge 1, neighbour charge chgsq, Ewald alpha as given. */
 double mdgpu_poteval(const double *potpar, double r, int ptype, double chgsq, double alpha);
 
+/* The tensor-core work items of the k-list for cell h (row-major) and the
+ * control values (host only, no device needed): runs of up to 64 l values of
+ * one (h, k) column, largest count first, padded with empty runs to a
+ * multiple of 128.  items[4 i ..] = (h, k, l0, count); k0[4 i + r] = index of
+ * the run's r-th 16 k-vectors in the k-list order the passes use (-1 past
+ * its end).  *nitems and *nk (k-vectors) are set; MDGPU_E_CAPACITY if nitems
+ * exceeds cap.  No counterpart in the reference. */
+mdgpu_status mdgpu_tc_items(const double *h, const mdgpu_control *ctl, int *items, int *k0, int cap,
+                            int *nitems, int *nk);
+
 #ifdef __cplusplus
 }
 #endif

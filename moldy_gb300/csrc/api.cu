@@ -716,6 +716,34 @@ double mdgpu_poteval(const double *potpar, double r, int ptype, double chgsq, do
    return host_poteval(potpar, r, ptype, chgsq, alpha);
 }
 
+mdgpu_status mdgpu_tc_items(const double *h, const mdgpu_control *ctl, int *items, int *k0, int cap,
+                            int *nitems, int *nk)
+{
+   if (!h || !ctl || !nitems || !nk || cap < 0) return MDGPU_E_ARG;
+   KList kl;
+   mdgpu_status s = build_klist(h, *ctl, kl);
+   if (s) return s;
+   const int n = (int)kl.tc_item.size();
+   *nitems = n;
+   *nk = kl.nk;
+   if (n > cap) return MDGPU_E_CAPACITY;
+   for (int i = 0; i < n; i++) {
+      if (items) {
+         items[4 * i] = kl.tc_item[i].x;
+         items[4 * i + 1] = kl.tc_item[i].y;
+         items[4 * i + 2] = kl.tc_item[i].z;
+         items[4 * i + 3] = kl.tc_item[i].w;
+      }
+      if (k0) {
+         k0[4 * i] = kl.tc_k0[i].x;
+         k0[4 * i + 1] = kl.tc_k0[i].y;
+         k0[4 * i + 2] = kl.tc_k0[i].z;
+         k0[4 * i + 3] = kl.tc_k0[i].w;
+      }
+   }
+   return MDGPU_OK;
+}
+
 // ------------------------------------------------ reference signatures
 // The caller's globals and log functions (src/main.c:83-84,
 // src/output.c:131-190), bound if the executable defines them.
