@@ -44,8 +44,7 @@ def _compile(src: str) -> str:
     deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
-    lang = [] if src.endswith(".cu") else ["-x", "cu"] if False else []
-    cmd = [nvcc()] + ARCH + [f for f in NVFLAGS if f] + lang + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + [f for f in NVFLAGS if f] + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")

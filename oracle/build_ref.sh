@@ -13,8 +13,11 @@
 #   moldy_ref_harness[_fast]  oracle/ref_harness.c linked against each
 #   moldy_ref_examples        oracle/ref_examples.c (start-up of the examples)
 #   moldy_ref_md[_fast]       oracle/ref_md.c (constant-energy do_step runs)
-# All of main.c is left out; the harness defines control/ithread/nthreads
-# (src/main.c:83-84).  version.h (normally written by a git hook) is generated
+# main.c is left out of the libraries (the harness defines control/ithread/
+# nthreads, src/main.c:83-84); it is compiled alone into obj_main/main.o for
+# the test that links the reference's own program against libmoldy_gb300.so.
+# The source directory used is recorded in oracle/_ref/SRC_DIR.  version.h
+# (normally written by a git hook) is generated
 # into oracle/_ref/.  Exits 0 without building when the sources are absent.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -42,7 +45,11 @@ for f in $FILES; do
     $CC -O2 -ffast-math $extra -fPIC -std=gnu89 -w -I"$OUT" -I"$SRC" $DEFS -c "$SRC/$f.c" -o "$OUT/obj_fast/$f.o" &
     pids="$pids $!"
 done
+mkdir -p "$OUT/obj_main"
+$CC -O2 -fPIC -std=gnu89 -w -I"$OUT" -I"$SRC" $DEFS -c "$SRC/main.c" -o "$OUT/obj_main/main.o" &
+pids="$pids $!"
 for p in $pids; do wait $p; done
+(cd "$SRC" && pwd) > "$OUT/SRC_DIR"
 $CC -shared -o "$OUT/libmoldyref.so" "$OUT"/obj/*.o -lm
 $CC -shared -o "$OUT/libmoldyref_fast.so" "$OUT"/obj_fast/*.o -lm
 $CC -O2 -std=gnu99 -w -I"$SRC" -I"$OUT" $DEFS "$HERE/ref_harness.c" -o "$OUT/moldy_ref_harness" \

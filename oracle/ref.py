@@ -24,6 +24,20 @@ def available() -> bool:
     return os.path.exists(os.path.join(REF_DIR, "moldy_ref_harness"))
 
 
+def source_dir() -> Optional[str]:
+    """The reference's src/ directory: MOLDY_SRC when set, else the one
+    oracle/build_ref.sh last built from (recorded in oracle/_ref/SRC_DIR);
+    None when neither exists (as on a machine without the sources)."""
+    cand = os.environ.get("MOLDY_SRC")
+    if not cand:
+        try:
+            with open(os.path.join(REF_DIR, "SRC_DIR")) as f:
+                cand = f.read().strip()
+        except OSError:
+            return None
+    return cand if os.path.isfile(os.path.join(cand, "force.c")) else None
+
+
 def build() -> bool:
     """Build oracle/_ref from the reference sources if they are present."""
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True,

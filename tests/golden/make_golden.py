@@ -34,7 +34,6 @@ from moldy_gb300 import system as S  # noqa: E402
 from moldy_gb300 import pairset  # noqa: E402
 from oracle import ref  # noqa: E402
 
-REF_SRC = os.environ.get("MOLDY_SRC", "/root/reference/src")
 FULL_KEYS_MAX = 60000
 
 
@@ -82,7 +81,7 @@ def examples():
     for c in ["water", "tips2", "tip4p", "mgclh2o", "argon", "quartz", "clay"]:
         with tempfile.TemporaryDirectory() as td:
             wd = os.path.join(td, "ex")
-            shutil.copytree(os.path.join(REF_SRC, "examples"), wd)
+            shutil.copytree(os.path.join(ref.source_dir(), "examples"), wd)
             out = os.path.join(wd, c + ".mdsys")
             subprocess.run([exe, "control." + c, out], cwd=wd, check=True,
                            stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)

@@ -9,9 +9,10 @@ import tempfile
 import pytest
 
 from conftest import ROOT
+from oracle.ref import source_dir
 
 INCLUDE = os.path.join(ROOT, "include")
-REF_SRC = "/root/reference/src"
+REF_SRC = source_dir()
 
 
 def declared_functions():
@@ -100,7 +101,7 @@ int main(void) {
 """
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+@pytest.mark.skipif(REF_SRC is None, reason="reference sources not present")
 def test_struct_layout_matches_the_reference_header():
     outs = []
     with tempfile.TemporaryDirectory() as td:
