@@ -178,22 +178,28 @@ mdgpu_status mdgpu_rdf_counts(mdgpu_ctx *ctx, const double *h, const double *sit
                               const double *c_of_m, double limit, int nbins, uint64_t *counts);
 
 /* Reciprocal-space Ewald sum that allocates nothing.  No counterpart in the
- * reference.  For callers that cannot call cudaMalloc: code running under
- * CUDA stream capture (allocation cannot be captured into a graph), hosts
- * that own all device memory through their own pools, and step loops that
- * must not take the allocator's locks or fail for lack of memory mid-run.
- * Adds the k-space forces into d_force[3][nsites], the k-space energy
- * (without the self and sheet terms of ewald(), src/ewald.c:367-433) into
- * *d_pe and the stress upper triangle into d_stress[9]; every pointer is the
- * caller's device memory, h is on the host, charges d_chg[nsites] are in
- * program units.  FP32-mixed arithmetic.  Intermediates live in a static
- * device array of MDGPU_NOALLOC_SCRATCH_BYTES that every GPU loading the
- * library holds until exit; nsites above MDGPU_NOALLOC_MAX_SITES or more
- * than MDGPU_NOALLOC_MAX_KVEC k-vectors return MDGPU_E_CAPACITY.  The first
- * call on a device looks the array up (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU (other streams, other host threads) race.  Runs on `stream`
- * (a cudaStream_t, NULL for the default stream) of the current device. */
+ * reference.  For callers that cannot call cudaMalloc: hosts that own all
+ * device memory through their own pools, and step loops that must not take
+ * the allocator's locks, synchronise the device or fail for lack of memory
+ * mid-run.  Adds the k-space forces into d_force[3][nsites], the k-space
+ * energy (without the self and sheet terms of ewald(), src/ewald.c:367-433)
+ * into *d_pe and the stress upper triangle into d_stress[9]; every pointer is
+ * the caller's device memory, h is on the host and read during the call
+ * only, charges d_chg[nsites] are in program units.  FP32-mixed arithmetic;
+ * the sites are ordered by a cell grid inside the scratch, so ionic systems
+ * listed species by species keep FP32 accuracy.  Intermediates, the k-vector
+ * list included, live in a static device array of
+ * MDGPU_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit; nsites above MDGPU_NOALLOC_MAX_SITES or more than
+ * MDGPU_NOALLOC_MAX_KVEC k-vectors return MDGPU_E_CAPACITY.  The first call
+ * on a device looks the array up (cudaGetSymbolAddress) and keeps its address
+ * for the process (the device's primary context must stay the same); make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (other streams, other host threads) race.  A
+ * device-side failure (a bounded wait that expired) is not seen by the
+ * returned status, which covers the launches only: it leaves NaN in *d_pe and
+ * in the forces.  Runs on `stream` (a cudaStream_t, NULL for the default
+ * stream) of the current device. */
 #define MDGPU_NOALLOC_MAX_SITES 16384
 #define MDGPU_NOALLOC_MAX_KVEC 8192
 #define MDGPU_NOALLOC_SCRATCH_BYTES (6u << 20)

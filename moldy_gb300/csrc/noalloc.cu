@@ -1,25 +1,28 @@
 // Reciprocal-space Ewald sum without any allocation: mdgpu_ewald_kspace_noalloc.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA stream is
-// being captured into a graph (allocation is not a capturable operation),
-// hosts that hand out all device memory from their own fixed pools and forbid
-// libraries to allocate behind their back, and step loops that must not take
-// the allocator's locks or risk an out-of-memory failure part-way through a
-// run.  For them this entry point runs the reciprocal-space kernels of the
-// force path with every intermediate array carved out of one file-scope
-// static device array of fixed size (MDGPU_NOALLOC_SCRATCH_BYTES, held by
-// every GPU that loads the library until the process exits), and the
-// k-vector list built in fixed static host buffers.  The caller passes the
-// inputs and outputs in its own device memory.
+// Some callers cannot call cudaMalloc: hosts that hand out all device memory
+// from their own fixed pools and forbid libraries to allocate behind their
+// back, and step loops that must not take the allocator's locks, synchronise
+// the device, or risk an out-of-memory failure part-way through a run.  For
+// them this entry point runs the reciprocal-space kernels of the force path
+// with every intermediate array -- the k-vector list included, which a small
+// kernel builds from the cell matrix, alpha and the k-cutoff passed by value
+// -- carved out of one file-scope static device array of fixed size
+// (MDGPU_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library
+// until the process exits).  The caller passes the inputs and outputs in its
+// own device memory; no host buffer is read after the call returns.
 //
 // Limits (calls beyond them are rejected with MDGPU_E_CAPACITY):
 //   nsites <= MDGPU_NOALLOC_MAX_SITES, k-vectors <= MDGPU_NOALLOC_MAX_KVEC.
 //
 // The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (which may load the module onto that device); make
-// that first call before any stream capture.  Every call shares the same
-// scratch and host buffers: calls that overlap -- on different streams, or
-// from different host threads -- race and corrupt each other.
+// cudaGetSymbolAddress (which may load the module onto that device) and
+// keeps it for the life of the process: it assumes the device's primary
+// context stays the same (no cudaDeviceReset in between).  Make that first
+// call before any stream capture.  Every call shares the same scratch:
+// calls that overlap on the GPU -- on different streams, or from different
+// host threads -- race and corrupt each other.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -48,6 +51,9 @@ constexpr int MAX_SITES = MDGPU_NOALLOC_MAX_SITES;
 constexpr int MAX_KVEC = MDGPU_NOALLOC_MAX_KVEC;
 constexpr int MAX_CHUNKS = 16;
 constexpr int MAX_SPLITS = 4;
+// site ordering grid: at most OG^3 cells, slot offsets held as 16-bit counts
+constexpr int OG = 8;
+static_assert(MAX_SITES <= 65535, "the ordering counts are 16-bit");
 
 constexpr size_t al(size_t x) { return (x + 255) / 256 * 256; }
 // byte offsets of the scratch regions
@@ -63,18 +69,241 @@ constexpr size_t O_PH = O_KDAT + al(sizeof(float4) * MAX_KVEC);
 constexpr size_t O_Z = O_PH + al(sizeof(int4) * MAX_SITES);
 constexpr size_t O_ZP = O_Z + al(sizeof(float2) * MAX_SITES);
 constexpr size_t O_SORT = O_ZP + al(sizeof(float2) * MAX_SITES * KI);
-constexpr size_t O_PART = O_SORT + al(sizeof(int) * MAX_SITES);
+constexpr size_t O_KEY = O_SORT + al(sizeof(int) * MAX_SITES);
+constexpr size_t O_PART = O_KEY + al(sizeof(int) * MAX_SITES);
 constexpr size_t O_FPART = O_PART + al(sizeof(float2) * MAX_CHUNKS * MAX_KVEC);
 constexpr size_t O_BLK = O_FPART + al(sizeof(double) * MAX_SPLITS * 3 * MAX_SITES);
 constexpr size_t O_END = O_BLK + al(sizeof(double) * 8 * ((MAX_KVEC + 255) / 256));
 static_assert(O_END <= MDGPU_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the stated size");
 
-// host-side k-list in fixed static buffers (same enumeration and prefactors
-// as the allocating path: ewald(), src/ewald.c:441-461, 510-511)
-int4 h_item[MAX_KVEC];
-int h_k0[MAX_KVEC + 1];
-float2 h_kxy[MAX_KVEC];
-double h_kvec[3 * MAX_KVEC], h_coef[MAX_KVEC], h_coef2[MAX_KVEC];
+// error bits of the result record set here (the shared kernels use 1 and 4)
+constexpr int ERR_KLIST = 64;   // the device k-list disagrees with the host's count
+
+// The k-vector list's geometry, by value: 2 pi h^-1 (upper triangle), the
+// cut, alpha's exponent factor and the energy prefactor 2 / (eps0 V).
+struct KlArgs {
+   double hp0, hp1, hp2, hp4, hp5, hp8;
+   double kcsq, r4a, pref;
+   int hmax, kmax, lmax;
+   int nk, ni;   // the host's counts (capacity already checked)
+};
+
+// Column c of the enumeration: (h, k) in the order of src/ewald.c:441-461,
+// h = 0 taking k >= 0 only.
+__host__ __device__ inline void kl_column(const KlArgs &a, int c, int &hh, int &k)
+{
+   if (c <= a.kmax) {
+      hh = 0;
+      k = c;
+   } else {
+      const int w = 2 * a.kmax + 1, cc = c - (a.kmax + 1);
+      hh = 1 + cc / w;
+      k = cc % w - a.kmax;
+   }
+}
+
+// One column of the k-list: its k-vectors (l ascending, kept where
+// |k|^2 < k_cutoff^2) grouped into items of up to KI consecutive l.  Counts
+// them (WRITE false) or writes them from k index nk and item index ni on.
+// Every product and sum is rounded separately, as the host computes it
+// (its code is built without contraction), so both see the same cut.
+template <bool WRITE>
+__host__ __device__ inline void kl_scan_column(const KlArgs &a, int hh, int k, int &nk, int &ni,
+                                               int4 *item, int *k0, float2 *kxy, double *kvec,
+                                               double *coef, double *coef2)
+{
+#ifdef __CUDA_ARCH__
+#define KL_MUL(x, y) __dmul_rn(x, y)
+#define KL_ADD(x, y) __dadd_rn(x, y)
+#else
+#define KL_MUL(x, y) ((x) * (y))
+#define KL_ADD(x, y) ((x) + (y))
+#endif
+   const double dh = (double)hh, dk = (double)k;
+   const double kx = KL_MUL(dh, a.hp0);
+   const double ky = KL_ADD(KL_MUL(dh, a.hp1), KL_MUL(dk, a.hp4));
+   const double kzt = KL_ADD(KL_MUL(dh, a.hp2), KL_MUL(dk, a.hp5));
+   const double ksq = KL_ADD(KL_MUL(kx, kx), KL_MUL(ky, ky));
+   int prev_l = -1000000, cur = 0;
+   for (int l = (hh == 0 && k == 0 ? 1 : -a.lmax); l <= a.lmax; l++) {
+      const double kz = KL_ADD(kzt, KL_MUL((double)l, a.hp8));
+      const double ks = KL_ADD(ksq, KL_MUL(kz, kz));
+      if (!(ks < a.kcsq)) continue;
+      const bool extend = prev_l == l - 1 && cur > 0 && cur < KI;
+      if (!extend) {
+         if (WRITE && ni < a.ni) {
+            item[ni] = make_int4(hh, k, l, 1);
+            k0[ni] = nk;
+            kxy[ni] = make_float2((float)kx, (float)ky);
+         }
+         ni++;
+         cur = 1;
+      } else {
+         if (WRITE && ni - 1 < a.ni) item[ni - 1].w++;
+         cur++;
+      }
+      prev_l = l;
+      if (WRITE && nk < a.nk) {
+         kvec[nk] = kx;
+         kvec[a.nk + nk] = ky;
+         kvec[2 * a.nk + nk] = kz;
+         const double e = KL_MUL(ks, a.r4a);
+#ifdef __CUDA_ARCH__
+         coef[nk] = __ddiv_rn(__dmul_rn(a.pref, exp(e)), ks);
+         coef2[nk] = __ddiv_rn(__dmul_rn(2.0, __dsub_rn(1.0, e)), ks);
+#endif
+      }
+      nk++;
+   }
+#undef KL_MUL
+#undef KL_ADD
+}
+
+// Builds the k-vector list on the device (one block of 1024 threads): each
+// thread takes a run of consecutive columns, counts them, a block scan gives
+// every run its first k and item index, then the runs are written.  The
+// totals are checked against the host's counts (ERR_KLIST on a mismatch;
+// nothing is written past them).
+__global__ void __launch_bounds__(1024)
+k_klist_na(KlArgs a, int4 *__restrict__ item, int *__restrict__ k0, float2 *__restrict__ kxy,
+           double *__restrict__ kvec, double *__restrict__ coef, double *__restrict__ coef2,
+           DevOut *__restrict__ out)
+{
+   __shared__ int wk[32], wi[32];
+   const int ncol = (a.hmax + 1) * (2 * a.kmax + 1) - a.kmax;
+   const int per = (ncol + blockDim.x - 1) / blockDim.x;
+   const int c0 = min(ncol, (int)threadIdx.x * per), c1 = min(ncol, c0 + per);
+   int nk = 0, ni = 0;
+   for (int c = c0; c < c1; c++) {
+      int hh, k;
+      kl_column(a, c, hh, k);
+      kl_scan_column<false>(a, hh, k, nk, ni, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+   }
+   // block-wide exclusive scan of (nk, ni)
+   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+   int sk = nk, si = ni;
+   for (int o = 1; o < 32; o <<= 1) {
+      const int tk = __shfl_up_sync(0xffffffffu, sk, o), ti = __shfl_up_sync(0xffffffffu, si, o);
+      if (lane >= o) {
+         sk += tk;
+         si += ti;
+      }
+   }
+   if (lane == 31) {
+      wk[w] = sk;
+      wi[w] = si;
+   }
+   __syncthreads();
+   if (w == 0) {
+      int vk = wk[lane], vi = wi[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+         const int tk = __shfl_up_sync(0xffffffffu, vk, o), ti = __shfl_up_sync(0xffffffffu, vi, o);
+         if (lane >= o) {
+            vk += tk;
+            vi += ti;
+         }
+      }
+      wk[lane] = vk;
+      wi[lane] = vi;
+   }
+   __syncthreads();
+   int ok = sk - nk + (w > 0 ? wk[w - 1] : 0), oi = si - ni + (w > 0 ? wi[w - 1] : 0);
+   if (threadIdx.x == 0 && (wk[31] != a.nk || wi[31] != a.ni)) atomicOr(&out->err, ERR_KLIST);
+   for (int c = c0; c < c1; c++) {
+      int hh, k;
+      kl_column(a, c, hh, k);
+      kl_scan_column<true>(a, hh, k, ok, oi, item, k0, kxy, kvec, coef, coef2);
+   }
+}
+
+// Orders the sites by a coarse cell grid (g^3 cells of the fractional
+// co-ordinates, ascending site index inside a cell), one block of 32 warps:
+// a structure-factor chunk is then a compact, nearly neutral region, so its
+// FP32 partial sum stays small even where the whole sum cancels (an ionic
+// crystal listed species by species would otherwise give chunks of a single
+// charge sign).  Warp w owns sites [w S, (w + 1) S): it counts them per
+// cell, one scan over (cell, warp) gives each warp its first slot per cell,
+// and the warp places its sites in order.  sorted[slot] = site.
+__global__ void __launch_bounds__(1024)
+k_order_na(int N, const double *__restrict__ site, double hi0, double hi1, double hi2, double hi4,
+           double hi5, double hi8, int g, int *__restrict__ key, int *__restrict__ sorted)
+{
+   __shared__ unsigned short tab[OG * OG * OG * 32];   // [cell][warp]: count, then first slot
+   __shared__ int wsum[32];
+   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+   const int ncell = g * g * g, nt = ncell * 32;
+   for (int j = threadIdx.x; j < nt; j += blockDim.x) tab[j] = 0;
+   __syncthreads();
+   const int S = (N + 31) / 32, s0 = min(N, w * S), s1 = min(N, s0 + S);
+   const unsigned int lt = (1u << lane) - 1u;
+   for (int b = s0; b < s1; b += 32) {
+      const int i = b + lane;
+      int kk = -1;
+      if (i < s1) {
+         const double x = site[i], y = site[N + i], z = site[2 * (size_t)N + i];
+         double f[3] = {hi0 * x + hi1 * y + hi2 * z, hi4 * y + hi5 * z, hi8 * z};
+         int cc[3];
+         for (int d = 0; d < 3; d++) {
+            double u = f[d] - floor(f[d]);
+            int v = (u == u) ? (int)(u * g) : 0;   // a NaN co-ordinate goes to cell 0
+            cc[d] = v < 0 ? 0 : (v >= g ? g - 1 : v);
+         }
+         kk = (cc[0] * g + cc[1]) * g + cc[2];
+         key[i] = kk;
+      }
+      const unsigned int peers = __match_any_sync(0xffffffffu, kk);
+      if (kk >= 0 && (peers & lt) == 0) tab[kk * 32 + w] += (unsigned short)__popc(peers);
+      __syncwarp();
+   }
+   __syncthreads();
+   // exclusive scan over tab in (cell, warp) order: 1024 threads, a run each
+   const int per = (nt + blockDim.x - 1) / blockDim.x;
+   const int j0 = min(nt, (int)threadIdx.x * per), j1 = min(nt, j0 + per);
+   int tot = 0;
+   for (int j = j0; j < j1; j++) tot += tab[j];
+   int sc = tot;
+   for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, sc, o);
+      if (lane >= o) sc += t;
+   }
+   if (lane == 31) wsum[w] = sc;
+   __syncthreads();
+   if (w == 0) {
+      int v = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+         const int t = __shfl_up_sync(0xffffffffu, v, o);
+         if (lane >= o) v += t;
+      }
+      wsum[lane] = v;
+   }
+   __syncthreads();
+   int run = sc - tot + (w > 0 ? wsum[w - 1] : 0);
+   for (int j = j0; j < j1; j++) {
+      const int cnt = tab[j];
+      tab[j] = (unsigned short)run;
+      run += cnt;
+   }
+   __syncthreads();
+   for (int b = s0; b < s1; b += 32) {
+      const int i = b + lane;
+      const int kk = i < s1 ? key[i] : -1;
+      const unsigned int peers = __match_any_sync(0xffffffffu, kk);
+      if (kk >= 0) sorted[tab[kk * 32 + w] + __popc(peers & lt)] = i;
+      __syncwarp();
+      if (kk >= 0 && (peers & lt) == 0) tab[kk * 32 + w] += (unsigned short)__popc(peers);
+      __syncwarp();
+   }
+}
+
+// A structure-factor tile that never arrived, or a k-list that does not
+// match the host's, leaves the forces undefined: they are overwritten with
+// NaN (the energy too, in k_add_energy), so a caller that checks only the
+// forces sees the failure.
+__global__ void k_poison_na(int n3, const DevOut *__restrict__ o, double *__restrict__ force)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n3 && (o->err & (4 | ERR_KLIST))) force[i] = __longlong_as_double(0x7ff8000000000000ll);
+}
 
 // per k: S(k) from the chunk partials (FP64, fixed order), energy, stress and
 // the force coefficients A = coeff Re S, B = coeff Im S (src/ewald.c:525-553);
@@ -119,18 +348,13 @@ k_kreduce_na(int nk, int nchunks, const float2 *__restrict__ part, const double 
    }
 }
 
-__global__ void k_iota(int n, int *a)
-{
-   int i = blockIdx.x * blockDim.x + threadIdx.x;
-   if (i < n) a[i] = i;
-}
-
 // adds the k-space energy and stress upper triangle into the caller's outputs
 __global__ void k_add_energy(const DevOut *o, double *pe, double *stress)
 {
    if (threadIdx.x != 0) return;
-   // a structure-factor tile that never arrived leaves the energy undefined
-   *pe += (o->err & 4) ? __longlong_as_double(0x7ff8000000000000ll) : o->pe_k;
+   // a structure-factor tile that never arrived, or a mismatched k-list,
+   // leaves the energy undefined
+   *pe += (o->err & (4 | ERR_KLIST)) ? __longlong_as_double(0x7ff8000000000000ll) : o->pe_k;
    stress[0] += o->st_k[0];
    stress[1] += o->st_k[1];
    stress[2] += o->st_k[2];
@@ -146,7 +370,8 @@ static __device__ __align__(256) unsigned char mdgpu_noalloc_scratch[MDGPU_NOALL
 
 namespace {
 constexpr int MAX_DEVICES = 64;
-unsigned char *g_scratch[MAX_DEVICES];   // device address of the array, per device
+// device address of the array, per device (looked up once per device)
+std::atomic<unsigned char *> g_scratch[MAX_DEVICES];
 }  // namespace
 
 extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, const double *d_site,
@@ -164,55 +389,51 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    // set-up, once per device, with that device current
    int dev = 0;
    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return MDGPU_E_CUDA;
-   if (!g_scratch[dev]) {
+   unsigned char *S = g_scratch[dev].load();
+   if (!S) {
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, mdgpu_noalloc_scratch) != cudaSuccess || !p) {
          cudaGetLastError();
          return MDGPU_E_CUDA;
       }
-      g_scratch[dev] = (unsigned char *)p;
+      S = (unsigned char *)p;
+      g_scratch[dev].store(S);
    }
-   unsigned char *S = g_scratch[dev];
 
-   // k-vector list into the static host buffers
+   // the k-list's geometry (src/ewald.c:441-461, 510-511), and its size
+   // counted here so that the capacity check is made before any launch;
+   // the list itself is built on the device from these values
    const double kc = k_cutoff;
-   const int hmax = (int)std::floor(kc / (2 * PI) * h[0]);
-   const int kmax = (int)std::floor(kc / (2 * PI) * std::sqrt(h[1] * h[1] + h[4] * h[4]));
-   const int lmax = (int)std::floor(kc / (2 * PI) * std::sqrt(h[2] * h[2] + h[5] * h[5] + h[8] * h[8]));
-   double hinv[9], hp[9];
+   double hinv[9];
    inv3(h, hinv);
-   for (int i = 0; i < 9; i++) hp[i] = 2 * PI * hinv[i];
-   const double kcsq = kc * kc, vol = det3(h), r4a = -1.0 / (4.0 * alpha * alpha), eps0 = 0.25 / PI;
-   int nk = 0, ni = 0;
-   for (int hh = 0; hh <= hmax; hh++)
-      for (int k = (hh == 0 ? 0 : -kmax); k <= kmax; k++) {
-         const double kx = hh * hp[0] + k * hp[3], ky = hh * hp[1] + k * hp[4];
-         const double kzt = hh * hp[2] + k * hp[5], ksq = kx * kx + ky * ky;
-         int prev_l = -1000000;
-         for (int l = (hh == 0 && k == 0 ? 1 : -lmax); l <= lmax; l++) {
-            const double kz = kzt + l * hp[8];
-            if (!(kz * kz + ksq < kcsq)) continue;
-            if (nk >= MAX_KVEC) return MDGPU_E_CAPACITY;
-            const bool extend = ni > 0 && prev_l == l - 1 && h_item[ni - 1].x == hh &&
-                                h_item[ni - 1].y == k && h_item[ni - 1].w < KI;
-            if (extend) {
-               h_item[ni - 1].w++;
-            } else {
-               h_item[ni] = make_int4(hh, k, l, 1);
-               h_k0[ni] = nk;
-               h_kxy[ni] = make_float2((float)kx, (float)ky);
-               ni++;
-            }
-            prev_l = l;
-            const double ks = kx * kx + ky * ky + kz * kz;
-            h_kvec[nk] = kx;
-            h_kvec[MAX_KVEC + nk] = ky;
-            h_kvec[2 * MAX_KVEC + nk] = kz;
-            h_coef[nk] = 2.0 / (eps0 * vol) * std::exp(ks * r4a) / ks;
-            h_coef2[nk] = 2.0 * (1.0 - ks * r4a) / ks;
-            nk++;
-         }
+   KlArgs ka;
+   ka.hp0 = 2 * PI * hinv[0];
+   ka.hp1 = 2 * PI * hinv[1];
+   ka.hp2 = 2 * PI * hinv[2];
+   ka.hp4 = 2 * PI * hinv[4];
+   ka.hp5 = 2 * PI * hinv[5];
+   ka.hp8 = 2 * PI * hinv[8];
+   ka.hmax = (int)std::floor(kc / (2 * PI) * h[0]);
+   ka.kmax = (int)std::floor(kc / (2 * PI) * std::sqrt(h[1] * h[1] + h[4] * h[4]));
+   ka.lmax = (int)std::floor(kc / (2 * PI) * std::sqrt(h[2] * h[2] + h[5] * h[5] + h[8] * h[8]));
+   ka.kcsq = kc * kc;
+   ka.r4a = -1.0 / (4.0 * alpha * alpha);
+   ka.pref = 2.0 / (0.25 / PI * det3(h));
+   ka.nk = ka.ni = 0;
+   if ((double)(ka.hmax + 1) * (2.0 * ka.kmax + 1) * (2.0 * ka.lmax + 1) > 1e7) return MDGPU_E_CAPACITY;
+   {
+      const int ncol = (ka.hmax + 1) * (2 * ka.kmax + 1) - ka.kmax;
+      int nk = 0, ni = 0;
+      for (int c = 0; c < ncol && nk <= MAX_KVEC; c++) {
+         int hh, k;
+         kl_column(ka, c, hh, k);
+         kl_scan_column<false>(ka, hh, k, nk, ni, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
       }
+      if (nk > MAX_KVEC) return MDGPU_E_CAPACITY;
+      ka.nk = nk;
+      ka.ni = ni;
+   }
+   const int nk = ka.nk, ni = ka.ni;
    if (nk == 0) return MDGPU_OK;
 
    DevOut *out = (DevOut *)(S + O_OUT);
@@ -224,31 +445,21 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    float4 *kdat = (float4 *)(S + O_KDAT);
    int4 *ph = (int4 *)(S + O_PH);
    float2 *z = (float2 *)(S + O_Z), *zp = (float2 *)(S + O_ZP);
-   int *sorted = (int *)(S + O_SORT);
+   int *sorted = (int *)(S + O_SORT), *key = (int *)(S + O_KEY);
    float2 *part = (float2 *)(S + O_PART);
    double *fpart = (double *)(S + O_FPART), *blk = (double *)(S + O_BLK);
 
-   cudaError_t e = cudaSuccess;
-   auto up = [&](void *dst, const void *src, size_t bytes) {
-      if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
-   };
-   up(item, h_item, sizeof(int4) * ni);
-   up(k0, h_k0, sizeof(int) * ni);
-   up(kxy, h_kxy, sizeof(float2) * ni);
-   // k-vector components are laid out [3][nk] for the kernels
-   up(kvec, h_kvec, sizeof(double) * nk);
-   up(kvec + nk, h_kvec + MAX_KVEC, sizeof(double) * nk);
-   up(kvec + 2 * nk, h_kvec + 2 * MAX_KVEC, sizeof(double) * nk);
-   up(coef, h_coef, sizeof(double) * nk);
-   up(coef2, h_coef2, sizeof(double) * nk);
-   // the result record must start at zero; every other region is written
-   // in full before it is read
-   if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, sizeof(DevOut), st);
-   if (e != cudaSuccess) return MDGPU_E_CUDA;
+   // the result record must start at zero (the last call left its values);
+   // every other region is written in full before it is read
+   if (cudaMemsetAsync(out, 0, sizeof(DevOut), st) != cudaSuccess) return MDGPU_E_CUDA;
+   k_klist_na<<<1, 1024, 0, st>>>(ka, item, k0, kxy, kvec, coef, coef2, out);
 
    const int N = nsites;
-   // site order: as given (no link-cell binning in this variant)
-   k_iota<<<(N + 255) / 256, 256, 0, st>>>(N, sorted);
+   // sites in the order of a coarse cell grid, about 32 sites a cell
+   int g = (int)std::lround(std::cbrt(N / 32.0));
+   g = g < 1 ? 1 : (g > OG ? OG : g);
+   k_order_na<<<1, 1024, 0, st>>>(N, d_site, hinv[0], hinv[1], hinv[2], hinv[4], hinv[5], hinv[8], g, key,
+                                  sorted);
    k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, N, sorted, d_site, d_chg, hinv[0], hinv[1], hinv[2], hinv[3],
                                            hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], 1, ph, z, zp,
                                            nullptr, nullptr, nullptr);
@@ -266,9 +477,10 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    const int per_split = (ni + splits - 1) / splits;
    splits = (ni + per_split - 1) / per_split;
    k_force32<<<dim3((N + 2 * FT_THREADS - 1) / (2 * FT_THREADS), splits), FT_THREADS, 0, st>>>(
-      item, k0, kxy, ni, nk, per_split, kdat, ph, zp, d_chg, sorted, N, 0, (float)hp[8], fpart);
+      item, k0, kxy, ni, nk, per_split, kdat, ph, zp, d_chg, sorted, N, 0, (float)ka.hp8, fpart);
    k_fsum<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, splits, fpart, d_force, 1);
+   k_poison_na<<<(3 * N + 255) / 256, 256, 0, st>>>(3 * N, out, d_force);
    k_add_energy<<<1, 32, 0, st>>>(out, d_pe, d_stress);
-   e = cudaGetLastError();
+   const cudaError_t e = cudaGetLastError();
    return e == cudaSuccess ? MDGPU_OK : MDGPU_E_CUDA;
 }

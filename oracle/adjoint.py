@@ -183,11 +183,11 @@ def _self_sheet_grad(sysm, gq: np.ndarray) -> float:
     return ga
 
 
-def _forces(sysm) -> Tuple[np.ndarray, float]:
-    rs = port.force_calc(sysm)
+def _forces(sysm, nthreads: int = 1) -> Tuple[np.ndarray, float]:
+    rs = port.force_calc(sysm, nthreads=nthreads)
     f, pe = rs.force, rs.pe
     if sysm.control.alpha > 1e-7:
-        ks = port.ewald(sysm)
+        ks = port.ewald(sysm, nthreads=nthreads)
         f, pe = f + ks.force, pe + ks.pe
     return f, pe
 
@@ -279,6 +279,6 @@ def energy(sysm) -> float:
     return _forces(sysm)[1]
 
 
-def fm_loss(sysm, f_ref, weight: float = 1.0) -> float:
-    F, _ = _forces(sysm)
+def fm_loss(sysm, f_ref, weight: float = 1.0, nthreads: int = 1) -> float:
+    F, _ = _forces(sysm, nthreads)
     return weight * float(np.sum((F - f_ref) ** 2))

@@ -115,22 +115,25 @@ def _water_theta_grads(ff_grad, base):
                      (np.sum(gq[ids == 2]) - 2.0 * np.sum(gq[ids == 3])) / CONV_Q, ff_grad["alpha"]])
 
 
+@pytest.mark.parametrize("nside,nframes", [(8, 2), (16, 4)])
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_water_fit_gradients_match_oracle_finite_differences(port_built, prec):
-    """Rigid water, 2048 sites, two seeded frames: the force-matching loss
-    with epsilon, sigma and q_H scaled by seeded factors in [0.9, 1.1] (q_M =
-    -2 q_H), reference forces at the original parameters.  The GPU gradient
-    with respect to (epsilon, sigma, q_H, alpha), through the torch harness,
-    is within 1e-4 relative of central finite differences of the FP64 C
-    restatement (step 1e-5 relative)."""
+def test_water_fit_gradients_match_oracle_finite_differences(port_built, prec, nside, nframes):
+    """Rigid water, 2048 sites over two seeded frames and the force-matching
+    workload's size, 16,384 sites (4096 molecules) over four: the
+    force-matching loss with epsilon, sigma and q_H scaled by seeded factors
+    in [0.9, 1.1] (q_M = -2 q_H), reference forces at the original
+    parameters.  The GPU gradient with respect to (epsilon, sigma, q_H,
+    alpha), through the torch harness, is within 1e-4 relative of central
+    finite differences of the FP64 C restatement (step 1e-5 relative)."""
     import torch
 
     from moldy_gb300 import ForceField, system
     from moldy_gb300.fitting import FitProblem, ForceMatchLoss, water_frames, water_tables
     from oracle import adjoint
 
-    base = system.water(nside=8, seed=11)
-    frames = water_frames(base, 2, seed=12)
+    threads = os.cpu_count() or 1
+    base = system.water(nside=nside, seed=11)
+    frames = water_frames(base, nframes, seed=12)
     theta0 = np.array([0.6485, 3.154, 0.52, base.control.alpha])
     rng = np.random.default_rng(13)
     theta = theta0 * np.append(rng.uniform(0.9, 1.1, 3), 1.0)
@@ -143,11 +146,11 @@ def test_water_fit_gradients_match_oracle_finite_differences(port_built, prec):
         qid[2], qid[3] = t[2] / system.CONV_Q, -2 * t[2] / system.CONV_Q
         return dataclasses.replace(fr, potpar=pot.numpy(), site_charge=qid, control=ctl)
 
-    f_refs = [adjoint._forces(sys_at(theta0, fr))[0] for fr in frames]
+    f_refs = [adjoint._forces(sys_at(theta0, fr), threads)[0] for fr in frames]
     w = 1.0 / (len(frames) * f_refs[0].size)
 
     def oracle_loss(t):
-        return sum(adjoint.fm_loss(sys_at(t, fr), f, w) for fr, f in zip(frames, f_refs))
+        return sum(adjoint.fm_loss(sys_at(t, fr), f, w, threads) for fr, f in zip(frames, f_refs))
 
     fd = np.zeros(4)
     for k in range(4):

@@ -6,9 +6,12 @@ of the reference (the oracle, bit-exact with the reference on every fixture):
   form within 1e-5 relative RMS force error of the FP64 oracle;
 * 2048-site water (512 rigid molecules, alpha 0.3, rc 9 Å, k-cutoff for
   1e-5): both forms;
-* 131,072-site water (the benchmark workload): the mixed form against the
-  FP64 GPU form (the oracle takes ~3 s there; its real-space part alone is
-  compared)."""
+* 131,072-site water (the benchmark workload, 69,876 k-vectors): both
+  forms' total forces (real space + reciprocal space), energies and stress
+  against the oracle run on every host core, and the mixed form against the
+  FP64 GPU form."""
+import os
+
 import numpy as np
 import pytest
 
@@ -19,11 +22,23 @@ def rel_rms(a, b):
     return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
 
 
-def oracle_forces(sysm, threads=16):
+def oracle_forces(sysm, threads=None):
     from oracle import port
+    threads = threads or os.cpu_count() or 1
     r = port.force_calc(sysm, nthreads=threads)
     e = port.ewald(sysm, nthreads=threads)
     return r.force + e.force, r.pe, e.pe
+
+
+@pytest.fixture(scope="module")
+def water131k(port_built):
+    """The benchmark configuration and the oracle's real-space and
+    reciprocal-space results for it (about 3 s on 16 host threads)."""
+    from moldy_gb300 import system
+    from oracle import port
+    sysm = system.water(nside=32, seed=7)
+    threads = os.cpu_count() or 1
+    return sysm, port.force_calc(sysm, nthreads=threads), port.ewald(sysm, nthreads=threads)
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("mixed", 1e-5)])
@@ -52,18 +67,40 @@ def test_water_2048(port_built, prec, tol):
     assert abs((pe[0] + pe[1]) - (pr + pk)) < tol * (abs(pr) + abs(pk))
 
 
-def test_water_131072_mixed_against_fp64(port_built):
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("mixed", 1e-5)])
+def test_water_131072_total_forces_against_the_oracle(water131k, prec, tol):
+    """The headline workload: both parts and their sum against the oracle
+    (src/force.c:1108-1320 and src/ewald.c:280-589 restated)."""
+    from moldy_gb300 import ForceField
+    sysm, r, e = water131k
+    ff = ForceField(sysm, precision=prec)
+    fr, per, str_ = ff.force_calc()
+    fk, pek, stk = ff.ewald()
+    f, pe, st = ff.forces()
+    nk = ff.info()["nkvec"]
+    ff.close()
+    assert nk == 69876 == e.info.nkvec
+    ftot = r.force + e.force
+    assert rel_rms(f, ftot) < tol, rel_rms(f, ftot)
+    assert rel_rms(fr, r.force) < tol, rel_rms(fr, r.force)
+    assert rel_rms(fk, e.force) < tol, rel_rms(fk, e.force)
+    assert abs(pe[0] - r.pe) < tol * abs(r.pe)
+    assert abs(pe[1] - e.pe) < tol * abs(e.pe)
+    assert abs(per - r.pe) < tol * abs(r.pe) and abs(pek - e.pe) < tol * abs(e.pe)
+    s_ref = r.stress + e.stress
+    s_gpu = np.triu(np.asarray(st).reshape(3, 3))
+    assert np.abs(s_gpu - np.triu(s_ref)).max() < tol * np.abs(s_ref).max()
+    for got, want in ((str_, r.stress), (stk, e.stress)):
+        assert np.abs(np.triu(got) - np.triu(want)).max() < tol * np.abs(want).max()
+
+
+def test_water_131072_mixed_against_fp64():
     from moldy_gb300 import ForceField, system
     sysm = system.water(nside=32, seed=7)
     ff = ForceField(sysm, precision="fp64")
     f64, pe64, _ = ff.forces()
-    fr64, per64, _ = ff.force_calc()
     ff.set_precision("mixed")
     f32, pe32, _ = ff.forces()
     ff.close()
     assert rel_rms(f32, f64) < 1e-5, rel_rms(f32, f64)
     assert abs(pe32.sum() - pe64.sum()) < 1e-5 * abs(pe64.sum())
-    from oracle import port
-    r = port.force_calc(sysm, nthreads=16)
-    assert rel_rms(fr64, r.force) < 1e-12
-    assert abs(per64 - r.pe) < 1e-12 * abs(r.pe)
