@@ -7,6 +7,7 @@
 // the reference's binning and cut-off decisions require.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "mdgpu_internal.h"
@@ -129,6 +130,61 @@ static mdgpu_status build_stencil(const double *h, double cutoff, int nx, int ny
    return MDGPU_OK;
 }
 
+// The full stencil regrouped by (dx, dy): each run of consecutive dz is one
+// column, so that the cells a column covers around a home cell are
+// consecutive in the link-cell order (cell index cz + nz (cy + ny cx)) and
+// their sites one contiguous range of slots.  Columns in (dx, dy) order;
+// the offset vectors of a column's cells are laid out in dz order.
+static void build_columns(RsGeom &g)
+{
+   std::vector<int4> e(g.full.begin(), g.full.end());
+   std::sort(e.begin(), e.end(), [](const int4 &a, const int4 &b) {
+      return a.x != b.x ? a.x < b.x : a.y != b.y ? a.y < b.y : a.z < b.z;
+   });
+   g.cols.clear();
+   g.col_base.clear();
+   g.coff_hi.clear();
+   g.coff_lo.clear();
+   g.cols_ok = true;
+   bool have[27] = {false};
+   for (size_t i = 0; i < e.size(); i++) {
+      const int4 d = e[i];
+      if (std::abs(d.x) <= 1 && std::abs(d.y) <= 1 && std::abs(d.z) <= 1)
+         have[9 * (d.x + 1) + 3 * (d.y + 1) + (d.z + 1)] = true;
+      const bool extend = !g.cols.empty() && g.cols.back().x == d.x && g.cols.back().y == d.y &&
+                          g.cols.back().z + g.cols.back().w == d.z;
+      if (extend) {
+         g.cols.back().w++;
+      } else {
+         g.cols.push_back(make_int4(d.x, d.y, d.z, 1));
+         g.col_base.push_back((int)g.coff_hi.size());
+      }
+      double v[3];
+      for (int r = 0; r < 3; r++)
+         v[r] = g.h[3 * r] * ((double)d.x / g.nx) + g.h[3 * r + 1] * ((double)d.y / g.ny) +
+                g.h[3 * r + 2] * ((double)d.z / g.nz);
+      float hi[3], lo[3];
+      for (int r = 0; r < 3; r++) {
+         hi[r] = (float)v[r];
+         lo[r] = (float)(v[r] - (double)hi[r]);
+      }
+      g.coff_hi.push_back(make_float4(hi[0], hi[1], hi[2], 0.f));
+      g.coff_lo.push_back(make_float4(lo[0], lo[1], lo[2], 0.f));
+   }
+   for (const int4 &c : g.cols)
+      if (c.w > g.nz) g.cols_ok = false;
+   // cell thickness along each lattice direction: 1 / (n_i |row i of h^-1|)
+   bool thick = true;
+   const int n[3] = {g.nx, g.ny, g.nz};
+   for (int r = 0; r < 3; r++) {
+      const double rn = std::sqrt(g.hinv[3 * r] * g.hinv[3 * r] + g.hinv[3 * r + 1] * g.hinv[3 * r + 1] +
+                                  g.hinv[3 * r + 2] * g.hinv[3 * r + 2]);
+      if (!(1.0 / (n[r] * rn) >= 0.5)) thick = false;
+   }
+   g.nbr27 = thick;
+   for (int k = 0; k < 27; k++) g.nbr27 = g.nbr27 && have[k];
+}
+
 mdgpu_status build_rs_geom(const double *h, const mdgpu_control &ctl, RsGeom &g)
 {
    double subcell = ctl.subcell;
@@ -181,6 +237,7 @@ mdgpu_status build_rs_geom(const double *h, const mdgpu_control &ctl, RsGeom &g)
    }
    g.cut2 = ctl.cutoff * ctl.cutoff;
    g.cut100 = 10000.0 * g.cut2;                               // src/force.c:831-832
+   build_columns(g);
    return MDGPU_OK;
 }
 

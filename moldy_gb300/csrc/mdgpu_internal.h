@@ -34,6 +34,19 @@ struct RsGeom {
    double origin_step[9];          // h / n (column j scaled by 1/n_j)
    double cut2 = 0, cut100 = 0;
    double key[12];                 // h, cutoff, subcell, strict: cache key
+   // The full stencil as columns: offsets of one (dx, dy) with consecutive
+   // dz form one column (dx, dy, dz_min, length); col_base[i] indexes the
+   // column's first entry in coff_hi/coff_lo, which hold the cell-offset
+   // vectors of its dz values in order (FP32 hi + lo parts).  cols_ok: every
+   // column is at most nz long (so it wraps the periodic cell at most once).
+   std::vector<int4> cols;
+   std::vector<int> col_base;
+   std::vector<float4> coff_hi, coff_lo;
+   bool cols_ok = false;
+   // every offset of the 27-cell neighbourhood is in the stencil and each
+   // cell is at least 0.5 A thick (any pair closer than the too-close
+   // distance lies in neighbouring cells)
+   bool nbr27 = false;
 };
 
 // Builds the stencil and cell geometry; returns MDGPU_E_CUTOFF as the
@@ -133,6 +146,16 @@ struct RsDev {
    DBuf<double> part2;     // their first-level sums
    DBuf<unsigned long long> keys;
    DBuf<int4> rdf_full;    // RDF stencil (strict, at the RDF limit)
+   // column walk of the mixed pair kernel (k_pairs_col): the stencil's
+   // columns and their offsets; the slots re-laid class by class (class 0:
+   // the sites that interact with charged sites; class 1: the rest), each
+   // class in link-cell order, with per-class cell starts cs[2][ncells+1]
+   DBuf<int4> cols;
+   DBuf<int> col_base;
+   DBuf<float4> coff_hi, coff_lo;
+   DBuf<int> cls_of_id, cls_pre, cs, sortc, cellc, cls_bsum;
+   DBuf<float4> posc;
+   DBuf<int2> tagc;
    DBuf<unsigned long long> rdf_counts;
    double rdf_key[11] = {0};
    int rdf_nfull = 0;
@@ -304,6 +327,12 @@ struct mdgpu_ctx {
    cudaEvent_t ev_fork = nullptr, ev_pairs = nullptr, ev_join = nullptr;
    bool ev_marked[MDGPU_NPHASES + 1] = {};
    bool have_nabor_note = false;
+   // interaction classes of the site identifiers (realspace.cu): class 0
+   // holds the identifiers that interact with charged sites, class 1 the
+   // rest; pairs across the classes add exactly nothing.  ncls 1 when
+   // every identifier is in class 0.
+   std::vector<int> cls_of_id;
+   int ncls = 1;
    // bumped by every call that changes what a captured step would launch
    // (system, control, parameters, precision, stream, dynamics state)
    uint64_t gen = 1;

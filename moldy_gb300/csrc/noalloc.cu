@@ -51,8 +51,10 @@ constexpr int MAX_SITES = MDGPU_NOALLOC_MAX_SITES;
 constexpr int MAX_KVEC = MDGPU_NOALLOC_MAX_KVEC;
 constexpr int MAX_CHUNKS = 16;
 constexpr int MAX_SPLITS = 4;
-// site ordering grid: at most OG^3 cells, slot offsets held as 16-bit counts
-constexpr int OG = 8;
+// site ordering grid: at most OG^3 cells, counted by ORDER_WARPS warps with
+// 16-bit counts and slot offsets
+constexpr int OG = 16;
+constexpr int ORDER_WARPS = 4;
 static_assert(MAX_SITES <= 65535, "the ordering counts are 16-bit");
 
 constexpr size_t al(size_t x) { return (x + 255) / 256 * 256; }
@@ -216,25 +218,26 @@ k_klist_na(KlArgs a, int4 *__restrict__ item, int *__restrict__ k0, float2 *__re
    }
 }
 
-// Orders the sites by a coarse cell grid (g^3 cells of the fractional
-// co-ordinates, ascending site index inside a cell), one block of 32 warps:
-// a structure-factor chunk is then a compact, nearly neutral region, so its
-// FP32 partial sum stays small even where the whole sum cancels (an ionic
-// crystal listed species by species would otherwise give chunks of a single
-// charge sign).  Warp w owns sites [w S, (w + 1) S): it counts them per
-// cell, one scan over (cell, warp) gives each warp its first slot per cell,
-// and the warp places its sites in order.  sorted[slot] = site.
-__global__ void __launch_bounds__(1024)
+// Orders the sites by a cell grid (g^3 cells of the fractional
+// co-ordinates, about two sites a cell; ascending site index inside a
+// cell), one block of ORDER_WARPS warps: a structure-factor chunk is then a
+// compact, nearly neutral region, so its FP32 partial sum stays small even
+// where the whole sum cancels (an ionic crystal listed species by species
+// would otherwise give chunks of a single charge sign).  Warp w owns sites
+// [w S, (w + 1) S): it counts them per cell, one scan over (cell, warp)
+// gives each warp its first slot per cell, and the warp places its sites in
+// order.  sorted[slot] = site.
+__global__ void __launch_bounds__(ORDER_WARPS * 32)
 k_order_na(int N, const double *__restrict__ site, double hi0, double hi1, double hi2, double hi4,
            double hi5, double hi8, int g, int *__restrict__ key, int *__restrict__ sorted)
 {
-   __shared__ unsigned short tab[OG * OG * OG * 32];   // [cell][warp]: count, then first slot
-   __shared__ int wsum[32];
+   __shared__ unsigned short tab[OG * OG * OG * ORDER_WARPS];   // [cell][warp]: count, then first slot
+   __shared__ int wsum[ORDER_WARPS];
    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-   const int ncell = g * g * g, nt = ncell * 32;
+   const int ncell = g * g * g, nt = ncell * ORDER_WARPS;
    for (int j = threadIdx.x; j < nt; j += blockDim.x) tab[j] = 0;
    __syncthreads();
-   const int S = (N + 31) / 32, s0 = min(N, w * S), s1 = min(N, s0 + S);
+   const int S = (N + ORDER_WARPS - 1) / ORDER_WARPS, s0 = min(N, w * S), s1 = min(N, s0 + S);
    const unsigned int lt = (1u << lane) - 1u;
    for (int b = s0; b < s1; b += 32) {
       const int i = b + lane;
@@ -252,11 +255,11 @@ k_order_na(int N, const double *__restrict__ site, double hi0, double hi1, doubl
          key[i] = kk;
       }
       const unsigned int peers = __match_any_sync(0xffffffffu, kk);
-      if (kk >= 0 && (peers & lt) == 0) tab[kk * 32 + w] += (unsigned short)__popc(peers);
+      if (kk >= 0 && (peers & lt) == 0) tab[kk * ORDER_WARPS + w] += (unsigned short)__popc(peers);
       __syncwarp();
    }
    __syncthreads();
-   // exclusive scan over tab in (cell, warp) order: 1024 threads, a run each
+   // exclusive scan over tab in (cell, warp) order: a run of entries per thread
    const int per = (nt + blockDim.x - 1) / blockDim.x;
    const int j0 = min(nt, (int)threadIdx.x * per), j1 = min(nt, j0 + per);
    int tot = 0;
@@ -268,16 +271,8 @@ k_order_na(int N, const double *__restrict__ site, double hi0, double hi1, doubl
    }
    if (lane == 31) wsum[w] = sc;
    __syncthreads();
-   if (w == 0) {
-      int v = wsum[lane];
-      for (int o = 1; o < 32; o <<= 1) {
-         const int t = __shfl_up_sync(0xffffffffu, v, o);
-         if (lane >= o) v += t;
-      }
-      wsum[lane] = v;
-   }
-   __syncthreads();
-   int run = sc - tot + (w > 0 ? wsum[w - 1] : 0);
+   int run = sc - tot;
+   for (int v = 0; v < w; v++) run += wsum[v];
    for (int j = j0; j < j1; j++) {
       const int cnt = tab[j];
       tab[j] = (unsigned short)run;
@@ -288,9 +283,9 @@ k_order_na(int N, const double *__restrict__ site, double hi0, double hi1, doubl
       const int i = b + lane;
       const int kk = i < s1 ? key[i] : -1;
       const unsigned int peers = __match_any_sync(0xffffffffu, kk);
-      if (kk >= 0) sorted[tab[kk * 32 + w] + __popc(peers & lt)] = i;
+      if (kk >= 0) sorted[tab[kk * ORDER_WARPS + w] + __popc(peers & lt)] = i;
       __syncwarp();
-      if (kk >= 0 && (peers & lt) == 0) tab[kk * 32 + w] += (unsigned short)__popc(peers);
+      if (kk >= 0 && (peers & lt) == 0) tab[kk * ORDER_WARPS + w] += (unsigned short)__popc(peers);
       __syncwarp();
    }
 }
@@ -455,10 +450,10 @@ extern "C" mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, 
    k_klist_na<<<1, 1024, 0, st>>>(ka, item, k0, kxy, kvec, coef, coef2, out);
 
    const int N = nsites;
-   // sites in the order of a coarse cell grid, about 32 sites a cell
-   int g = (int)std::lround(std::cbrt(N / 32.0));
+   // sites in the order of a cell grid, about two sites a cell
+   int g = (int)std::lround(std::cbrt(N / 2.0));
    g = g < 1 ? 1 : (g > OG ? OG : g);
-   k_order_na<<<1, 1024, 0, st>>>(N, d_site, hinv[0], hinv[1], hinv[2], hinv[4], hinv[5], hinv[8], g, key,
+   k_order_na<<<1, ORDER_WARPS * 32, 0, st>>>(N, d_site, hinv[0], hinv[1], hinv[2], hinv[4], hinv[5], hinv[8], g, key,
                                   sorted);
    k_prep<<<(N + 255) / 256, 256, 0, st>>>(N, N, sorted, d_site, d_chg, hinv[0], hinv[1], hinv[2], hinv[3],
                                            hinv[4], hinv[5], hinv[6], hinv[7], hinv[8], 1, ph, z, zp,

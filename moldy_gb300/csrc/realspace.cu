@@ -25,7 +25,9 @@
 // mixed form r is formed in FP32 from cell-relative co-ordinates and an
 // (hi, lo) pair of the exact cell-offset vector; decisions within a narrow
 // band of the threshold are re-made in FP64 from the original co-ordinates.
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -39,6 +41,7 @@ struct RsParams {
    // molecule entities binned by centre of mass in molecular-cutoff mode
    // (the framework's sites are binned one by one, src/force.c:458-470)
    int fw_mol, fw_site0, nmol_ent;
+   int ncols;             // stencil columns (k_pairs_col)
    double hinv[9];
    double h[9];
    double reloc[27][3];
@@ -691,6 +694,310 @@ __global__ void __launch_bounds__(256) k_reduce_rs2(const double *__restrict__ p
    }
 }
 
+// ------------------------------------------------- column walk (mixed form)
+// The pair kernel of the mixed form, k_pairs_col, walks the stencil by
+// columns and over one interaction class at a time.
+//
+// Columns: for a home cell (cx, cy, cz) and a stencil column (dx, dy, dz0,
+// len) the partner cells (cx+dx, cy+dy, cz+dz0 .. cz+dz0+len-1) are
+// consecutive cells of the link-cell order (at most two runs where the
+// column wraps the periodic cell in z), so their sites are one or two
+// contiguous slot ranges: a home site needs about 75 column lookups on the
+// benchmark workload instead of about 485 cell lookups.
+//
+// Classes: identifiers are split into class 0 (those that interact with a
+// charged site, directly or through a potential with nonzero parameters)
+// and class 1 (the rest).  A pair across the classes has no charge product
+// and a potential with all parameters zero, so it adds exactly nothing to
+// forces, energy and virial: each home site walks the sites of its own class
+// only (rigid water: O meets only O, H and M only H and M -- 37.5% of the
+// ordered pairs skipped).  The slots are re-laid class by class, each class
+// in link-cell order, with per-class cell starts.  The pair count still
+// counts every class (the reference's evaluated pairs), and pairs across the
+// classes closer than the too-close distance are reported by k_tooclose_x.
+constexpr int COL_E = 3;                    // stencil columns per lane in one pass
+constexpr int COL_ROWS = 32 * COL_E * 2;    // slot runs per pass (two per column at most)
+constexpr int COL_WIN = 256;                // candidates decoded per window
+
+// per slot (link-cell order): 1 when its identifier is in class 0; the
+// entry after the last is 0 (so the exclusive scan ends with the class-0
+// count)
+__global__ void k_cls_flag(int N, const int2 *__restrict__ tag, const int *__restrict__ cls_of_id,
+                           int *__restrict__ flag)
+{
+   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   if (p < N) flag[p] = cls_of_id[tag[p].x] == 0 ? 1 : 0;
+   else if (p == N) flag[p] = 0;
+}
+
+// Slots re-laid class by class (stable): class 0 first, then class 1, each
+// in link-cell order; per-class cell starts cs[K][c].  pre[p] is the number
+// of class-0 slots before p (pre[N] their total).  The per-slot tag carries
+// the identifier in its low 16 bits and the cell's z index above them.
+__global__ void k_cls_split(RsParams P, const int *__restrict__ pre, const int *__restrict__ cls_of_id,
+                            const int *__restrict__ cell_start, const float4 *__restrict__ pos32,
+                            const int2 *__restrict__ tag, const int *__restrict__ sorted,
+                            const int *__restrict__ slot_cell, int *__restrict__ cs, float4 *__restrict__ posc,
+                            int2 *__restrict__ tagc, int *__restrict__ sortc, int *__restrict__ cellc)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   const int N = P.nsites, n0 = pre[N];
+   if (i < N) {
+      const int2 t = tag[i];
+      const int q = cls_of_id[t.x] == 0 ? pre[i] : n0 + (i - pre[i]);
+      const int c = slot_cell[i];
+      posc[q] = pos32[i];
+      tagc[q] = make_int2(t.x | ((c % P.nz) << 16), t.y);
+      sortc[q] = sorted[i];
+      cellc[q] = c;
+   }
+   if (i <= P.ncells) {
+      const int a = cell_start[i], b = pre[a];
+      cs[i] = b;
+      cs[P.ncells + 1 + i] = n0 + (a - b);
+   }
+}
+
+// One warp per home slot of the class-major layout.  A pass gives each lane
+// COL_E columns (up to two slot runs each, of the home site's class); a warp
+// prefix sum lays the runs end to end; windows of COL_WIN candidates are
+// decoded into shared memory (slot | run << 24) and dealt out 32 at a time.
+// The pair arithmetic is k_pairs's mixed form: FP32 from cell-relative
+// co-ordinates and the exact cell offset as an (hi, lo) pair, decisions near
+// a threshold re-made in FP64, Kahan-free per-lane sums reduced by warp
+// trees.
+template <int PT, bool EW>
+__global__ void __launch_bounds__(PAIR_WARPS * 32, 8)
+k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ cs,
+            const int *__restrict__ pre, const int4 *__restrict__ cols, const int *__restrict__ col_base,
+            const float4 *__restrict__ coff_hi, const float4 *__restrict__ coff_lo,
+            const float4 *__restrict__ posc, const int2 *__restrict__ tagc, const int *__restrict__ cellc,
+            const int *__restrict__ sortc, const double *__restrict__ site, const float *__restrict__ potg,
+            double *__restrict__ force, double *__restrict__ part, DevOut *out)
+{
+   typedef float R;
+   constexpr int NP = NPar<PT>::v;
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   __shared__ int s_inc[PAIR_WARPS][COL_ROWS], s_jb[PAIR_WARPS][COL_ROWS], s_inf[PAIR_WARPS][COL_ROWS];
+   __shared__ int s_cand[PAIR_WARPS][COL_WIN];
+   R *pot_s = reinterpret_cast<R *>(smem_raw);
+   const int npot = P.max_id * P.max_id;
+   if (P.pot_in_smem)
+      for (int q = threadIdx.x; q < npot * NPOTP; q += blockDim.x) pot_s[q] = potg[q];
+   __syncthreads();
+   const R *pot = P.pot_in_smem ? pot_s : potg;
+
+   const int N = P.nsites, n0 = pre[N];
+   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int p = blockIdx.x * PAIR_WARPS + w;   // home slot (class-major)
+   int *inc = s_inc[w], *jbr = s_jb[w], *infr = s_inf[w], *cand = s_cand[w];
+   R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+   long long nall = 0;   // candidates of every class (the reference's evaluated pairs)
+   if (p < N) {
+      const int *csk = cs + (p < n0 ? 0 : P.ncells + 1);
+      const int c = cellc[p];
+      const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
+      const int2 ti = tagc[p];
+      const R *prow = pot + (size_t)(ti.x & 0xffff) * P.max_id * NPOTP;
+      const float4 xi = posc[p];
+      const R qi = xi.w;
+      const R alpha = P.alphaf, norm = P.normf;
+      const int oi = sortc[p];
+      const R cut100 = (R)P.cut100;
+      for (int base = 0; base < P.ncols; base += 32 * COL_E) {
+         int cnt[2 * COL_E], jb[2 * COL_E], inf[2 * COL_E], tot = 0;
+#pragma unroll
+         for (int u = 0; u < COL_E; u++) {
+            cnt[2 * u] = cnt[2 * u + 1] = jb[2 * u] = jb[2 * u + 1] = inf[2 * u] = inf[2 * u + 1] = 0;
+            const int col = base + lane * COL_E + u;
+            if (col < P.ncols) {
+               const int4 cd = __ldg(&cols[col]);
+               const int ob = __ldg(&col_base[col]);
+               int bx = cx + cd.x, by = cy + cd.y;
+               const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
+               const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
+               bx -= ix * P.nx;
+               by -= iy * P.ny;
+               const int cc = P.nz * (by + P.ny * bx);   // the partner column's first cell
+               const int z0 = cz + cd.z, z1 = z0 + cd.w - 1;
+               // at most two runs of consecutive cells, each with one z image
+               int za[2], zb[2], iz[2], ns = 1;
+               if (z1 < 0) { za[0] = z0 + P.nz; zb[0] = z1 + P.nz; iz[0] = -1; }
+               else if (z0 >= P.nz) { za[0] = z0 - P.nz; zb[0] = z1 - P.nz; iz[0] = 1; }
+               else if (z0 < 0) { za[0] = z0 + P.nz; zb[0] = P.nz - 1; iz[0] = -1; za[1] = 0; zb[1] = z1; iz[1] = 0; ns = 2; }
+               else if (z1 >= P.nz) { za[0] = z0; zb[0] = P.nz - 1; iz[0] = 0; za[1] = 0; zb[1] = z1 - P.nz; iz[1] = 1; ns = 2; }
+               else { za[0] = z0; zb[0] = z1; iz[0] = 0; }
+#pragma unroll
+               for (int s = 0; s < 2; s++) {
+                  if (s < ns) {
+                     const int a = __ldg(&csk[cc + za[s]]), b = __ldg(&csk[cc + zb[s] + 1]);
+                     cnt[2 * u + s] = b - a;
+                     jb[2 * u + s] = a;
+                     // offset-table index of a candidate in cell z: z + eb
+                     const int eb = ob - cd.z - cz + iz[s] * P.nz;
+                     inf[2 * u + s] = (eb * 32) | (9 * (ix + 1) + 3 * (iy + 1) + (iz[s] + 1));
+                     nall += __ldg(&cell_start[cc + zb[s] + 1]) - __ldg(&cell_start[cc + za[s]]);
+                  }
+               }
+            }
+#pragma unroll
+            for (int s = 0; s < 2; s++) tot += cnt[2 * u + s];
+         }
+         const int linc = warp_incl_scan(tot);
+         const int T = __shfl_sync(0xffffffffu, linc, 31);
+         int run = linc - tot;
+#pragma unroll
+         for (int r = 0; r < 2 * COL_E; r++) {
+            const int q = lane * 2 * COL_E + r;
+            jbr[q] = jb[r] - run;        // slot = jbr[q] + candidate index
+            run += cnt[r];
+            inc[q] = run;
+            infr[q] = inf[r];
+         }
+         __syncwarp();
+         for (int w0 = 0; w0 < T; w0 += COL_WIN) {
+            const int w1 = min(T, w0 + COL_WIN);
+            // decode this lane's runs that fall in [w0, w1)
+#pragma unroll
+            for (int r = 0; r < 2 * COL_E; r++) {
+               const int q = lane * 2 * COL_E + r;
+               const int e1 = inc[q], e0 = e1 - cnt[r];
+               const int a = max(e0, w0), b = min(e1, w1);
+               const int jq = jbr[q];
+               for (int t = a; t < b; t++) cand[t - w0] = (jq + t) | (q << 24);
+            }
+            __syncwarp();
+            for (int r0 = w0; r0 < w1; r0 += 32) {
+               const int idx = r0 + lane;
+               if (idx < w1) {
+                  const int v = cand[idx - w0];
+                  const int j = v & 0xffffff, q = (unsigned)v >> 24;
+                  const int inf_q = infr[q];
+                  const int kimg = inf_q & 31;
+                  if (j != p || kimg != 13) {
+                     const int2 tj = __ldg(&tagc[j]);
+                     const int e = (tj.x >> 16) + (inf_q >> 5);
+                     const float4 xj = __ldg(&posc[j]);
+                     const float4 h4 = __ldg(&coff_hi[e]), l4 = __ldg(&coff_lo[e]);
+                     const R rx = (h4.x + (xj.x - xi.x)) + l4.x;
+                     const R ry = (h4.y + (xj.y - xi.y)) + l4.y;
+                     const R rz = (h4.z + (xj.z - xi.z)) + l4.z;
+                     R r2 = rx * rx + ry * ry + rz * rz;
+                     const bool intra = ti.y == tj.y;
+                     bool too_close, clip;
+                     pair_flags<true>(P, r2, oi, j, kimg, sortc, site, too_close, clip);
+                     if (too_close && !intra) {
+                        const int oj = sortc[j];
+                        if (oi < oj) note_too_close(out, oi, oj);
+                     }
+                     const R r2a = r2;
+                     if (clip) r2 = cut100;
+                     R pp[NP];
+                     const R *pj = prow + (size_t)(tj.x & 0xffff) * NPOTP;
+#pragma unroll
+                     for (int k = 0; k < NP; k++) pp[k] = pj[k];
+                     R f, u;
+                     pair_fu<PT, EW, R>(r2, xj.w * qi, pp, alpha, norm, f, u);
+                     if (intra) {
+                        // as in k_pairs: an intramolecular pair's energy is
+                        // what the intramolecular correction subtracts again
+                        R fa, ua = R(0);
+                        if (clip) pair_fu<PT, EW, R>(r2a, xj.w * qi, pp, alpha, norm, fa, ua);
+                        u = clip ? u - ua : R(0);
+                     }
+                     const R hf = R(0.5) * f;
+                     fx -= f * rx;
+                     fy -= f * ry;
+                     fz -= f * rz;
+                     pe += R(0.5) * u;
+                     v0 += hf * rx * rx;
+                     v1 += hf * rx * ry;
+                     v2 += hf * rx * rz;
+                     v3 += hf * ry * ry;
+                     v4 += hf * ry * rz;
+                     v5 += hf * rz * rz;
+                  }
+               }
+            }
+            __syncwarp();
+         }
+      }
+      R Fx = fx, Fy = fy, Fz = fz;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+         Fx += __shfl_down_sync(0xffffffffu, Fx, o);
+         Fy += __shfl_down_sync(0xffffffffu, Fy, o);
+         Fz += __shfl_down_sync(0xffffffffu, Fz, o);
+      }
+      if (lane == 0) {
+         force[oi] = (double)Fx;
+         force[N + oi] = (double)Fy;
+         force[2 * N + oi] = (double)Fz;
+         nall -= 1;   // the home site itself
+      }
+   }
+   __shared__ R wred[7][PAIR_WARPS];
+   R vv[7] = {pe, v0, v1, v2, v3, v4, v5};
+#pragma unroll
+   for (int k = 0; k < 7; k++) {
+      R s = vv[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) wred[k][w] = s;
+   }
+   __syncthreads();
+   if (threadIdx.x < 7) {
+      double s = 0.0;
+      for (int q = 0; q < PAIR_WARPS; q++) s += (double)wred[threadIdx.x][q];
+      part[blockIdx.x * 8 + threadIdx.x] = s;
+   }
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) nall += __shfl_down_sync(0xffffffffu, nall, o);
+   if (lane == 0 && nall) atomicAdd((unsigned long long *)&out->npairs2, (unsigned long long)nall);
+}
+
+// Pairs across the interaction classes that come closer than the too-close
+// distance (the reference warns of every evaluated pair with r^2 < 0.25,
+// src/force.c:943-948, whatever its potential): such a pair lies in the
+// 27-cell neighbourhood (cells at least 0.5 A thick), so each site checks
+// the other class's sites there in FP64, with the reference's operation
+// order and the image of the cell offset.  Reported once per pair (from
+// the lower site index), intramolecular pairs excepted, as k_pairs does.
+__global__ void k_tooclose_x(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ slot_cell,
+                             const int2 *__restrict__ tag, const int *__restrict__ cls_of_id,
+                             const int *__restrict__ sorted, const double *__restrict__ site, DevOut *out)
+{
+   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   const int N = P.nsites;
+   if (p >= N) return;
+   const int c = slot_cell[p];
+   const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
+   const int2 ti = tag[p];
+   const int ki = cls_of_id[ti.x], oi = sorted[p];
+   const double xi = site[oi], yi = site[N + oi], zi = site[2 * (size_t)N + oi];
+   for (int d = 0; d < 27; d++) {
+      int bx = cx + d / 9 - 1, by = cy + (d / 3) % 3 - 1, bz = cz + d % 3 - 1;
+      const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
+      const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
+      const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
+      bx -= ix * P.nx;
+      by -= iy * P.ny;
+      bz -= iz * P.nz;
+      const int cb = bz + P.nz * (by + P.ny * bx);
+      const double *rl = P.reloc[9 * (ix + 1) + 3 * (iy + 1) + (iz + 1)];
+      for (int j = cell_start[cb]; j < cell_start[cb + 1]; j++) {
+         const int2 tj = tag[j];
+         const int oj = sorted[j];
+         if (cls_of_id[tj.x] == ki || tj.y == ti.y || oj <= oi) continue;
+         const double ax = __dadd_rn(__dsub_rn(site[oj], xi), rl[0]);
+         const double ay = __dadd_rn(__dsub_rn(site[N + oj], yi), rl[1]);
+         const double az = __dadd_rn(__dsub_rn(site[2 * (size_t)N + oj], zi), rl[2]);
+         const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az));
+         if (d2 < TOO_CLOSE) note_too_close(out, oi, oj);
+      }
+   }
+}
+
 // ----------------------------------------------------------------- adjoint
 // Derivatives of one pair evaluation of pair_fu (f = -U'(r)/r, U) with
 // respect to the potential parameters and the Ewald terms:
@@ -1018,6 +1325,7 @@ static RsParams make_params(mdgpu_ctx *c)
    P.nent = c->ctl.molpbc ? c->nmols_nf + (c->nsites - c->fw_site0) : c->nsites;
    P.nx = g.nx; P.ny = g.ny; P.nz = g.nz; P.ncells = g.ncells;
    P.nfull = (int)g.full.size();
+   P.ncols = (int)g.cols.size();
    P.max_id = c->max_id;
    P.molpbc = c->ctl.molpbc;
    P.strict = c->ctl.strict_cutoff;
@@ -1065,6 +1373,48 @@ mdgpu_status rs_prepare(mdgpu_ctx *c)
       for (size_t i = 0; i < np; i++) p32[i] = (float)c->potpar[i];
       CK(cudaMemcpyAsync(d.pot64.p, c->potpar.data(), np * sizeof(double), cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(d.pot32.p, p32.data(), np * sizeof(float), cudaMemcpyHostToDevice, st));
+      // interaction classes: identifiers joined when they interact (both
+      // charged, or a potential with a nonzero parameter either way); the
+      // group holding the charged identifiers (else the most populous) is
+      // class 0, every other group class 1
+      {
+         const int M = c->max_id, npar = pot_nparams(c->ptype);
+         std::vector<int> grp(M), pop(M, 0);
+         std::vector<char> charged(M, 0);
+         for (int i = 0; i < N; i++) {
+            pop[c->site_id[i]]++;
+            if (c->chg[i] != 0.0) charged[c->site_id[i]] = 1;
+         }
+         for (int a = 0; a < M; a++) grp[a] = a;
+         auto root = [&](int a) { while (grp[a] != a) a = grp[a] = grp[grp[a]]; return a; };
+         for (int a = 0; a < M; a++)
+            for (int b = 0; b < M; b++) {
+               bool link = charged[a] && charged[b];
+               for (int k = 0; k < npar && !link; k++)
+                  link = c->potpar[((size_t)a * M + b) * NPOTP + k] != 0.0;
+               if (link) grp[root(a)] = root(b);
+            }
+         int g0 = -1, best = -1;
+         std::vector<int> gpop(M, 0);
+         for (int a = 0; a < M; a++) gpop[root(a)] += pop[a];
+         for (int a = 0; a < M; a++)
+            if (charged[a]) g0 = root(a);
+         if (g0 < 0)
+            for (int a = 0; a < M; a++)
+               if (gpop[root(a)] > best) best = gpop[g0 = root(a)];
+         c->cls_of_id.assign(2 * (size_t)M, 0);   // second half: every identifier in class 0
+         c->ncls = 1;
+         for (int a = 0; a < M; a++)
+            if (pop[a] > 0 && root(a) != g0) {
+               c->cls_of_id[a] = 1;
+               c->ncls = 2;
+            }
+         for (int a = 0; a < M; a++)
+            if (pop[a] == 0) c->cls_of_id[a] = 0;
+         CK(d.cls_of_id.ensure(2 * (size_t)M));
+         CK(cudaMemcpyAsync(d.cls_of_id.p, c->cls_of_id.data(), 2 * (size_t)M * sizeof(int),
+                            cudaMemcpyHostToDevice, st));
+      }
       CK(cudaStreamSynchronize(st));
       CK(d.cell_of.ensure(N));
       CK(d.sorted.ensure(N));
@@ -1083,11 +1433,28 @@ mdgpu_status rs_prepare(mdgpu_ctx *c)
       CK(cudaMemcpyAsync(d.full.p, g.full.data(), g.full.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(d.off_hi.p, g.off_hi.data(), g.off_hi.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(d.off_lo.p, g.off_lo.data(), g.off_lo.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+      CK(d.cols.ensure(g.cols.size()));
+      CK(d.col_base.ensure(g.col_base.size()));
+      CK(d.coff_hi.ensure(g.coff_hi.size()));
+      CK(d.coff_lo.ensure(g.coff_lo.size()));
+      CK(cudaMemcpyAsync(d.cols.p, g.cols.data(), g.cols.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.col_base.p, g.col_base.data(), g.col_base.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.coff_hi.p, g.coff_hi.data(), g.coff_hi.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.coff_lo.p, g.coff_lo.data(), g.coff_lo.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+      CK(d.cs.ensure(2 * ((size_t)g.ncells + 1)));
       CK(cudaStreamSynchronize(st));
       c->rs_uploaded = true;
    }
    const int nb = (N + PAIR_WARPS - 1) / PAIR_WARPS;
    CK(d.part.ensure((size_t)nb * 8));
+   if (c->sys_dirty) {
+      CK(d.cls_pre.ensure((size_t)N + 1));
+      CK(d.cls_bsum.ensure(((size_t)N + 1 + 1023) / 1024 + 2));
+      CK(d.sortc.ensure(N));
+      CK(d.cellc.ensure(N));
+      CK(d.posc.ensure(N));
+      CK(d.tagc.ensure(N));
+   }
    return MDGPU_OK;
 }
 
@@ -1263,6 +1630,77 @@ mdgpu_status rs_launch(mdgpu_ctx *c, const double *d_site, const double *d_cofm,
 #undef CK
 }
 
+// The column walk serves the mixed form without a framework molecule or
+// molecular cut-off, where every stencil column wraps the cell at most once.
+static bool col_walk_ok(const mdgpu_ctx *c)
+{
+   static const bool off = [] {
+      const char *e = std::getenv("MDGPU_PAIRS_COLUMNS");
+      return e && e[0] == '0';
+   }();
+   return !off && c->rs.cols_ok && c->fw_mol < 0 && !c->ctl.molpbc && c->nsites < (1 << 24) &&
+          c->max_id < (1 << 16) && c->rs.cols.size() > 0;
+}
+
+template <int PT, bool EW>
+static cudaError_t launch_col_t(const RsParams &P, mdgpu_ctx *c, double *force, size_t smem)
+{
+   RsDev &d = c->rd;
+   const int nb = (P.nsites + PAIR_WARPS - 1) / PAIR_WARPS;
+   auto kfn = k_pairs_col<PT, EW>;
+   if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+   }
+   kfn<<<nb, PAIR_WARPS * 32, smem, c->stream>>>(P, d.cell_start.p, d.cs.p, d.cls_pre.p, d.cols.p, d.col_base.p,
+                                                 d.coff_hi.p, d.coff_lo.p, d.posc.p, d.tagc.p, d.cellc.p,
+                                                 d.sortc.p, c->cur_site, d.pot32.p, force, d.part.p, c->out.p);
+   return cudaGetLastError();
+}
+
+// Class split of the binned slots, the column-walk pair kernel and, with
+// two classes, the too-close scan across them.
+static mdgpu_status rs_pairs_col(mdgpu_ctx *c, const RsParams &P, double *d_force, bool ew, size_t smem)
+{
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+   RsDev &d = c->rd;
+   cudaStream_t st = c->stream;
+   const int N = c->nsites, M = c->max_id;
+   const bool two = c->ncls == 2 && c->rs.nbr27;
+   const int *cls = d.cls_of_id.p + (two ? 0 : M);
+   const int n1 = N + 1, nbs = (n1 + 1023) / 1024;
+   k_cls_flag<<<(n1 + 255) / 256, 256, 0, st>>>(N, d.tag.p, cls, d.cls_pre.p);
+   k_scan_blocks<<<nbs, 1024, 0, st>>>(d.cls_pre.p, d.cls_pre.p, d.cls_bsum.p, n1);
+   k_scan_sums<<<1, 1024, 0, st>>>(d.cls_bsum.p, nbs, d.cls_bsum.p + nbs);
+   k_scan_add<<<nbs, 1024, 0, st>>>(d.cls_pre.p, d.cls_bsum.p, n1);
+   const int nsplit = std::max(N, P.ncells + 1);
+   k_cls_split<<<(nsplit + 255) / 256, 256, 0, st>>>(P, d.cls_pre.p, cls, d.cell_start.p, d.pos32.p, d.tag.p,
+                                                    d.sorted.p, d.slot_cell.p, d.cs.p, d.posc.p, d.tagc.p,
+                                                    d.sortc.p, d.cellc.p);
+   CK(cudaGetLastError());
+   c->launches += 5;
+   cudaError_t e;
+   switch (c->ptype) {
+   case 0: e = ew ? launch_col_t<0, true>(P, c, d_force, smem) : launch_col_t<0, false>(P, c, d_force, smem); break;
+   case 1: e = ew ? launch_col_t<1, true>(P, c, d_force, smem) : launch_col_t<1, false>(P, c, d_force, smem); break;
+   case 2: e = ew ? launch_col_t<2, true>(P, c, d_force, smem) : launch_col_t<2, false>(P, c, d_force, smem); break;
+   case 3: e = ew ? launch_col_t<3, true>(P, c, d_force, smem) : launch_col_t<3, false>(P, c, d_force, smem); break;
+   case 4: e = ew ? launch_col_t<4, true>(P, c, d_force, smem) : launch_col_t<4, false>(P, c, d_force, smem); break;
+   case 6: e = ew ? launch_col_t<6, true>(P, c, d_force, smem) : launch_col_t<6, false>(P, c, d_force, smem); break;
+   default: return fail(c, MDGPU_E_PTYPE, "KERNEL called with unknown potential type");
+   }
+   CK(e);
+   c->launches += 1;
+   if (two) {
+      k_tooclose_x<<<(N + 255) / 256, 256, 0, st>>>(P, d.cell_start.p, d.slot_cell.p, d.tag.p, d.cls_of_id.p,
+                                                    d.sorted.p, c->cur_site, c->out.p);
+      CK(cudaGetLastError());
+      c->launches += 1;
+   }
+   return MDGPU_OK;
+#undef CK
+}
+
 mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys, int64_t key_cap)
 {
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
@@ -1278,6 +1716,10 @@ mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys,
    const bool ew = c->ctl.alpha > 0.0;
    const int mode = d_keys ? 1 : 0;
    cudaError_t e;
+   if (mode == 0 && mixed && col_walk_ok(c)) {
+      const mdgpu_status s = rs_pairs_col(c, P, d_force, ew, smem);
+      if (s != MDGPU_OK) return s;
+   } else {
    switch (c->ptype) {
    case 0: e = launch_pairs_pt<0>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
    case 1: e = launch_pairs_pt<1>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
@@ -1289,6 +1731,7 @@ mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys,
    }
    CK(e);
    c->launches += 1;
+   }
    if (mode == 0) {
       CK(d.part2.ensure(8 * RS_RED));
       k_reduce_rs<<<RS_RED, 256, 0, st>>>(d.part.p, (N + PAIR_WARPS - 1) / PAIR_WARPS, d.part2.p);

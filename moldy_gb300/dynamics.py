@@ -177,3 +177,36 @@ def drift_per_ns(energies: np.ndarray, step_ps: float, nmols: Optional[int] = No
     slope = float(np.polyfit(t, H, 1)[0]) if len(H) > 1 else 0.0
     return slope / nmols if nmols else slope
 
+
+
+def restart_state(data: bytes, nspecies: int, nmols: int, nmols_r: int) -> MDState:
+    """The dynamic state held in a restart file the reference wrote in its
+    native format, to start GPU dynamics from (mdgpu_md_init/set_state).
+
+    The file is a sequence of records, each an unsigned long byte count
+    (8 bytes, little-endian on LP64 hosts) followed by that many bytes
+    (cwrite, src/restart.c:183-191).  write_restart (src/restart.c:435-548)
+    writes the header, the control record, the system record, the species
+    records, then per species the principal-frame sites and site ids, the
+    site table and the potential table, and then the dynamic variables:
+    c_of_m, mom, momp, and with rotating molecules quat, amom, amomp."""
+    recs, o = [], 0
+    while o + 8 <= len(data):
+        n = int.from_bytes(data[o:o + 8], "little")
+        recs.append((o + 8, n))
+        o += 8 + n
+    first = 3 + 1 + 2 * nspecies + 2          # header, control, system, species, per-species pairs, sites, pots
+
+    def arr(k, shape):
+        off, n = recs[first + k]
+        want = 8 * int(np.prod(shape))
+        if n != want:
+            raise ValueError(f"restart record {first + k}: {n} bytes, expected {want}")
+        return np.frombuffer(data, "<f8", count=want // 8, offset=off).reshape(shape).copy()
+
+    cm, mo = arr(0, (nmols, 3)), arr(1, (nmols, 3))
+    if nmols_r > 0:
+        qu, am = arr(3, (nmols_r, 4)), arr(4, (nmols_r, 4))
+    else:
+        qu, am = np.zeros((0, 4)), np.zeros((0, 4))
+    return MDState(cm, mo, qu, am)

@@ -39,13 +39,15 @@ def write_mdstate(path: str, sysm, dyn, state, nsteps: int) -> None:
             f.write(np.ascontiguousarray(a, "<f8").tobytes())
 
 
-def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None):
+def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_out=None, restart_in=None):
     """(records [nsteps, 3] = (H_0, pe[0], pe[1]) per step, final MDState,
     seconds per step).  The reference prints its notes to stdout.
 
     dump = (name, level, interval, ndumps, title) has the reference write
     its dump files (from step 1); they are returned as a fourth item,
-    {file name: bytes}."""
+    {file name: bytes}.  restart_out: path the reference's write_restart
+    saves the final state to; restart_in: a restart file whose dynamic
+    state, read back by the reference's own reader, replaces `state`."""
     from moldy_gb300.dynamics import MDState
     exe = os.path.join(REF, "moldy_ref_md_fast" if fast else "moldy_ref_md")
     if not os.path.exists(exe):
@@ -55,7 +57,12 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None):
         pin, pout = os.path.join(d, "in.mdstate"), os.path.join(d, "out.bin")
         write_mdstate(pin, sysm, dyn, state, nsteps)
         args = [exe, pin, pout] + ([str(x) for x in dump] if dump else [])
-        subprocess.run(args, check=True, cwd=d, stdout=subprocess.DEVNULL)
+        env = dict(os.environ)
+        if restart_out:
+            env["MOLDY_REF_RESTART_OUT"] = os.path.abspath(restart_out)
+        if restart_in:
+            env["MOLDY_REF_RESTART_IN"] = os.path.abspath(restart_in)
+        subprocess.run(args, check=True, cwd=d, stdout=subprocess.DEVNULL, env=env)
         raw = np.fromfile(pout, "<f8")
         files = {}
         if dump:

@@ -26,6 +26,15 @@
  *   f64    c_of_m[nmols][3] mom[nmols][3] quat[nmols_r][4] amom[nmols_r][4]
  * out.bin: f64 per step (H_0, pe[0], pe[1]); then c_of_m, mom, quat, amom;
  *   then f64 seconds per step.
+ *
+ * Restart files (the reference's own writer and reader, src/restart.c):
+ *   MOLDY_REF_RESTART_OUT=path  after the run, write_restart (native
+ *     format, src/restart.c:435-548) saves the whole state to path;
+ *   MOLDY_REF_RESTART_IN=path   before the run, the dynamic state (centres
+ *     of mass, momenta, quaternions, angular momenta) is taken from the
+ *     restart file at path instead, read back by the reference's start-up
+ *     sequence: re_re_header, re_re_sysdef, allocate_dynamics,
+ *     init_averages, read_restart (src/startup.c:1001-1023).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -40,6 +49,12 @@ int ithread = 0, nthreads = 1;
 
 void do_step(system_mt *, spec_mt *, site_mt *, pot_mt *, vec_mt (*)[2], double *, real *, mat_mt,
              restrt_mt *, int, int);
+void write_restart(char *, restrt_mt *, system_mp, spec_mp, site_mp, pot_mp);
+void re_re_header(FILE *, restrt_mt *, contr_mt *);
+void re_re_sysdef(FILE *, char *, system_mp, spec_mp *, site_mp *, pot_mp *);
+void allocate_dynamics(system_mp, spec_mt *);
+void init_averages(int, char *, long int, long int, int *);
+void read_restart(FILE *, char *, system_mp, int);
 
 static void rd(void *p, size_t sz, size_t n, FILE *f)
 {
@@ -161,6 +176,39 @@ int main(int argc, char **argv)
          sp->dipole = sp->rdof > 0 ? sqrt(dip[0] * dip[0] + dip[1] * dip[1] + dip[2] * dip[2]) : 0.0;
       }
    }
+   control.roll_interval = 10;
+   if (getenv("MOLDY_REF_RESTART_IN")) {
+      const char *rin = getenv("MOLDY_REF_RESTART_IN");
+      FILE *rf = fopen(rin, "rb");
+      restrt_mt rhdr;
+      contr_mt rctl;
+      system_mt rsys;
+      spec_mp rspec;
+      site_mp rsite;
+      pot_mp rpot;
+      int avc = 0;
+      if (!rf) { perror(rin); return 2; }
+      memset(&rsys, 0, sizeof rsys);
+      re_re_header(rf, &rhdr, &rctl);
+      re_re_sysdef(rf, rhdr.vsn, &rsys, &rspec, &rsite, &rpot);
+      allocate_dynamics(&rsys, rspec);
+      init_averages(rsys.nspecies, rhdr.vsn, rctl.roll_interval, rctl.roll_interval, &avc);
+      read_restart(rf, rhdr.vsn, &rsys, avc);
+      fclose(rf);
+      if (rsys.nmols != sys.nmols || rsys.nmols_r != sys.nmols_r) {
+         fprintf(stderr, "ref_md: restart file does not match the system\n");
+         return 2;
+      }
+      memcpy(sys.c_of_m, rsys.c_of_m, sizeof(vec_mt) * sys.nmols);
+      memcpy(sys.mom, rsys.mom, sizeof(vec_mt) * sys.nmols);
+      if (nq) {
+         memcpy(sys.quat, rsys.quat, sizeof(quat_mt) * nq);
+         memcpy(sys.amom, rsys.amom, sizeof(quat_mt) * nq);
+      }
+   } else if (getenv("MOLDY_REF_RESTART_OUT")) {
+      int avc = 0;
+      init_averages(sys.nspecies, (char *)0, control.roll_interval, control.roll_interval, &avc);
+   }
    msq = (vec_mt(*)[2])calloc(sys.nspecies, sizeof(vec_mt[2]));
    o = fopen(argv[2], "wb");
    if (!o) { perror(argv[2]); return 2; }
@@ -172,6 +220,12 @@ int main(int argc, char **argv)
       fwrite(rec, 8, 3, o);
    }
    clock_gettime(CLOCK_MONOTONIC, &t1);
+   if (getenv("MOLDY_REF_RESTART_OUT")) {
+      char *rout = getenv("MOLDY_REF_RESTART_OUT");
+      snprintf(control.temp_file, sizeof control.temp_file, "%s.tmp", rout);
+      strncpy(control.backup_file, "none", sizeof control.backup_file);
+      write_restart(rout, &rh, &sys, species, site_info, potpar);
+   }
    fwrite(sys.c_of_m, 8, 3 * (size_t)sys.nmols, o);
    fwrite(sys.mom, 8, 3 * (size_t)sys.nmols, o);
    if (nq) {

@@ -16,7 +16,13 @@ The framework fixture (md_waterwall) holds rigid water over a fixed,
 charged framework molecule: the reference zeroes the framework's momentum
 after each step's kicks (src/accel.c:748-755).
 
-usage: python tests/golden/make_md_golden.py [--skip-drift] [--only NAME | --only drift-extra]
+The restart fixture (md_restart_water864) holds a restart file the
+reference's write_restart saved after 10 steps from the thermal start, the
+state those steps reached, and the reference's next 10 steps from that file
+as its own reader (re_re_header, re_re_sysdef, read_restart) reads it back.
+
+usage: python tests/golden/make_md_golden.py [--skip-drift] [--only NAME | --only drift-extra |
+                                                --only drift-more]
 """
 import os
 import subprocess
@@ -52,12 +58,31 @@ def save(name, sysm, dyn, st, rec, fin, sec, temp, seed, **extra):
     print(name, sysm.nsites, "sites", len(rec), "steps", "%.3g s/step" % sec)
 
 
+def _drift_more(job):
+    strict, tag, seed = job
+    w2 = S.water(nside=8, seed=11)
+    s = dataclasses.replace(w2, control=dataclasses.replace(w2.control, strict_cutoff=strict))
+    dyn, st, rec, fin, sec = case(s, 0.001, 300.0, seed, 10000)
+    save("md_drift_water2048" + ("_strict" if strict else "") + "_" + tag, s, dyn, st, rec[::10], fin, sec, 300.0,
+         seed, rec_stride=10)
+
+
 def main():
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     ww = S.water_on_framework()
     if only in (None, "md_waterwall"):
         save("md_waterwall", ww, *case(ww, 0.001, 300.0, 9, 30), 300.0, 9)
+    if only == "drift-more":
+        # five more thermal starts of each water drift run, kept every 10th
+        # step (the drift is a least-squares slope over the whole run), so
+        # that each mean is taken over eight starts
+        import multiprocessing as mp
+        jobs = [(strict, tag, seed) for strict in (False, True)
+                for tag, seed in (("d", 42), ("e", 52), ("f", 62), ("g", 72), ("h", 82))]
+        with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+            pool.map(_drift_more, jobs)
+        return
     if only == "drift-extra":
         # two more independent thermal starts of each drift run: the drift of
         # a 10^4-step run is a noisy quantity, compared as a mean over starts
@@ -69,6 +94,21 @@ def main():
                 save("md_drift_water2048" + ("_strict" if strict else "") + "_" + tag, s, dyn, st, rec, fin, sec,
                      300.0, seed)
         return
+    if only in (None, "md_restart_water864"):
+        # the reference's restart file after 10 steps (its own
+        # write_restart) and its continuation read back from that file
+        import tempfile
+        w = S.water(nside=6, seed=3)
+        dyn = species_dynamics(w, 0.001)
+        st = thermal_state(w, dyn, 300.0, 14)
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "water.rst")
+            rec1, fin1, sec = md.run(w, dyn, st, 10, restart_out=path)
+            rec2, fin2, _ = md.run(w, dyn, st, 10, restart_in=path)
+            with open(path, "rb") as f:
+                rst = np.frombuffer(f.read(), np.uint8)
+        save("md_restart_water864", w, dyn, st, rec2, fin2, sec, 300.0, 14, restart_file=rst, ref_rec_before=rec1,
+             c_of_m_restart=fin1.c_of_m, mom_restart=fin1.mom, quat_restart=fin1.quat, amom_restart=fin1.amom)
     if only is not None:
         return
     w = S.water(nside=6, seed=3)

@@ -139,3 +139,79 @@ def test_template_rules(tmp_path):
     with DumpWriter(str(tmp_path / "plain"), sp, 1, 1, 2, 0.01, 2, 0) as w:
         with pytest.raises(MdgpuError, match="exists"):
             w.append(np.zeros(w.size, np.float32))
+
+
+def _xdr_expected(title, istep, interval, level, maxdumps, records, timestamp, dump_init, rts, deltat,
+                  nmols, nmols_r, species):
+    """A dump file as the XDR standard (RFC 4506: big-endian 4-byte units,
+    fixed-length opaque data padded to a multiple of 4) encodes the
+    reference's XDR routines' field order, written here from those rules
+    alone: xdr_dump (src/xdr.c:150-157) -- opaque title and version (128 +
+    16 bytes), xdr_long istep and dump_interval, xdr_int dump_level,
+    maxdumps, ndumps, dump_size, xdr_u_long timestamp, dump_init,
+    restart_timestamp, sysinfo_size; xdr_dump_sysinfo_2_23
+    (src/xdr.c:168-182) -- xdr_float deltat, xdr_int nmols, nmols_r,
+    nspecies, per species xdr_float inertia[3], mass, dipole, charge, xdr_int
+    nmols, rdof, framework, opaque name (32 bytes); then each record as
+    dump_size xdr_floats (src/dump.c:263-264)."""
+    import struct
+
+    def opaque(b, n):
+        b = b[:n] + b"\0" * (n - len(b[:n]))
+        return b + b"\0" * (-n % 4)
+    nd, size = records.shape
+    out = opaque(title.encode(), 128) + opaque(b"2.27(XDR)", 16)
+    out += struct.pack(">ll", istep, interval)
+    out += struct.pack(">iiii", level, maxdumps, nd, size)
+    out += struct.pack(">LLLL", timestamp, dump_init, rts, 16 + 68 * len(species))
+    out += struct.pack(">fiii", deltat, nmols, nmols_r, len(species))
+    for s in species:
+        out += struct.pack(">ffffff", *s["inertia"], s["mass"], s["dipole"], s["charge"])
+        out += struct.pack(">iii", s["nmols"], s["rdof"], s["framework"])
+        out += opaque(s["name"].encode(), 32)
+    for r in records:
+        out += struct.pack(">%df" % size, *[float(v) for v in r])
+    return out
+
+
+def test_xdr_bytes_follow_rfc4506(tmp_path):
+    """The XDR dump file, byte for byte, against an encoder written from the
+    XDR standard and the reference's field order (the reference's own XDR
+    build needs a system rpc/xdr.h, absent here, so its files cannot be
+    made): only the wall-clock stamp is taken from the file."""
+    import struct
+
+    from moldy_gb300.dumpfile import DumpWriter, species_info
+    z, files = _fixture("dump_water864")
+    sysm, dyn = _md(str(z["md_fixture"]))
+    ref = _read(tmp_path, "ref.dmp", files["run00.dmp"])
+    sp = species_info(sysm, dyn)
+    with DumpWriter(str(tmp_path / "x%d.xdr"), sp, ref.dump_level, ref.dump_interval, 8, dyn.step,
+                    ref.nmols, ref.nmols_r, istep=3, title="rfc4506 check", xdr=True, dump_init=424242,
+                    restart_timestamp=99) as w:
+        for rec in ref.records:
+            w.append(rec)
+    got = (tmp_path / "x0.xdr").read_bytes()
+    stamp = struct.unpack_from(">L", got, 168)[0]
+    spf = [dict(s, inertia=[float(np.float32(v)) for v in s["inertia"]]) for s in sp]
+    for s in spf:
+        for k in ("mass", "dipole", "charge"):
+            s[k] = float(np.float32(s[k]))
+    want = _xdr_expected("rfc4506 check", 3, ref.dump_interval, ref.dump_level, 8, ref.records, stamp,
+                         424242, 99, float(np.float32(dyn.step * ref.dump_interval)), ref.nmols, ref.nmols_r, spf)
+    assert len(got) == len(want)
+    bad = [i for i in range(len(got)) if got[i] != want[i]]
+    assert not bad, f"bytes differ at {bad[:10]}"
+
+
+def test_restart_state_reads_the_reference_restart_file():
+    """moldy_gb300.dynamics.restart_state takes the dynamic state out of a
+    restart file the reference's write_restart produced (native format):
+    bit for bit the state the reference's run reached."""
+    from moldy_gb300 import system
+    from moldy_gb300.dynamics import restart_state
+    sysm, z = system.load_npz(os.path.join(GOLDEN, "md_restart_water864.npz"))
+    st = restart_state(z["restart_file"].tobytes(), len(sysm.species), sysm.nmols, len(z["quat0"]))
+    for got, key in ((st.c_of_m, "c_of_m_restart"), (st.mom, "mom_restart"), (st.quat, "quat_restart"),
+                     (st.amom, "amom_restart")):
+        np.testing.assert_array_equal(got, z[key])

@@ -71,6 +71,38 @@ def test_mixed_dynamics_follows_reference(name):
     assert np.max(np.abs(d)) < 1e-6
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 2e-5)])
+def test_continues_from_the_reference_restart_file(prec, tol):
+    """A restart file the reference's own write_restart saved after 10
+    steps (src/restart.c:435-548) starts the GPU dynamics (the state read by
+    moldy_gb300.dynamics.restart_state, handed over by mdgpu_md_init); the
+    next 10 GPU steps follow the reference's continuation from the same file
+    (its own reader, src/restart.c:357-433), and the GPU's own first 10
+    steps from the thermal start reach the state the file holds."""
+    from moldy_gb300 import ForceField
+    from moldy_gb300.dynamics import MDState, MolecularDynamics, restart_state
+    sysm, dyn, st0, st1, z = _load("md_restart_water864")
+    nq = len(z["quat0"])
+    st_r = restart_state(z["restart_file"].tobytes(), len(sysm.species), sysm.nmols, nq)
+    rec = z["ref_rec"]
+    ff = ForceField(sysm, precision=prec)
+    try:
+        e = MolecularDynamics(ff, dyn, st_r).run(len(rec))
+        first = MolecularDynamics(ff, dyn, st0)
+        first.run(len(z["ref_rec_before"]))
+        reached = first.state()
+    finally:
+        ff.close()
+    scale = np.abs(e[:, 0]) + np.abs(e[:, 1]) + e[:, 2] + e[:, 3]
+    assert np.all(np.abs(e.sum(1) - rec[:, 0]) <= tol * scale), np.max(np.abs(e.sum(1) - rec[:, 0]) / scale)
+    d = reached.c_of_m - st_r.c_of_m
+    d -= np.round(d)
+    assert np.max(np.abs(d)) < (1e-9 if prec == "fp64" else 1e-6)
+    if prec == "fp64":
+        sgn = np.sign(np.sum(reached.quat * st_r.quat, 1))[:, None]
+        assert np.max(np.abs(reached.quat * sgn - st_r.quat)) < 1e-9
+
+
 def test_md_run_needs_init():
     from moldy_gb300 import ForceField, system
     from moldy_gb300._lib import MdgpuError

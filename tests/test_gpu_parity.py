@@ -143,3 +143,38 @@ def test_accumulates_like_the_reference(lib):
     assert rel_rms(f, fo) < 1e-12
     assert rel(pe, peo[0]) < 1e-12
     assert np.abs(st.reshape(9) - sto).max() / np.abs(sto).max() < 1e-12
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_too_close_pairs_counted_like_the_reference(port_built, prec, tol):
+    """Molecules moved so that sites come closer than the reference's
+    too-close distance (r^2 < 0.25 A^2, src/force.c:939-949): an O by another
+    molecule's H (a pair with no interaction at all -- O carries no charge
+    and LJ acts O-O only) and an H by another molecule's M.  The count of such pairs is the
+    reference's, and the forces still match the oracle."""
+    import dataclasses
+
+    from moldy_gb300 import system
+    from moldy_gb300.forcefield import ForceField
+    base = system.water(nside=6, seed=3)
+    site = np.array(base.site, copy=True)
+    # whole molecules moved (their own geometry kept): the O of molecule 7
+    # by an H of molecule 0, an H of molecule 9 by the M of molecule 0
+    for mol, own, other, d in ((7, 0, 1, (0.3, 0.0, 0.0)), (9, 1, 3, (0.0, 0.35, 0.0))):
+        shift = site[:, other] + np.array(d) - site[:, 4 * mol + own]
+        site[:, 4 * mol:4 * mol + 4] += shift[:, None]
+    sysm = dataclasses.replace(base, site=site)
+    r = port_built.force_calc(sysm)
+    assert r.info.n_too_close >= 2
+    ff = ForceField(sysm, precision=prec)
+    try:
+        f, pe, _ = ff.force_calc()
+        info = ff.info()
+    finally:
+        ff.close()
+    assert info["n_too_close"] == r.info.n_too_close
+    for a, b in info["too_close"]:
+        d = site[:, a] - site[:, b]
+        assert float(d @ d) < 0.25
+    assert rel_rms(f, r.force) < tol, rel_rms(f, r.force)
+    assert rel(pe, r.pe) < tol
