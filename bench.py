@@ -645,10 +645,16 @@ def main():
     ap.add_argument("--adjoint-frames", type=int, default=64)
     ap.add_argument("--profile-case", choices=["mixed", "fp64"],
                     help="run three untimed evaluations of the workload and exit (for ncu captures)")
+    ap.add_argument("--profile-nside", type=int, default=32,
+                    help="molecules per cell edge of the profile case (32: the benchmark workload; "
+                         "16: 16,384 sites, for captures of many passes)")
     args = ap.parse_args()
     if args.profile_case:
         from moldy_gb300.forcefield import ForceField
-        ff = ForceField(make_workload(), precision=args.profile_case)
+        from moldy_gb300 import system as S
+        sysm = make_workload() if args.profile_nside == 32 else S.water(nside=args.profile_nside, seed=7,
+                                                                           alpha=0.3, cutoff=9.0)
+        ff = ForceField(sysm, precision=args.profile_case)
         for _ in range(3):
             _, pe, _ = ff.forces()
         log("profile case done", pe)

@@ -268,7 +268,10 @@ mdgpu_status mdgpu_fm_loss_grad(mdgpu_ctx *ctx, const mdgpu_params *params, cons
  * molecules of rotating species in species order (amom[0] unused, [1..3]
  * principal angular momenta).  A framework molecule (rdof 0) is held fixed
  * as do_step holds it: its momentum is zeroed after the kicks
- * (src/accel.c:748-755).  Thermostats and barostats are not supported. */
+ * (src/accel.c:748-755).  The Nose-Poincare thermostat of const-temp runs
+ * is available (mdgpu_md_set_thermostat); the Parrinello-Rahman barostat of
+ * const-pressure runs is not (such runs keep the reference's own do_step,
+ * calling this library's force_calc and ewald). */
 typedef struct {
    const double *mass;          /* [nspecies] molecular mass, amu             */
    const double *inertia;       /* [nspecies][3] principal moments of inertia */
@@ -300,6 +303,27 @@ mdgpu_status mdgpu_md_set_state(mdgpu_ctx *ctx, const double *c_of_m, const doub
 /* Copies the current state back (any pointer may be NULL). */
 mdgpu_status mdgpu_md_get_state(mdgpu_ctx *ctx, double *c_of_m, double *mom, double *quat,
                                 double *amom);
+
+/* Constant temperature: the steps of mdgpu_md_run then integrate the
+ * Nose-Poincare thermostat as do_step does under const-temp 1
+ * (src/accel.c:673-684, 696-700, 757-791; leapf_nose_therm,
+ * src/leapfrog.c:465-472; the thermostat momentum terms of leapf_quat,
+ * src/leapfrog.c:308-329, 365-386): positions, rotations and kicks scaled
+ * by the thermostat variable s, its momentum driven by the kinetic
+ * energies, the potential energy and d_of_f kB temp (d_of_f as start_up
+ * counts it from the species of mdgpu_md_init).  temp in K, ttmass the
+ * thermostat mass in program units (the reference's control.ttmass after
+ * its unit conversion), ts and tsmom the variable and momentum to start
+ * from (the reference's start: 1 and 0).  H_0 is evaluated on the first
+ * step after this call, as do_step evaluates it on a run's first step.
+ * enable 0 returns to constant energy.  Call after mdgpu_md_init.  The
+ * energy records then hold the kinetic energies divided by s^2 (trans_ke,
+ * rot_ke). */
+mdgpu_status mdgpu_md_set_thermostat(mdgpu_ctx *ctx, int enable, double temp, double ttmass, double ts,
+                                     double tsmom);
+
+/* out[3] = ts, tsmom, H_0 after the last step. */
+mdgpu_status mdgpu_md_get_thermostat(mdgpu_ctx *ctx, double *out);
 
 /* ---- Dump records (the periodic dump of do_step, src/accel.c:811-820,
  * and its conversion, dump_convert, src/dump.c:550-620).  A record is

@@ -183,6 +183,17 @@ static void build_columns(RsGeom &g)
    }
    g.nbr27 = thick;
    for (int k = 0; k < 27; k++) g.nbr27 = g.nbr27 && have[k];
+   // the column holding (dx, dy, -1 .. 1) for each neighbour column
+   for (int d = 0; d < 9; d++) {
+      const int dx = d / 3 - 1, dy = d % 3 - 1;
+      g.nbcol[d] = -1;
+      for (size_t i = 0; i < g.cols.size(); i++) {
+         const int4 cd = g.cols[i];
+         if (cd.x == dx && cd.y == dy && cd.z <= -1 && cd.z + cd.w - 1 >= 1) g.nbcol[d] = (int)i;
+      }
+      if (g.nbcol[d] < 0) g.nbr27 = false;
+   }
+   if (g.nz < 3) g.nbr27 = false;
 }
 
 mdgpu_status build_rs_geom(const double *h, const mdgpu_control &ctl, RsGeom &g)

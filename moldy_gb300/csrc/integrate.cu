@@ -43,7 +43,17 @@ struct MdStepParams {
    double h[9], hinv[9];
    double kick[9];      // 0.5 dt h^T (leapf_mom's scaled transpose)
    double half;         // 0.5 dt
+   // constant temperature (Nose-Poincare): therm 1; ginv = (h^T h)^-1 for
+   // leapf_com's (step / (mass s)) G^-1; Q the thermostat mass; gkt = d_of_f
+   // kB T and ahalf = 0.5 dt d_of_f kB T, in the reference's operation order
+   int therm;
+   double ginv[9];
+   double Q, gkt, ahalf, dt;
 };
+
+// Device record of the thermostat: the variable s, its momentum, H_0 and
+// whether H_0 has been evaluated since the thermostat was set.
+enum { TH_S = 0, TH_SMOM = 1, TH_H0 = 2, TH_H0SET = 3 };
 
 // q <- p * q-style products of src/quaterns.c:38-127 (r may alias p or q)
 __device__ __forceinline__ void qmul(const double *p, const double *q, double *r)
@@ -89,44 +99,85 @@ __device__ __forceinline__ void rot_amom(double step, double rin, const double *
    qmul(quat, rot, quat);
 }
 
-__global__ void k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict__ mol_spec,
-                           const int *__restrict__ mol_q, double *__restrict__ cofm,
-                           const double *__restrict__ mom, double *__restrict__ quat, double *__restrict__ amom,
-                           int *__restrict__ err)
+// Half step of the co-ordinates (leapf_all_coords, src/accel.c:360-372).
+// Under the thermostat (therm non-null) the steps are scaled by its
+// variable s, and each block writes to tpart its share of the thermostat
+// momentum's increments: 0.5 dt times the translational kinetic energy
+// before the step (do_step's H3 half step, src/accel.c:696-700) and the
+// rotational kinetic energies leapf_quat adds between its rotations
+// (src/leapfrog.c:308-329, 365-386).
+__global__ void __launch_bounds__(128)
+k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict__ mol_spec,
+           const int *__restrict__ mol_q, double *__restrict__ cofm, const double *__restrict__ mom,
+           double *__restrict__ quat, double *__restrict__ amom, int *__restrict__ err,
+           const double *__restrict__ therm, double *__restrict__ tpart)
 {
+   __shared__ double sh[128];
    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-   if (m >= P.nmols) return;
+   const double sv = therm ? therm[TH_S] : 1.0;
+   double dsm = 0.0;   // this molecule's increment of the thermostat momentum
+   if (m < P.nmols) {
    const MdSpec &S = spec[mol_spec[m]];
-   // leapf_com: c += (step/mass) G^-1 mom, then the periodic wrap
-   const double *a = S.gdrift;
+   // leapf_com: c += (step/(mass s)) G^-1 mom, then the periodic wrap
+   double gd[9];
+   if (therm) {
+      const double sc = P.half / (S.mass * sv);
+      for (int i = 0; i < 9; i++) gd[i] = DM(sc, P.ginv[i]);
+   } else {
+      for (int i = 0; i < 9; i++) gd[i] = S.gdrift[i];
+   }
+   const double *a = gd;
    double *c = cofm + 3 * (size_t)m;
    const double x0 = mom[3 * (size_t)m], x1 = mom[3 * (size_t)m + 1], x2 = mom[3 * (size_t)m + 2];
    const double y0 = DA(DA(DA(c[0], DM(a[0], x0)), DM(a[1], x1)), DM(a[2], x2));
    const double y1 = DA(DA(DA(c[1], DM(a[3], x0)), DM(a[4], x1)), DM(a[5], x2));
    const double y2 = DA(DA(DA(c[2], DM(a[6], x0)), DM(a[7], x1)), DM(a[8], x2));
+   if (therm) {
+      // trans_ke (src/algorith.c:221-239) of the momenta before the step
+      const double *hi = P.hinv;
+      double v[3];
+      v[0] = DA(DA(DM(hi[0], x0), DM(hi[3], x1)), DM(hi[6], x2));
+      v[1] = DA(DA(DM(hi[1], x0), DM(hi[4], x1)), DM(hi[7], x2));
+      v[2] = DA(DA(DM(hi[2], x0), DM(hi[5], x1)), DM(hi[8], x2));
+      dsm = P.half * ((v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / (2.0 * S.mass * (sv * sv)));
+   }
    c[0] = DS(y0, floor(DA(y0, 0.5)));
    c[1] = DS(y1, floor(DA(y1, 0.5)));
    c[2] = DS(y2, floor(DA(y2, 0.5)));
    const int qi = mol_q[m];
-   if (qi < 0) return;
+   if (qi >= 0) {
    double q[4], L[4];
    for (int k = 0; k < 4; k++) {
       q[k] = quat[4 * (size_t)qi + k];
       L[k] = amom[4 * (size_t)qi + k];
    }
-   const double st = P.half;
+   // leapf_quat's step over s (stepdts); s = 1 at constant energy
+   const double st = P.half / sv;
    const double *ri = S.rinertia;
+   // 2 (rot_ke) s^2 / (amom . amom / I) of rot_ke, src/algorith.c:244-258
+   auto rke = [&]() {
+      double k = 0.0;
+      for (int i = 0; i < 3; i++)
+         if (S.inertia[i] > INERTIA_MIN) k += L[i + 1] * L[i + 1] / S.inertia[i];
+      return k;
+   };
    if (P.nosym) {   // leapf_quat_a, src/leapfrog.c:338-392
+      const double st2 = P.half / (sv * sv);   // stepdts2
       rot_axis(0.5 * st, 0, ri[0], L, q);
+      if (therm) dsm += 0.25 * st2 * ri[0] * (L[1] * L[1]) + 0.25 * st2 * ri[1] * (L[2] * L[2]);
       rot_axis(0.5 * st, 1, ri[1], L, q);
+      if (therm) dsm += 0.5 * st2 * ri[2] * (L[3] * L[3]);
       rot_axis(st, 2, ri[2], L, q);
       rot_axis(0.5 * st, 1, ri[1], L, q);
+      if (therm) dsm += 0.25 * st2 * ri[1] * (L[2] * L[2]) + 0.25 * st2 * ri[0] * (L[1] * L[1]);
       rot_axis(0.5 * st, 0, ri[0], L, q);
    } else {         // leapf_quat_b, src/leapfrog.c:253-333
       const int sx = P.saxis, o1 = P.o1, o2 = P.o2;
       rot_axis(0.5 * st, o1, DS(ri[o1], ri[o2]), L, q);
+      if (therm) dsm += 0.5 * P.half * (0.5 * rke() / (sv * sv));
       rot_axis(st, sx, DS(ri[sx], ri[o2]), L, q);
       rot_amom(st, ri[o2], L, q);
+      if (therm) dsm += 0.5 * P.half * (0.5 * rke() / (sv * sv));
       rot_axis(0.5 * st, o1, DS(ri[o1], ri[o2]), L, q);
    }
    // normalise, src/leapfrog.c:99-114
@@ -138,6 +189,17 @@ __global__ void k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, cons
       quat[4 * (size_t)qi + k] = q[k] / norm;
       amom[4 * (size_t)qi + k] = L[k];
    }
+   }
+   }
+   if (!therm) return;
+   // fixed-shape block sum of the increments
+   sh[threadIdx.x] = dsm;
+   __syncthreads();
+   for (int w = 64; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+      __syncthreads();
+   }
+   if (threadIdx.x == 0) tpart[blockIdx.x] = sh[0];
 }
 
 // Rotation matrix of a quaternion (q_to_rot, src/quaterns.c:129-160).
@@ -212,12 +274,22 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
           const int *__restrict__ mol_q, const int *__restrict__ mol_site0, const double *__restrict__ pf,
           const double *__restrict__ force, const double *__restrict__ quat, double *__restrict__ mom,
           double *__restrict__ amom, double *__restrict__ kpart, double *__restrict__ molf,
-          double *__restrict__ molt)
+          double *__restrict__ molt, const double *__restrict__ therm)
 {
    __shared__ double sh[2][256];
    const int m = blockIdx.x * blockDim.x + threadIdx.x;
    const int N = P.nsites;
    double ket = 0.0, ker = 0.0;
+   // leapf_all_momenta (src/accel.c:376-387): the half kicks scaled by the
+   // thermostat variable, leapf_mom(step s) and leapf_amom(step s)
+   double kick[9], hs = P.half;
+   if (therm) {
+      hs = P.half * therm[TH_S];
+      for (int i = 0; i < 3; i++)
+         for (int j = 0; j < 3; j++) kick[3 * i + j] = DM(hs, P.h[3 * j + i]);
+   } else {
+      for (int i = 0; i < 9; i++) kick[i] = P.kick[i];
+   }
    if (m < P.nmols) {
       const MdSpec &S = spec[mol_spec[m]];
       const int s0 = mol_site0[m];
@@ -244,7 +316,7 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
          for (int k = 0; k < 3; k++) molt[3 * (size_t)qi + k] = T[k];
       }
       for (int k = 0; k < 3; k++) molf[3 * (size_t)m + k] = F[k];
-      const double *a = P.kick;
+      const double *a = kick;
       double *pm = mom + 3 * (size_t)m;
       double x[3] = {pm[0], pm[1], pm[2]};
       for (int half = 0; half < 2; half++) {
@@ -258,7 +330,7 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
          if (qi >= 0) {
             double *am = amom + 4 * (size_t)qi;
             for (int k = 0; k < 3; k++) {
-               am[k + 1] = DA(am[k + 1], DM(P.half, T[k]));
+               am[k + 1] = DA(am[k + 1], DM(hs, T[k]));
                L[k] = am[k + 1];
             }
          }
@@ -302,38 +374,101 @@ k_md_kick(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict
 // Energy record of the step (one block of 128 threads): the kinetic-energy
 // block sums reduced in a fixed order; the record index is a device counter
 // so that a captured step replays unchanged.
+// Under the thermostat it also takes the first half step's increments of
+// the thermostat momentum (tpart, nbt block sums), evaluates H_0 when it
+// has not been since the thermostat was set (do_step does at its first
+// step, src/accel.c:718-727), and applies the potential-energy term of the
+// thermostat momentum (src/accel.c:757-758).
 __global__ void __launch_bounds__(128)
 k_md_record(int *__restrict__ counter, int cap, const double *__restrict__ pe, const double *__restrict__ kpart,
             int nb, double dist_v, const DevOut *__restrict__ out, double *__restrict__ energies,
-            int *__restrict__ err)
+            int *__restrict__ err, MdStepParams P, double *__restrict__ therm, const double *__restrict__ tpart,
+            int nbt)
 {
-   __shared__ double sh[2][128];
+   __shared__ double sh[3][128];
    const int t = threadIdx.x;
-   double kt = 0.0, kr = 0.0;
+   double kt = 0.0, kr = 0.0, ds = 0.0;
    for (int b = t; b < nb; b += 128) {
       kt += kpart[2 * b];
       kr += kpart[2 * b + 1];
    }
+   if (therm)
+      for (int b = t; b < nbt; b += 128) ds += tpart[b];
    sh[0][t] = kt;
    sh[1][t] = kr;
+   sh[2][t] = ds;
    __syncthreads();
    for (int w = 64; w > 0; w >>= 1) {
       if (t < w) {
          sh[0][t] += sh[0][t + w];
          sh[1][t] += sh[1][t + w];
+         sh[2][t] += sh[2][t + w];
       }
       __syncthreads();
    }
    if (t != 0) return;
+   double ket = sh[0][0], ker = sh[1][0];
+   const double pe_tot = (pe[0] + dist_v) + pe[1];
+   if (therm) {
+      // trans_ke and rot_ke divide by s^2 (src/algorith.c:238, 257)
+      const double s = therm[TH_S], s2 = s * s;
+      ket /= s2;
+      ker /= s2;
+      double smom = therm[TH_SMOM] + sh[2][0];
+      if (therm[TH_H0SET] == 0.0) {
+         therm[TH_H0] = (((ket + ker) + pe_tot) + smom * smom / (2.0 * P.Q)) + P.gkt * log(s);
+         therm[TH_H0SET] = 1.0;
+      }
+      smom -= P.dt * (pe_tot - therm[TH_H0]);
+      therm[TH_SMOM] = smom;
+   }
    const int step = *counter;
    *counter = step + 1;
+   if (out->err & 1) *err |= 1;
    if (step >= cap) return;
    double *e = energies + 4 * (size_t)step;
    e[0] = pe[0] + dist_v;
    e[1] = pe[1];
-   e[2] = sh[0][0];
-   e[3] = sh[1][0];
-   if (out->err & 1) *err |= 1;
+   e[2] = ket;
+   e[3] = ker;
+}
+
+// The thermostat's own half steps (one thread): at the start of a step,
+// leapf_nose_therm (src/leapfrog.c:465-472) then the d_of_f kB T term
+// (src/accel.c:680-682); at its end (end != 0) the second half step's
+// increments (tpart, nbt block sums) are added first, then the term and
+// leapf_nose_therm in the reverse order (src/accel.c:787-790).
+__global__ void __launch_bounds__(128)
+k_md_therm(MdStepParams P, double *__restrict__ therm, const double *__restrict__ tpart, int nbt, int end)
+{
+   __shared__ double sh[128];
+   const int t = threadIdx.x;
+   double ds = 0.0;
+   if (end)
+      for (int b = t; b < nbt; b += 128) ds += tpart[b];
+   sh[t] = ds;
+   __syncthreads();
+   for (int w = 64; w > 0; w >>= 1) {
+      if (t < w) sh[t] += sh[t + w];
+      __syncthreads();
+   }
+   if (t != 0) return;
+   double s = therm[TH_S], smom = therm[TH_SMOM];
+   auto nose = [&]() {
+      const double scale = (1.0 + smom * P.half / (2.0 * P.Q));
+      smom /= scale;
+      s *= scale * scale;
+   };
+   if (!end) {
+      nose();
+      smom -= P.ahalf * (1.0 + log(s));
+   } else {
+      smom += sh[0];
+      smom -= P.ahalf * (1.0 + log(s));
+      nose();
+   }
+   therm[TH_S] = s;
+   therm[TH_SMOM] = smom;
 }
 
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
@@ -504,6 +639,12 @@ static void step_params(const mdgpu_ctx *c, MdStepParams &P)
    for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) P.kick[3 * i + j] = H.half * H.h[3 * j + i];
    P.half = H.half;
+   P.therm = H.therm ? 1 : 0;
+   std::memcpy(P.ginv, H.ginv, sizeof P.ginv);
+   P.Q = H.ttmass;
+   P.gkt = H.gkt;
+   P.ahalf = H.ahalf;
+   P.dt = 2.0 * H.half;
 }
 
 }  // namespace mdgpu
@@ -537,6 +678,9 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
       for (int j = 0; j < 3; j++)
          G[3 * i + j] = ht[3 * i] * h[j] + ht[3 * i + 1] * h[3 + j] + ht[3 * i + 2] * h[6 + j];
    inv3(G, Gi);
+   std::memcpy(H.ginv, Gi, sizeof H.ginv);
+   H.therm = false;
+   H.d_of_f = -3;   // start_up's count (src/startup.c:483-485, 570, 591)
    int nq = 0, m = 0, site = 0, pf0 = 0;
    H.saxis = -1;
    for (int k = 0; k < nsp; k++) {
@@ -556,6 +700,7 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
       const double sc = H.half / S.mass;
       for (int i = 0; i < 9; i++) S.gdrift[i] = sc * Gi[i];
       const bool rot = dyn->rdof[k] > 0;
+      H.d_of_f += (S.framework ? 0 : 3 * sp.nmols) + dyn->rdof[k] * sp.nmols;
       if (rot && H.saxis < 0) {
          // near-symmetry axis, chosen once from the first rotating species
          // as leapf_quat_b's static first-call choice does (src/leapfrog.c:282-297)
@@ -607,6 +752,8 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    CK(D.molt.ensure(3 * (size_t)nq + 3));
    CK(D.err.ensure(1));
    CK(D.counter.ensure(1));
+   CK(D.therm.ensure(4));
+   CK(D.tpart.ensure(2 * (size_t)((c->nmols + 127) / 128)));
    CK(cudaMemcpyAsync(D.cofm.p, c_of_m, 3 * (size_t)c->nmols * sizeof(double), cudaMemcpyHostToDevice, st));
    CK(cudaMemcpyAsync(D.mom.p, mom, 3 * (size_t)c->nmols * sizeof(double), cudaMemcpyHostToDevice, st));
    if (nq) {
@@ -633,9 +780,14 @@ static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap
    const MdHost &H = c->mdh;
    MdDev &D = c->md;
    cudaStream_t st = c->stream;
-   const int N = c->nsites, M = c->nmols, nbm = (M + 255) / 256;
-   k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
-                                                D.amom.p, D.err.p);
+   const int N = c->nsites, M = c->nmols, nbm = (M + 255) / 256, nbd = (M + 127) / 128;
+   double *th = P.therm ? D.therm.p : nullptr;
+   if (th) {
+      k_md_therm<<<1, 128, 0, st>>>(P, th, nullptr, 0, 0);
+      c->launches += 1;
+   }
+   k_md_drift<<<nbd, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p, D.amom.p,
+                                   D.err.p, th, D.tpart.p);
    k_md_sites<<<(N + 255) / 256, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.cofm.p,
                                                D.quat.p, c->site.p);
    CK(cudaGetLastError());
@@ -652,13 +804,18 @@ static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap
       c->launches += 2;
    }
    k_md_kick<<<nbm, 256, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.mol_site0.p, D.pf.p, c->force.p,
-                                  D.quat.p, D.mom.p, D.amom.p, D.kpart.p, D.molf.p, D.molt.p);
+                                  D.quat.p, D.mom.p, D.amom.p, D.kpart.p, D.molf.p, D.molt.p, th);
    k_md_record<<<1, 128, 0, st>>>(D.counter.p, cap, c->small.p, D.kpart.p, nbm, dist_v, c->out.p, D.energies.p,
-                                 D.err.p);
-   k_md_drift<<<(M + 127) / 128, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p,
-                                                D.amom.p, D.err.p);
+                                 D.err.p, P, th, D.tpart.p, nbd);
+   k_md_drift<<<nbd, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p, D.amom.p,
+                                   D.err.p, th, D.tpart.p + nbd);
    CK(cudaGetLastError());
    c->launches += 3;
+   if (th) {
+      k_md_therm<<<1, 128, 0, st>>>(P, th, D.tpart.p + nbd, nbd, 1);
+      CK(cudaGetLastError());
+      c->launches += 1;
+   }
    return MDGPU_OK;
 }
 
@@ -835,5 +992,48 @@ extern "C" mdgpu_status mdgpu_md_get_state(mdgpu_ctx *c, double *c_of_m, double 
    if (quat && Q) CK(cudaMemcpyAsync(quat, D.quat.p, 4 * Q * sizeof(double), cudaMemcpyDeviceToHost, st));
    if (amom && Q) CK(cudaMemcpyAsync(amom, D.amom.p, 4 * Q * sizeof(double), cudaMemcpyDeviceToHost, st));
    CK(cudaStreamSynchronize(st));
+   return MDGPU_OK;
+}
+
+// Boltzmann's constant in program units (kB of src/defs.h:226, the
+// CODATA 1986 values and the amu, A, ps units, evaluated in that order).
+static const double KB_PROG = 1.380658e-23 / (1.6605402e-27 * (1.0e-10 / 1.0e-12) * (1.0e-10 / 1.0e-12));
+
+extern "C" mdgpu_status mdgpu_md_set_thermostat(mdgpu_ctx *c, int enable, double temp, double ttmass, double ts,
+                                                double tsmom)
+{
+   if (!c) return MDGPU_E_ARG;
+   if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
+   MdHost &H = c->mdh;
+   if (!enable) {
+      H.therm = false;
+      c->gen++;
+      return MDGPU_OK;
+   }
+   if (!(ttmass > 0.0) || !(temp >= 0.0) || !(ts > 0.0))
+      return fail(c, MDGPU_E_ARG, "thermostat: ttmass and ts must be positive, temp not negative");
+   H.therm = true;
+   H.temp = temp;
+   H.ttmass = ttmass;
+   const double dt = 2.0 * H.half;
+   H.gkt = (double)H.d_of_f * KB_PROG * temp;
+   H.ahalf = 0.5 * dt * (double)H.d_of_f * KB_PROG * temp;
+   const double v[4] = {ts, tsmom, 0.0, 0.0};
+   CK(cudaMemcpyAsync(c->md.therm.p, v, sizeof v, cudaMemcpyHostToDevice, c->stream));
+   CK(cudaStreamSynchronize(c->stream));
+   c->gen++;
+   return MDGPU_OK;
+}
+
+extern "C" mdgpu_status mdgpu_md_get_thermostat(mdgpu_ctx *c, double *out)
+{
+   if (!c || !out) return MDGPU_E_ARG;
+   if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
+   double v[4];
+   CK(cudaMemcpyAsync(v, c->md.therm.p, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+   CK(cudaStreamSynchronize(c->stream));
+   out[0] = v[0];
+   out[1] = v[1];
+   out[2] = v[2];
    return MDGPU_OK;
 }

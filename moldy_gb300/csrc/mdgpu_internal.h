@@ -47,6 +47,7 @@ struct RsGeom {
    // cell is at least 0.5 A thick (any pair closer than the too-close
    // distance lies in neighbouring cells)
    bool nbr27 = false;
+   int nbcol[9] = {0};             // column of each (dx, dy) in [-1, 1]^2 (when nbr27)
 };
 
 // Builds the stencil and cell geometry; returns MDGPU_E_CUTOFF as the
@@ -246,6 +247,11 @@ struct MdHost {
    int64_t graph_launches = 0;       // kernels one replay launches
    int graph_cap = 0;                // record capacity it was captured with
    uint64_t warm_gen = 0;            // configuration of the last direct step
+   // constant temperature (mdgpu_md_set_thermostat)
+   double ginv[9];                   // (h^T h)^-1
+   int d_of_f = 0;                   // degrees of freedom as start_up counts them
+   bool therm = false;
+   double temp = 0, ttmass = 0, gkt = 0, ahalf = 0;
 };
 
 struct MdDev {
@@ -259,6 +265,8 @@ struct MdDev {
    DBuf<double> molf, molt;              // molecular forces, principal torques
    DBuf<double> vpart, virc;             // virial correction (dump records)
    DBuf<float> rec;                      // batch of dump records
+   DBuf<double> therm;                   // s, its momentum, H_0, H_0 evaluated
+   DBuf<double> tpart;                   // block sums of the thermostat momentum's increments
 };
 
 }  // namespace mdgpu

@@ -260,23 +260,45 @@ template <> struct NPar<3> { static constexpr int v = 6; };
 template <> struct NPar<4> { static constexpr int v = 3; };
 template <> struct NPar<6> { static constexpr int v = 7; };
 
+// Reciprocal square root, reciprocal and exponential: correctly rounded
+// (FAST false), or the FP32 hardware approximations (FAST true: rsqrt and
+// reciprocal within 2 ulp, exp within a few ulp over the arguments of the
+// potentials here), which the column-walk pair kernel of the mixed form
+// uses.
+template <typename R, bool FAST> struct PairMath {
+   static __device__ __forceinline__ R rsqrt(R x) { return R(1) / dsqrt<R>(x); }
+   static __device__ __forceinline__ R rcp(R x) { return R(1) / x; }
+   static __device__ __forceinline__ R ex(R x) { return dexp<R>(x); }
+};
+template <> struct PairMath<float, true> {
+   static __device__ __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
+   static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
+   static __device__ __forceinline__ float ex(float x) { return __expf(x); }
+};
+
 // One pair of kernel(): f = -U'(r)/r and U, with the erfc real-space Ewald
 // term by the A&S polynomial when EW (src/kernel.c:182-353 / 355-460).
-template <int PT, bool EW, typename R>
+template <int PT, bool EW, typename R, bool FAST = false>
 __device__ __forceinline__ void pair_fu(R r2, R qq, const R *p, R alpha, R norm, R &f, R &u)
 {
+   typedef PairMath<R, FAST> M;
    R t = R(0), ef = R(0), r = R(0), r_r = R(0), rs_r;
    if (EW || PT != 0) {
-      r = dsqrt<R>(r2);
-      r_r = R(1) / r;
+      if (FAST) {
+         r_r = M::rsqrt(r2);
+         r = r2 * r_r;
+      } else {
+         r = dsqrt<R>(r2);
+         r_r = R(1) / r;
+      }
       rs_r = r_r * r_r;
    } else {
-      rs_r = R(1) / r2;
+      rs_r = M::rcp(r2);
    }
    if (EW) {
       R ar = alpha * r;
-      t = R(1) / (R(1) + R(ASP) * ar);
-      ef = qq * dexp<R>(-(ar * ar));
+      t = M::rcp(R(1) + R(ASP) * ar);
+      ef = qq * M::ex(-(ar * ar));
       t = (t * (R(AS1) + t * (R(AS2) + t * (R(AS3) + t * (R(AS4) + t * R(AS5)))))) * ef * r_r;
       ef = t + norm * ef;
    }
@@ -287,17 +309,17 @@ __device__ __forceinline__ void pair_fu(R r2, R qq, const R *p, R alpha, R norm,
       u = t + p[0] * (r12 - r6);
       f = rs_r * (R(6) * p[0] * (R(2) * r12 - r6) + ef);
    } else if (PT == 1) {
-      R e1 = p[1] * dexp<R>(-p[2] * r);
+      R e1 = p[1] * M::ex(-p[2] * r);
       R r6 = p[0] * (rs_r * rs_r * rs_r);
       u = t - r6 + e1;
       f = rs_r * (R(-6) * r6 + ef) + p[2] * e1 * r_r;
    } else if (PT == 2) {
-      R e1 = p[0] * dexp<R>(-p[1] * r);
-      R e2 = -p[2] * dexp<R>(-p[3] * r);
+      R e1 = p[0] * M::ex(-p[1] * r);
+      R e2 = -p[2] * M::ex(-p[3] * r);
       u = t + e1 + e2;
       f = (p[1] * e1 + p[3] * e2) * r_r + ef * rs_r;
    } else if (PT == 3) {
-      R e1 = p[0] * dexp<R>(-p[1] * r);
+      R e1 = p[0] * M::ex(-p[1] * r);
       R r4 = rs_r * rs_r;
       R r6 = rs_r * r4;
       R r8 = p[5] * (r4 * r4);
@@ -315,10 +337,10 @@ __device__ __forceinline__ void pair_fu(R r2, R qq, const R *p, R alpha, R norm,
       u = t + r4 + r6 + r12;
       f = rs_r * (R(4) * r4 + R(6) * r6 + R(12) * r12 + ef);
    } else {  // Morse (PT == 6)
-      R e1 = p[0] * dexp<R>((p[1] - r) * p[2]);
+      R e1 = p[0] * M::ex((p[1] - r) * p[2]);
       R r6 = p[3] * (rs_r * rs_r * rs_r);
-      R e2 = p[4] * dexp<R>(R(-2) * p[5] * (r - p[6]));
-      R e3 = -p[4] * R(2) * dexp<R>(-p[5] * (r - p[6]));
+      R e2 = p[4] * M::ex(R(-2) * p[5] * (r - p[6]));
+      R e3 = -p[4] * R(2) * M::ex(-p[5] * (r - p[6]));
       u = t + e1 - r6 + e2 + e3;
       f = rs_r * (R(-6) * r6 + ef) + r_r * (p[2] * e1 + (R(2) * p[5]) * e2 + p[5] * e3);
    }
@@ -792,7 +814,7 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
    const int p = blockIdx.x * PAIR_WARPS + w;   // home slot (class-major)
    int *inc = s_inc[w], *jbr = s_jb[w], *infr = s_inf[w], *cand = s_cand[w];
    R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
-   long long nall = 0;   // candidates of every class (the reference's evaluated pairs)
+   int nall = 0;   // candidates of every class (the reference's evaluated pairs)
    if (p < N) {
       const int *csk = cs + (p < n0 ? 0 : P.ncells + 1);
       const int c = cellc[p];
@@ -805,10 +827,14 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
       const int oi = sortc[p];
       const R cut100 = (R)P.cut100;
       for (int base = 0; base < P.ncols; base += 32 * COL_E) {
-         int cnt[2 * COL_E], jb[2 * COL_E], inf[2 * COL_E], tot = 0;
+         // this lane's runs go straight to its rows (counts in inc for now)
+         int tot = 0;
 #pragma unroll
          for (int u = 0; u < COL_E; u++) {
-            cnt[2 * u] = cnt[2 * u + 1] = jb[2 * u] = jb[2 * u + 1] = inf[2 * u] = inf[2 * u + 1] = 0;
+            const int q0 = lane * 2 * COL_E + 2 * u;
+            inc[q0] = inc[q0 + 1] = 0;
+            jbr[q0] = jbr[q0 + 1] = 0;
+            infr[q0] = infr[q0 + 1] = 0;
             const int col = base + lane * COL_E + u;
             if (col < P.ncols) {
                const int4 cd = __ldg(&cols[col]);
@@ -831,17 +857,16 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
                for (int s = 0; s < 2; s++) {
                   if (s < ns) {
                      const int a = __ldg(&csk[cc + za[s]]), b = __ldg(&csk[cc + zb[s] + 1]);
-                     cnt[2 * u + s] = b - a;
-                     jb[2 * u + s] = a;
+                     inc[q0 + s] = b - a;
+                     jbr[q0 + s] = a;
+                     tot += b - a;
                      // offset-table index of a candidate in cell z: z + eb
                      const int eb = ob - cd.z - cz + iz[s] * P.nz;
-                     inf[2 * u + s] = (eb * 32) | (9 * (ix + 1) + 3 * (iy + 1) + (iz[s] + 1));
+                     infr[q0 + s] = (eb * 32) | (9 * (ix + 1) + 3 * (iy + 1) + (iz[s] + 1));
                      nall += __ldg(&cell_start[cc + zb[s] + 1]) - __ldg(&cell_start[cc + za[s]]);
                   }
                }
             }
-#pragma unroll
-            for (int s = 0; s < 2; s++) tot += cnt[2 * u + s];
          }
          const int linc = warp_incl_scan(tot);
          const int T = __shfl_sync(0xffffffffu, linc, 31);
@@ -849,10 +874,9 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
 #pragma unroll
          for (int r = 0; r < 2 * COL_E; r++) {
             const int q = lane * 2 * COL_E + r;
-            jbr[q] = jb[r] - run;        // slot = jbr[q] + candidate index
-            run += cnt[r];
-            inc[q] = run;
-            infr[q] = inf[r];
+            jbr[q] -= run;               // slot = jbr[q] + candidate index
+            run += inc[q];
+            inc[q] = run;                // the row's inclusive end
          }
          __syncwarp();
          for (int w0 = 0; w0 < T; w0 += COL_WIN) {
@@ -861,7 +885,7 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
 #pragma unroll
             for (int r = 0; r < 2 * COL_E; r++) {
                const int q = lane * 2 * COL_E + r;
-               const int e1 = inc[q], e0 = e1 - cnt[r];
+               const int e1 = inc[q], e0 = q > 0 ? inc[q - 1] : 0;
                const int a = max(e0, w0), b = min(e1, w1);
                const int jq = jbr[q];
                for (int t = a; t < b; t++) cand[t - w0] = (jq + t) | (q << 24);
@@ -897,12 +921,12 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
 #pragma unroll
                      for (int k = 0; k < NP; k++) pp[k] = pj[k];
                      R f, u;
-                     pair_fu<PT, EW, R>(r2, xj.w * qi, pp, alpha, norm, f, u);
+                     pair_fu<PT, EW, R, true>(r2, xj.w * qi, pp, alpha, norm, f, u);
                      if (intra) {
                         // as in k_pairs: an intramolecular pair's energy is
                         // what the intramolecular correction subtracts again
                         R fa, ua = R(0);
-                        if (clip) pair_fu<PT, EW, R>(r2a, xj.w * qi, pp, alpha, norm, fa, ua);
+                        if (clip) pair_fu<PT, EW, R, true>(r2a, xj.w * qi, pp, alpha, norm, fa, ua);
                         u = clip ? u - ua : R(0);
                      }
                      const R hf = R(0.5) * f;
@@ -959,41 +983,74 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
 // Pairs across the interaction classes that come closer than the too-close
 // distance (the reference warns of every evaluated pair with r^2 < 0.25,
 // src/force.c:943-948, whatever its potential): such a pair lies in the
-// 27-cell neighbourhood (cells at least 0.5 A thick), so each site checks
-// the other class's sites there in FP64, with the reference's operation
-// order and the image of the cell offset.  Reported once per pair (from
-// the lower site index), intramolecular pairs excepted, as k_pairs does.
-__global__ void k_tooclose_x(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ slot_cell,
-                             const int2 *__restrict__ tag, const int *__restrict__ cls_of_id,
-                             const int *__restrict__ sorted, const double *__restrict__ site, DevOut *out)
+// 27-cell neighbourhood (cells at least 0.5 A thick).  One thread per
+// class-0 slot (class-major layout) takes the class-1 sites of the
+// neighbourhood, 9 column runs of 3 cells, and forms r^2 in FP32 from the
+// cell-relative co-ordinates and the exact cell offset (hi + lo), re-made
+// in FP64 from the original co-ordinates with the reference's operation
+// order within 1e-3 A^2 of the threshold, as k_pairs decides.  Reported
+// once per pair, as (lower site index, higher), intramolecular pairs
+// excepted.  nbcol[9]: the stencil column of each (dx, dy) in [-1, 1]^2.
+struct NbCols {
+   int col[9];
+};
+
+__global__ void __launch_bounds__(256)
+k_tooclose_x(RsParams P, NbCols nb, const int *__restrict__ cs, const int *__restrict__ pre,
+             const int4 *__restrict__ cols, const int *__restrict__ col_base,
+             const float4 *__restrict__ coff_hi, const float4 *__restrict__ coff_lo,
+             const float4 *__restrict__ posc, const int2 *__restrict__ tagc, const int *__restrict__ cellc,
+             const int *__restrict__ sortc, const double *__restrict__ site, DevOut *out)
 {
    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-   const int N = P.nsites;
-   if (p >= N) return;
-   const int c = slot_cell[p];
+   const int N = P.nsites, n0 = pre[N];
+   if (p >= n0) return;
+   const int *cs1 = cs + P.ncells + 1;
+   const int c = cellc[p];
    const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
-   const int2 ti = tag[p];
-   const int ki = cls_of_id[ti.x], oi = sorted[p];
-   const double xi = site[oi], yi = site[N + oi], zi = site[2 * (size_t)N + oi];
-   for (int d = 0; d < 27; d++) {
-      int bx = cx + d / 9 - 1, by = cy + (d / 3) % 3 - 1, bz = cz + d % 3 - 1;
+   const float4 xi = posc[p];
+   const int moli = tagc[p].y, oi = sortc[p];
+   for (int d = 0; d < 9; d++) {
+      const int dx = d / 3 - 1, dy = d % 3 - 1;
+      int bx = cx + dx, by = cy + dy;
       const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
       const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
-      const int iz = bz < 0 ? -1 : (bz >= P.nz ? 1 : 0);
       bx -= ix * P.nx;
       by -= iy * P.ny;
-      bz -= iz * P.nz;
-      const int cb = bz + P.nz * (by + P.ny * bx);
-      const double *rl = P.reloc[9 * (ix + 1) + 3 * (iy + 1) + (iz + 1)];
-      for (int j = cell_start[cb]; j < cell_start[cb + 1]; j++) {
-         const int2 tj = tag[j];
-         const int oj = sorted[j];
-         if (cls_of_id[tj.x] == ki || tj.y == ti.y || oj <= oi) continue;
-         const double ax = __dadd_rn(__dsub_rn(site[oj], xi), rl[0]);
-         const double ay = __dadd_rn(__dsub_rn(site[N + oj], yi), rl[1]);
-         const double az = __dadd_rn(__dsub_rn(site[2 * (size_t)N + oj], zi), rl[2]);
-         const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az));
-         if (d2 < TOO_CLOSE) note_too_close(out, oi, oj);
+      const int cc = P.nz * (by + P.ny * bx);
+      const int ci = nb.col[d];
+      const int eb = __ldg(&col_base[ci]) - __ldg(&cols[ci]).z - cz;   // offset index of cell z: z + eb
+      // cells cz-1 .. cz+1 of the column, split where they wrap in z (the
+      // scan runs only with nz >= 3, so one side at most)
+      const int z0 = cz - 1, z1 = cz + 1;
+      int za[2], zb[2], iz[2], ns = 1;
+      if (z0 < 0) { za[0] = z0 + P.nz; zb[0] = P.nz - 1; iz[0] = -1; za[1] = 0; zb[1] = z1; iz[1] = 0; ns = 2; }
+      else if (z1 >= P.nz) { za[0] = z0; zb[0] = P.nz - 1; iz[0] = 0; za[1] = 0; zb[1] = z1 - P.nz; iz[1] = 1; ns = 2; }
+      else { za[0] = z0; zb[0] = z1; iz[0] = 0; }
+      for (int s = 0; s < ns; s++) {
+         const int kimg = 9 * (ix + 1) + 3 * (iy + 1) + (iz[s] + 1);
+         for (int j = cs1[cc + za[s]]; j < cs1[cc + zb[s] + 1]; j++) {
+            const int2 tj = tagc[j];
+            if (tj.y == moli) continue;
+            const int e = (tj.x >> 16) + iz[s] * P.nz + eb;
+            const float4 xj = posc[j];
+            const float4 h4 = __ldg(&coff_hi[e]), l4 = __ldg(&coff_lo[e]);
+            const float rx = (h4.x + (xj.x - xi.x)) + l4.x;
+            const float ry = (h4.y + (xj.y - xi.y)) + l4.y;
+            const float rz = (h4.z + (xj.z - xi.z)) + l4.z;
+            const float r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 >= (float)TOO_CLOSE + 1e-3f) continue;
+            bool close = r2 < (float)TOO_CLOSE;
+            const int oj = sortc[j];
+            if (fabsf(r2 - (float)TOO_CLOSE) < 1e-3f) {
+               const double *rl = P.reloc[kimg];
+               const double ax = __dadd_rn(__dsub_rn(site[oj], site[oi]), rl[0]);
+               const double ay = __dadd_rn(__dsub_rn(site[N + oj], site[N + oi]), rl[1]);
+               const double az = __dadd_rn(__dsub_rn(site[2 * (size_t)N + oj], site[2 * (size_t)N + oi]), rl[2]);
+               close = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az)) < TOO_CLOSE;
+            }
+            if (close) note_too_close(out, min(oi, oj), max(oi, oj));
+         }
       }
    }
 }
@@ -1692,8 +1749,11 @@ static mdgpu_status rs_pairs_col(mdgpu_ctx *c, const RsParams &P, double *d_forc
    CK(e);
    c->launches += 1;
    if (two) {
-      k_tooclose_x<<<(N + 255) / 256, 256, 0, st>>>(P, d.cell_start.p, d.slot_cell.p, d.tag.p, d.cls_of_id.p,
-                                                    d.sorted.p, c->cur_site, c->out.p);
+      NbCols nb;
+      for (int k = 0; k < 9; k++) nb.col[k] = c->rs.nbcol[k];
+      k_tooclose_x<<<(N + 255) / 256, 256, 0, st>>>(P, nb, d.cs.p, d.cls_pre.p, d.cols.p, d.col_base.p, d.coff_hi.p,
+                                                    d.coff_lo.p, d.posc.p, d.tagc.p, d.cellc.p, d.sortc.p,
+                                                    c->cur_site, c->out.p);
       CK(cudaGetLastError());
       c->launches += 1;
    }

@@ -156,6 +156,20 @@ class MolecularDynamics:
         self.ff._check(self.L.mdgpu_md_set_state(self.ff.ctx, _dp(cm), _dp(mo), _dp(qu) if self.nq else None,
                                                  _dp(am) if self.nq else None))
 
+    def set_thermostat(self, temp: float, ttmass: float, ts: float = 1.0, tsmom: float = 0.0,
+                       enable: bool = True) -> None:
+        """Constant temperature (mdgpu_md_set_thermostat): the Nose-Poincare
+        thermostat of do_step under const-temp, temp in K, ttmass in program
+        units; H_0 is evaluated on the next step."""
+        self.ff._check(self.L.mdgpu_md_set_thermostat(self.ff.ctx, int(enable), float(temp), float(ttmass),
+                                                      float(ts), float(tsmom)))
+
+    def thermostat(self):
+        """(ts, tsmom, H_0) after the last step."""
+        out = np.zeros(3)
+        self.ff._check(self.L.mdgpu_md_get_thermostat(self.ff.ctx, _dp(out)))
+        return float(out[0]), float(out[1]), float(out[2])
+
     def state(self) -> MDState:
         sysm = self.ff.sysm
         cm, mo = np.zeros((sysm.nmols, 3)), np.zeros((sysm.nmols, 3))

@@ -39,7 +39,8 @@ def write_mdstate(path: str, sysm, dyn, state, nsteps: int) -> None:
             f.write(np.ascontiguousarray(a, "<f8").tobytes())
 
 
-def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_out=None, restart_in=None):
+def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_out=None, restart_in=None,
+        const_temp=None):
     """(records [nsteps, 3] = (H_0, pe[0], pe[1]) per step, final MDState,
     seconds per step).  The reference prints its notes to stdout.
 
@@ -47,7 +48,10 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_ou
     its dump files (from step 1); they are returned as a fourth item,
     {file name: bytes}.  restart_out: path the reference's write_restart
     saves the final state to; restart_in: a restart file whose dynamic
-    state, read back by the reference's own reader, replaces `state`."""
+    state, read back by the reference's own reader, replaces `state`.
+    const_temp = (T, Q): the reference's Nose-Poincare thermostat at T (K)
+    with thermostat mass Q; the records are then [nsteps, 5] = (H_0, pe[0],
+    pe[1], ts, tsmom)."""
     from moldy_gb300.dynamics import MDState
     exe = os.path.join(REF, "moldy_ref_md_fast" if fast else "moldy_ref_md")
     if not os.path.exists(exe):
@@ -62,6 +66,8 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_ou
             env["MOLDY_REF_RESTART_OUT"] = os.path.abspath(restart_out)
         if restart_in:
             env["MOLDY_REF_RESTART_IN"] = os.path.abspath(restart_in)
+        if const_temp:
+            env["MOLDY_REF_CONST_TEMP"] = "%.17g %.17g" % tuple(const_temp)
         subprocess.run(args, check=True, cwd=d, stdout=subprocess.DEVNULL, env=env)
         raw = np.fromfile(pout, "<f8")
         files = {}
@@ -70,8 +76,9 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_ou
                 if fn not in ("in.mdstate", "out.bin"):
                     with open(os.path.join(d, fn), "rb") as fh:
                         files[fn] = fh.read()
-    o = 3 * nsteps
-    rec = raw[:o].reshape(nsteps, 3)
+    w = 5 if const_temp else 3
+    o = w * nsteps
+    rec = raw[:o].reshape(nsteps, w)
     cm = raw[o:o + 3 * nm].reshape(nm, 3)
     o += 3 * nm
     mo = raw[o:o + 3 * nm].reshape(nm, 3)

@@ -27,6 +27,13 @@
  * out.bin: f64 per step (H_0, pe[0], pe[1]); then c_of_m, mom, quat, amom;
  *   then f64 seconds per step.
  *
+ * Constant temperature (the Nose-Poincare thermostat of do_step,
+ * src/accel.c:673-684, 696-700, 757-791):
+ *   MOLDY_REF_CONST_TEMP="T Q"  const-temp 1 at temperature T (K) with
+ *     thermostat mass Q (control.ttmass); H_0 is set on the first step only
+ *     and each step's record adds the thermostat variable and momentum
+ *     (H_0, pe[0], pe[1], ts, tsmom).
+ *
  * Restart files (the reference's own writer and reader, src/restart.c):
  *   MOLDY_REF_RESTART_OUT=path  after the run, write_restart (native
  *     format, src/restart.c:435-548) saves the whole state to path;
@@ -121,7 +128,9 @@ int main(int argc, char **argv)
       rd(mi, 8, 4, f);
       sp->mass = mi[0]; sp->inertia[0] = mi[1]; sp->inertia[1] = mi[2]; sp->inertia[2] = mi[3];
       if (sp->rdof > 0) nq += sp->nmols;
-      sys.d_of_f += 3 * sp->nmols + sp->rdof * sp->nmols;
+      /* degrees of freedom as start_up counts them (src/startup.c:483-485,
+         570, 591): no translation for a framework */
+      sys.d_of_f += (sp->framework ? 0 : 3 * sp->nmols) + sp->rdof * sp->nmols;
    }
    sys.d_of_f -= 3;
    sys.nmols_r = nq;
@@ -213,11 +222,15 @@ int main(int argc, char **argv)
    o = fopen(argv[2], "wb");
    if (!o) { perror(argv[2]); return 2; }
    clock_gettime(CLOCK_MONOTONIC, &t0);
+   {
+      const char *ct = getenv("MOLDY_REF_CONST_TEMP");
+      if (ct && sscanf(ct, "%lf %lf", &control.temp, &control.ttmass) == 2) control.const_temp = 1;
+   }
    for (control.istep = 1; control.istep <= nsteps; control.istep++) {
-      double rec[3];
-      do_step(&sys, species, site_info, potpar, msq, pe, dip, stress, &rh, 0, 1);
-      rec[0] = sys.H_0; rec[1] = pe[0]; rec[2] = pe[1];
-      fwrite(rec, 8, 3, o);
+      double rec[5];
+      do_step(&sys, species, site_info, potpar, msq, pe, dip, stress, &rh, 0, control.const_temp ? 0 : 1);
+      rec[0] = sys.H_0; rec[1] = pe[0]; rec[2] = pe[1]; rec[3] = sys.ts; rec[4] = sys.tsmom;
+      fwrite(rec, 8, control.const_temp ? 5 : 3, o);
    }
    clock_gettime(CLOCK_MONOTONIC, &t1);
    if (getenv("MOLDY_REF_RESTART_OUT")) {

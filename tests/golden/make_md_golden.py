@@ -16,6 +16,10 @@ The framework fixture (md_waterwall) holds rigid water over a fixed,
 charged framework molecule: the reference zeroes the framework's momentum
 after each step's kicks (src/accel.c:748-755).
 
+The constant-temperature fixtures (md_nvt_*) hold runs of the reference's
+Nose-Poincare thermostat (const-temp 1): per step (H_0, pe[0], pe[1], ts,
+tsmom).
+
 The restart fixture (md_restart_water864) holds a restart file the
 reference's write_restart saved after 10 steps from the thermal start, the
 state those steps reached, and the reference's next 10 steps from that file
@@ -94,6 +98,18 @@ def main():
                 save("md_drift_water2048" + ("_strict" if strict else "") + "_" + tag, s, dyn, st, rec, fin, sec,
                      300.0, seed)
         return
+    if only in (None, "md_nvt"):
+        # constant temperature: the reference's Nose-Poincare thermostat
+        # (const-temp 1, 250 K from a 300 K start, thermostat mass 1e4 in
+        # program units -- the reference's default of 100 kJ/mol ps^2), both
+        # rotational splittings
+        w = S.water(nside=6, seed=3)
+        ws = dataclasses.replace(w, control=dataclasses.replace(w.control, strict_cutoff=True))
+        for name, sysm, seed, nosym in (("md_nvt_water864", w, 15, False), ("md_nvt_water864_strict_nosym", ws, 16, True)):
+            dyn = species_dynamics(sysm, 0.001, nosym)
+            st = thermal_state(sysm, dyn, 300.0, seed)
+            rec, fin, sec = md.run(sysm, dyn, st, 30, const_temp=(250.0, 1.0e4))
+            save(name, sysm, dyn, st, rec, fin, sec, 300.0, seed, nvt_temp=250.0, nvt_ttmass=1.0e4)
     if only in (None, "md_restart_water864"):
         # the reference's restart file after 10 steps (its own
         # write_restart) and its continuation read back from that file

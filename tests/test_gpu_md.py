@@ -103,6 +103,42 @@ def test_continues_from_the_reference_restart_file(prec, tol):
         assert np.max(np.abs(reached.quat * sgn - st_r.quat)) < 1e-9
 
 
+@pytest.mark.parametrize("name", ["md_nvt_water864", "md_nvt_water864_strict_nosym"])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 2e-5)])
+def test_thermostat_follows_reference(name, prec, tol):
+    """Constant temperature: the reference's own do_step under const-temp 1
+    (the Nose-Poincare thermostat, 250 K from a 300 K start) and the GPU run
+    from the same state give the same potential energies every step, the
+    same H_0 (evaluated on the first step), thermostat variable s and
+    momentum, and final state."""
+    from moldy_gb300 import ForceField
+    from moldy_gb300.dynamics import MolecularDynamics
+    sysm, dyn, st0, st1, z = _load(name)
+    rec = z["ref_rec"]
+    ff = ForceField(sysm, precision=prec)
+    try:
+        md = MolecularDynamics(ff, dyn, st0)
+        md.set_thermostat(float(z["nvt_temp"]), float(z["nvt_ttmass"]))
+        e = md.run(len(rec))
+        ts, tsmom, H0 = md.thermostat()
+        st = md.state()
+    finally:
+        ff.close()
+    scale = np.abs(e[:, 0]) + np.abs(e[:, 1]) + e[:, 2] + e[:, 3]
+    assert np.all(np.abs(e[:, 0] - rec[:, 1]) <= tol * scale), np.max(np.abs(e[:, 0] - rec[:, 1]) / scale)
+    assert np.all(np.abs(e[:, 1] - rec[:, 2]) <= tol * scale)
+    assert abs(H0 - rec[0, 0]) <= tol * scale[0], (H0, rec[0, 0])
+    assert abs(ts - rec[-1, 3]) <= tol * abs(rec[-1, 3] - 1.0) + 1e-12, (ts, rec[-1, 3])
+    assert abs(tsmom - rec[-1, 4]) <= tol * np.max(np.abs(rec[:, 4])) * 10, (tsmom, rec[-1, 4])
+    d = st.c_of_m - st1.c_of_m
+    d -= np.round(d)
+    assert np.max(np.abs(d)) < (1e-9 if prec == "fp64" else 1e-6)
+    if prec == "fp64":
+        sgn = np.sign(np.sum(st.quat * st1.quat, 1))[:, None]
+        assert np.max(np.abs(st.quat * sgn - st1.quat)) < 1e-9
+        assert np.max(np.abs(st.mom - st1.mom)) <= 1e-7 * np.max(np.abs(st1.mom))
+
+
 def test_md_run_needs_init():
     from moldy_gb300 import ForceField, system
     from moldy_gb300._lib import MdgpuError
@@ -113,8 +149,8 @@ def test_md_run_needs_init():
 
 
 DRIFT = {
-    "water2048": ["md_drift_water2048", "md_drift_water2048_b", "md_drift_water2048_c"],
-    "water2048_strict": ["md_drift_water2048_strict", "md_drift_water2048_strict_b", "md_drift_water2048_strict_c"],
+    "water2048": ["md_drift_water2048"] + ["md_drift_water2048_" + t for t in "bcdefgh"],
+    "water2048_strict": ["md_drift_water2048_strict"] + ["md_drift_water2048_strict_" + t for t in "bcdefgh"],
     "argon500": ["md_drift_argon500"],
 }
 
@@ -122,36 +158,53 @@ DRIFT = {
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 @pytest.mark.parametrize("case", sorted(DRIFT))
 def test_energy_drift_no_worse_than_reference(case, prec):
-    """Whole reference runs (10^4 steps of water from three thermal starts,
-    10^3 of argon) on the GPU from the same starts: the least-squares drift
-    of the conserved quantity and its fluctuation about the trend, averaged
-    over the starts, are no larger than the reference's own, within a
-    margin.  The trajectories part within a few hundred steps, after which
-    each run's drift is one sample of a noisy quantity (in lazy link-cell
-    mode pairs beyond the cutoff enter and leave the evaluated set at
-    random; with strict cut-offs the slope of a 10^4-step run is dominated
-    by slow fluctuations of the conserved quantity): single runs of the
-    reference's own arithmetic (the FP64 GPU form) measured 2.1-2.2x the
-    reference's figure, hence the average over starts and a factor 2.5."""
-    from moldy_gb300.dynamics import drift_per_ns
+    """Whole reference runs (10^4 steps of 2048-site water from eight thermal
+    starts, lazy and strict cut-offs; 10^3 steps of argon) on the GPU from the
+    same starts: the least-squares drift of the conserved quantity and its
+    fluctuation about the trend.  The trajectories part within a few hundred
+    steps, after which each run's drift is one sample of a noisy quantity
+    (lazy link cells: pairs beyond the cutoff enter and leave the evaluated
+    set; strict cut-offs: slow fluctuations of the conserved quantity set
+    the slope of a 10^4-step run), so the water cases compare means over
+    the eight starts: the GPU's mean |drift| may exceed the reference's by at
+    most two standard errors of the difference of the means (a one-sided
+    bound at about 98%).  Sixteen further starts of the GPU alone measured
+    the FP32-mixed form's mean at 1.01x (strict) and 1.18x (lazy) the FP64
+    form's, within those errors.  Argon has one start and keeps a margin of
+    2.5x the reference's drift plus 1e-5 of the kinetic energy over the
+    run."""
+    from moldy_gb300 import ForceField
+    from moldy_gb300.dynamics import MolecularDynamics, drift_per_ns
     names = [n for n in DRIFT[case] if os.path.exists(os.path.join(GOLDEN, n + ".npz"))]
     if not names:
         pytest.skip("drift fixtures not generated")
     d_ref, d_gpu, fl_ref, fl_gpu, kes, span = [], [], [], [], [], 0.0
     for name in names:
-        sysm, z, e, st, st1 = _run(name, prec)
+        sysm, dyn, st0, st1, z = _load(name)
+        stride = int(z["rec_stride"]) if "rec_stride" in z else 1
         rec = z["ref_rec"]
         dt = float(z["md_step"])
+        ff = ForceField(sysm, precision=prec)
+        try:
+            e = MolecularDynamics(ff, dyn, st0).run(len(rec) * stride)
+        finally:
+            ff.close()
         H_ref, H = rec[:, 0], e.sum(1)
-        d_ref.append(abs(drift_per_ns(np.stack([H_ref, 0 * H_ref, 0 * H_ref, 0 * H_ref], 1), dt)))
+        d_ref.append(abs(drift_per_ns(np.stack([H_ref, 0 * H_ref, 0 * H_ref, 0 * H_ref], 1), dt * stride)))
         d_gpu.append(abs(drift_per_ns(e, dt)))
-        t = np.arange(len(H))
-        fl_ref.append(np.std(H_ref - np.polyval(np.polyfit(t, H_ref, 1), t)))
+        t, tr = np.arange(len(H)), np.arange(len(H_ref))
+        fl_ref.append(np.std(H_ref - np.polyval(np.polyfit(tr, H_ref, 1), tr)))
         fl_gpu.append(np.std(H - np.polyval(np.polyfit(t, H, 1), t)))
         kes.append(float(np.mean(e[:, 2] + e[:, 3])))
         span = len(H) * dt * 1e-3
     ke = float(np.mean(kes))
-    # margin: 2.5x the reference's mean plus 1e-5 of the kinetic energy
-    # over the run
-    assert np.mean(d_gpu) <= 2.5 * np.mean(d_ref) + 1e-5 * ke / span, (d_gpu, d_ref)
-    assert np.mean(fl_gpu) <= 2.5 * np.mean(fl_ref) + 1e-6 * ke, (fl_gpu, fl_ref)
+    n = len(names)
+    print(f"{case} {prec}: mean |drift| GPU {np.mean(d_gpu):.4g} reference {np.mean(d_ref):.4g} over {n} starts; "
+          f"fluctuation GPU {np.mean(fl_gpu):.4g} reference {np.mean(fl_ref):.4g}")
+    if n >= 4:
+        for g, r in ((d_gpu, d_ref), (fl_gpu, fl_ref)):
+            se = np.sqrt(np.var(g, ddof=1) / n + np.var(r, ddof=1) / n)
+            assert np.mean(g) - np.mean(r) <= 2.0 * se, (g, r, se)
+    else:
+        assert np.mean(d_gpu) <= 2.5 * np.mean(d_ref) + 1e-5 * ke / span, (d_gpu, d_ref)
+        assert np.mean(fl_gpu) <= 2.5 * np.mean(fl_ref) + 1e-6 * ke, (fl_gpu, fl_ref)
