@@ -468,7 +468,7 @@ def run_gpu(args):
     dom = max(work, key=lambda k: phases.get(k, 0.0))
     achieved = work[dom] / (phases[dom] * 1e-3) / 1e12
     traffic = traffic_from_profiles().get(dom)
-    kernel_names = {"kforce": "k_force_tc", "sfac": "k_sfac_tc", "pairs": "k_pairs<LJ,erfc,mixed>"}
+    kernel_names = {"kforce": "k_force_tc", "sfac": "k_sfac_tc", "pairs": "k_pairs_col<LJ,erfc>"}
     peaks = measured_peaks()
     mma = tc_mma_flops(sysA, n_q)
     if dom in mma:
