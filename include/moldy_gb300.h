@@ -269,9 +269,8 @@ mdgpu_status mdgpu_fm_loss_grad(mdgpu_ctx *ctx, const mdgpu_params *params, cons
  * principal angular momenta).  A framework molecule (rdof 0) is held fixed
  * as do_step holds it: its momentum is zeroed after the kicks
  * (src/accel.c:748-755).  The Nose-Poincare thermostat of const-temp runs
- * is available (mdgpu_md_set_thermostat); the Parrinello-Rahman barostat of
- * const-pressure runs is not (such runs keep the reference's own do_step,
- * calling this library's force_calc and ewald). */
+ * (mdgpu_md_set_thermostat) and the Parrinello-Rahman cell dynamics of
+ * const-pressure runs (mdgpu_md_set_barostat) are available. */
 typedef struct {
    const double *mass;          /* [nspecies] molecular mass, amu             */
    const double *inertia;       /* [nspecies][3] principal moments of inertia */
@@ -324,6 +323,29 @@ mdgpu_status mdgpu_md_set_thermostat(mdgpu_ctx *ctx, int enable, double temp, do
 
 /* out[3] = ts, tsmom, H_0 after the last step. */
 mdgpu_status mdgpu_md_get_thermostat(mdgpu_ctx *ctx, double *out);
+
+/* Constant pressure: the steps of mdgpu_md_run then integrate the
+ * Parrinello-Rahman cell dynamics as do_step does under const-pressure
+ * (src/accel.c:686-704, 759-783; gleap_cell and update_hmom,
+ * src/leapfrog.c:474-535): mode 1 anisotropic, 2 uniform dilation (the
+ * reference's const-pressure 1 and 2), pressure and pmass (the cell mass W)
+ * in program units as the reference's control record holds them after its
+ * unit conversion, strain_mask its strain-mask (bit 3i+j set: element (i,j)
+ * of h held fixed; the reference's default 200 keeps h upper triangular, as
+ * the force path needs), hmom the cell momentum to start from ([3][3]
+ * row-major, NULL for zero).  The kinetic and virial stress are reduced on
+ * the device each step and h advances on the host, so each step runs its
+ * launches directly and the force path rebuilds its cell grid and k-vector
+ * list for the new h.  Combines with the thermostat.  H_0 (with the cell's
+ * kinetic energy and pressure x volume terms) is evaluated on the next step.
+ * mode 0 returns to constant volume; MDGPU_E_UNSUPPORTED with molecular
+ * cut-offs.  Call after mdgpu_md_init. */
+mdgpu_status mdgpu_md_set_barostat(mdgpu_ctx *ctx, int mode, double pressure, double pmass, int strain_mask,
+                                   const double *hmom);
+
+/* The current cell h and its momentum ([3][3] each, row-major; either may be
+ * NULL). */
+mdgpu_status mdgpu_md_get_barostat(mdgpu_ctx *ctx, double *h, double *hmom);
 
 /* ---- Dump records (the periodic dump of do_step, src/accel.c:811-820,
  * and its conversion, dump_convert, src/dump.c:550-620).  A record is

@@ -24,7 +24,8 @@ EXPORTS = ["mdgpu_create", "mdgpu_destroy", "mdgpu_last_error", "mdgpu_set_preci
            "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak", "mdgpu_tc_probe", "mdgpu_tc_rate", "mdgpu_tc_items",
            "mdgpu_ewald_kspace_noalloc", "mdgpu_set_params", "mdgpu_energy_grad",
            "mdgpu_fm_loss_grad", "mdgpu_md_init", "mdgpu_md_run", "mdgpu_md_get_state", "mdgpu_md_set_state",
-           "mdgpu_md_set_thermostat", "mdgpu_md_get_thermostat",
+           "mdgpu_md_set_thermostat", "mdgpu_md_get_thermostat", "mdgpu_md_set_barostat",
+           "mdgpu_md_get_barostat",
            "mdgpu_rdf_counts", "mdgpu_dump_size", "mdgpu_md_run_dump", "mdgpu_dump_open",
            "mdgpu_dump_append", "mdgpu_dump_filename", "mdgpu_dump_errmsg", "mdgpu_dump_close",
            "force_calc", "ewald", "poteval"]
@@ -139,6 +140,8 @@ def load():
         "mdgpu_md_set_state": ([vp, dp, dp, dp, dp], ip),
         "mdgpu_md_set_thermostat": ([vp, ip, C.c_double, C.c_double, C.c_double, C.c_double], ip),
         "mdgpu_md_get_thermostat": ([vp, dp], ip),
+        "mdgpu_md_set_barostat": ([vp, ip, C.c_double, C.c_double, ip, dp], ip),
+        "mdgpu_md_get_barostat": ([vp, dp, dp], ip),
         "mdgpu_dump_size": ([ip, ip, ip], ip),
         "mdgpu_md_run_dump": ([vp, ip, ip, ip, ip, dp, C.POINTER(C.c_float)], ip),
         "mdgpu_dump_open": ([C.POINTER(vp), C.c_char_p, C.POINTER(DumpInfo)], ip),

@@ -49,6 +49,13 @@ struct MdStepParams {
    int therm;
    double ginv[9];
    double Q, gkt, ahalf, dt;
+   // constant pressure (Parrinello-Rahman): baro 1.  The cell's terms of
+   // H_0 (ke_cell, pressure x volume), increments of the thermostat
+   // momentum made on the host by the cell's half steps (dsm_mid before H_0,
+   // dsm_end at the step's end), and h's momentum for dump records.
+   int baro;
+   double kecell, pv, dsm_mid, dsm_end, W;
+   double hmom[9];
 };
 
 // Device record of the thermostat: the variable s, its momentum, H_0 and
@@ -120,19 +127,15 @@ k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restric
    const MdSpec &S = spec[mol_spec[m]];
    // leapf_com: c += (step/(mass s)) G^-1 mom, then the periodic wrap
    double gd[9];
-   if (therm) {
-      const double sc = P.half / (S.mass * sv);
-      for (int i = 0; i < 9; i++) gd[i] = DM(sc, P.ginv[i]);
-   } else {
-      for (int i = 0; i < 9; i++) gd[i] = S.gdrift[i];
-   }
+   const double sc = P.half / (S.mass * sv);
+   for (int i = 0; i < 9; i++) gd[i] = DM(sc, P.ginv[i]);
    const double *a = gd;
    double *c = cofm + 3 * (size_t)m;
    const double x0 = mom[3 * (size_t)m], x1 = mom[3 * (size_t)m + 1], x2 = mom[3 * (size_t)m + 2];
    const double y0 = DA(DA(DA(c[0], DM(a[0], x0)), DM(a[1], x1)), DM(a[2], x2));
    const double y1 = DA(DA(DA(c[1], DM(a[3], x0)), DM(a[4], x1)), DM(a[5], x2));
    const double y2 = DA(DA(DA(c[2], DM(a[6], x0)), DM(a[7], x1)), DM(a[8], x2));
-   if (therm) {
+   if (therm && P.therm) {
       // trans_ke (src/algorith.c:221-239) of the momenta before the step
       const double *hi = P.hinv;
       double v[3];
@@ -164,20 +167,20 @@ k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restric
    if (P.nosym) {   // leapf_quat_a, src/leapfrog.c:338-392
       const double st2 = P.half / (sv * sv);   // stepdts2
       rot_axis(0.5 * st, 0, ri[0], L, q);
-      if (therm) dsm += 0.25 * st2 * ri[0] * (L[1] * L[1]) + 0.25 * st2 * ri[1] * (L[2] * L[2]);
+      if (therm && P.therm) dsm += 0.25 * st2 * ri[0] * (L[1] * L[1]) + 0.25 * st2 * ri[1] * (L[2] * L[2]);
       rot_axis(0.5 * st, 1, ri[1], L, q);
-      if (therm) dsm += 0.5 * st2 * ri[2] * (L[3] * L[3]);
+      if (therm && P.therm) dsm += 0.5 * st2 * ri[2] * (L[3] * L[3]);
       rot_axis(st, 2, ri[2], L, q);
       rot_axis(0.5 * st, 1, ri[1], L, q);
-      if (therm) dsm += 0.25 * st2 * ri[1] * (L[2] * L[2]) + 0.25 * st2 * ri[0] * (L[1] * L[1]);
+      if (therm && P.therm) dsm += 0.25 * st2 * ri[1] * (L[2] * L[2]) + 0.25 * st2 * ri[0] * (L[1] * L[1]);
       rot_axis(0.5 * st, 0, ri[0], L, q);
    } else {         // leapf_quat_b, src/leapfrog.c:253-333
       const int sx = P.saxis, o1 = P.o1, o2 = P.o2;
       rot_axis(0.5 * st, o1, DS(ri[o1], ri[o2]), L, q);
-      if (therm) dsm += 0.5 * P.half * (0.5 * rke() / (sv * sv));
+      if (therm && P.therm) dsm += 0.5 * P.half * (0.5 * rke() / (sv * sv));
       rot_axis(st, sx, DS(ri[sx], ri[o2]), L, q);
       rot_amom(st, ri[o2], L, q);
-      if (therm) dsm += 0.5 * P.half * (0.5 * rke() / (sv * sv));
+      if (therm && P.therm) dsm += 0.5 * P.half * (0.5 * rke() / (sv * sv));
       rot_axis(0.5 * st, o1, DS(ri[o1], ri[o2]), L, q);
    }
    // normalise, src/leapfrog.c:99-114
@@ -392,7 +395,7 @@ k_md_record(int *__restrict__ counter, int cap, const double *__restrict__ pe, c
       kt += kpart[2 * b];
       kr += kpart[2 * b + 1];
    }
-   if (therm)
+   if (therm && P.therm)
       for (int b = t; b < nbt; b += 128) ds += tpart[b];
    sh[0][t] = kt;
    sh[1][t] = kr;
@@ -414,13 +417,20 @@ k_md_record(int *__restrict__ counter, int cap, const double *__restrict__ pe, c
       const double s = therm[TH_S], s2 = s * s;
       ket /= s2;
       ker /= s2;
-      double smom = therm[TH_SMOM] + sh[2][0];
+      double smom = P.therm ? (therm[TH_SMOM] + sh[2][0]) + P.dsm_mid : 0.0;
       if (therm[TH_H0SET] == 0.0) {
-         therm[TH_H0] = (((ket + ker) + pe_tot) + smom * smom / (2.0 * P.Q)) + P.gkt * log(s);
+         // src/accel.c:718-727; without the thermostat its terms are zero
+         double h0 = (ket + ker) + pe_tot;
+         if (P.therm) h0 = (h0 + smom * smom / (2.0 * P.Q)) + P.gkt * log(s);
+         h0 = h0 + P.kecell;
+         if (P.baro) h0 += P.pv;
+         therm[TH_H0] = h0;
          therm[TH_H0SET] = 1.0;
       }
-      smom -= P.dt * (pe_tot - therm[TH_H0]);
-      therm[TH_SMOM] = smom;
+      if (P.therm) {
+         smom -= P.dt * (pe_tot - therm[TH_H0]);
+         therm[TH_SMOM] = smom;
+      }
    }
    const int step = *counter;
    *counter = step + 1;
@@ -463,7 +473,7 @@ k_md_therm(MdStepParams P, double *__restrict__ therm, const double *__restrict_
       nose();
       smom -= P.ahalf * (1.0 + log(s));
    } else {
-      smom += sh[0];
+      smom += sh[0] + P.dsm_end;
       smom -= P.ahalf * (1.0 + log(s));
       nose();
    }
@@ -472,6 +482,39 @@ k_md_therm(MdStepParams P, double *__restrict__ therm, const double *__restrict_
 }
 
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+
+// Kinetic part of the stress (stress_kin / energy_dyad, src/accel.c:348-356,
+// src/algorith.c:261-284): per block the sums over molecules of
+// v_i v_j / (mass s^2) with v = h^-T mom the real momenta, nine components.
+__global__ void __launch_bounds__(128)
+k_md_kedyad(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict__ mol_spec,
+            const double *__restrict__ mom, const double *__restrict__ therm, double *__restrict__ part)
+{
+   __shared__ double sh[9][128];
+   const int m = blockIdx.x * blockDim.x + threadIdx.x;
+   double d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+   if (m < P.nmols) {
+      const MdSpec &S = spec[mol_spec[m]];
+      const double s = therm ? therm[TH_S] : 1.0;
+      const double *hi = P.hinv;
+      const double x0 = mom[3 * (size_t)m], x1 = mom[3 * (size_t)m + 1], x2 = mom[3 * (size_t)m + 2];
+      double v[3];
+      v[0] = DA(DA(DM(hi[0], x0), DM(hi[3], x1)), DM(hi[6], x2));
+      v[1] = DA(DA(DM(hi[1], x0), DM(hi[4], x1)), DM(hi[7], x2));
+      v[2] = DA(DA(DM(hi[2], x0), DM(hi[5], x1)), DM(hi[8], x2));
+      const double r = 1.0 / (S.mass * (s * s));
+      for (int i = 0; i < 3; i++)
+         for (int j = 0; j < 3; j++) d[3 * i + j] = v[i] * v[j] * r;
+   }
+   for (int k = 0; k < 9; k++) sh[k][threadIdx.x] = d[k];
+   __syncthreads();
+   for (int w = 64; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w)
+         for (int k = 0; k < 9; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+      __syncthreads();
+   }
+   if (threadIdx.x < 9) part[9 * blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+}
 
 // ------------------------------------------------------------ dump records
 // Sum over sites of f (x) d, d = R(q) p the site's offset from its centre of
@@ -569,17 +612,22 @@ __global__ void k_md_dump(MdStepParams P, DumpLayout L, const MdSpec *__restrict
                           const double *__restrict__ quat, const double *__restrict__ amom,
                           const double *__restrict__ molf, const double *__restrict__ molt,
                           const double *__restrict__ small, const double *__restrict__ virc, double dist_v,
-                          double distp_v, float *__restrict__ rec)
+                          double distp_v, float *__restrict__ rec, const double *__restrict__ therm)
 {
    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+   // thermostat variable and momentum, h's momentum (1, 0, 0 at constant
+   // energy and volume)
+   const double ts = therm ? therm[TH_S] : 1.0, tsmom = (therm && P.therm) ? therm[TH_SMOM] : 0.0;
    if (m == 0) {
       if (L.h >= 0) {
          for (int k = 0; k < 9; k++) rec[L.h + k] = (float)P.h[k];
-         rec[L.h + 9] = 1.0f;
+         rec[L.h + 9] = (float)ts;
          rec[L.h + 10] = (float)(DA(DA(small[0], dist_v), small[1]));
       }
-      if (L.hmom >= 0)
-         for (int k = 0; k < 10; k++) rec[L.hmom + k] = 0.0f;
+      if (L.hmom >= 0) {
+         for (int k = 0; k < 9; k++) rec[L.hmom + k] = (float)P.hmom[k];
+         rec[L.hmom + 9] = (float)tsmom;
+      }
       if (L.st >= 0) {
          // force_calc and ewald fill the upper triangle; eval_forces mirrors
          // it, subtracts the molecular correction and adds the distant
@@ -605,21 +653,38 @@ __global__ void k_md_dump(MdStepParams P, DumpLayout L, const MdSpec *__restrict
          for (int k = 0; k < 4; k++) rec[L.quat + 4 * qi + k] = (float)quat[4 * (size_t)qi + k];
    }
    if (L.vel >= 0) {
+      // dr/dt = h^-T mom / (m s) + (1/W) hmom s_c (the second term is zero
+      // at constant volume)
       const double *x = mom + 3 * (size_t)m, *hi = P.hinv;
-      const double rm = 1.0 / S.mass;
+      const double rm = 1.0 / (S.mass * ts);
+      double hw[9];
+      for (int k = 0; k < 9; k++) hw[k] = P.baro ? DM(1.0 / P.W, P.hmom[k]) : 0.0;
       for (int i = 0; i < 3; i++) {
          const double v = DA(DA(DM(hi[i], x[0]), DM(hi[3 + i], x[1])), DM(hi[6 + i], x[2]));
-         rec[L.vel + 3 * m + i] = (float)DA(DM(v, rm), 0.0);
+         rec[L.vel + 3 * m + i] =
+            (float)DA(DA(DA(DM(v, rm), DM(hw[3 * i], s[0])), DM(hw[3 * i + 1], s[1])), DM(hw[3 * i + 2], s[2]));
       }
       if (qi >= 0)
          for (int i = 0; i < 3; i++)
-            rec[L.avel + 3 * qi + i] = (float)DM(amom[4 * (size_t)qi + i + 1], S.rinertia[i]);
+            rec[L.avel + 3 * qi + i] = (float)DM(DM(amom[4 * (size_t)qi + i + 1], 1.0 / ts), S.rinertia[i]);
    }
    if (L.frc >= 0) {
       for (int k = 0; k < 3; k++) rec[L.frc + 3 * m + k] = (float)molf[3 * (size_t)m + k];
       if (qi >= 0)
          for (int k = 0; k < 3; k++) rec[L.trq + 3 * qi + k] = (float)molt[3 * (size_t)qi + k];
    }
+}
+
+// (h^T h)^-1, the G^-1 of leapf_com (src/leapfrog.c:137-140)
+static void gram_inverse(const double *h, double *Gi)
+{
+   double ht[9], G[9];
+   for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) ht[3 * i + j] = h[3 * j + i];
+   for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+         G[3 * i + j] = ht[3 * i] * h[j] + ht[3 * i + 1] * h[3 + j] + ht[3 * i + 2] * h[6 + j];
+   inv3(G, Gi);
 }
 
 static void step_params(const mdgpu_ctx *c, MdStepParams &P)
@@ -640,11 +705,14 @@ static void step_params(const mdgpu_ctx *c, MdStepParams &P)
       for (int j = 0; j < 3; j++) P.kick[3 * i + j] = H.half * H.h[3 * j + i];
    P.half = H.half;
    P.therm = H.therm ? 1 : 0;
-   std::memcpy(P.ginv, H.ginv, sizeof P.ginv);
+   gram_inverse(H.h, P.ginv);
    P.Q = H.ttmass;
    P.gkt = H.gkt;
    P.ahalf = H.ahalf;
    P.dt = 2.0 * H.half;
+   P.baro = H.baro ? 1 : 0;
+   P.W = H.pmass;
+   std::memcpy(P.hmom, H.hmom, sizeof P.hmom);
 }
 
 }  // namespace mdgpu
@@ -670,16 +738,9 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    std::memcpy(H.h, h, sizeof H.h);
    H.half = 0.5 * dyn->step;
    H.nosym = dyn->nosymmetric_rot ? 1 : 0;
-   // leapf_com's matrix (step/(mass s)) G^-1 with G = h^T h (src/leapfrog.c:133-143)
-   double ht[9], G[9], Gi[9];
-   for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) ht[3 * i + j] = h[3 * j + i];
-   for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++)
-         G[3 * i + j] = ht[3 * i] * h[j] + ht[3 * i + 1] * h[3 + j] + ht[3 * i + 2] * h[6 + j];
-   inv3(G, Gi);
-   std::memcpy(H.ginv, Gi, sizeof H.ginv);
    H.therm = false;
+   H.baro = 0;
+   std::memset(H.hmom, 0, sizeof H.hmom);
    H.d_of_f = -3;   // start_up's count (src/startup.c:483-485, 570, 591)
    int nq = 0, m = 0, site = 0, pf0 = 0;
    H.saxis = -1;
@@ -697,8 +758,6 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
       S.pf0 = pf0;
       S.framework = sp.framework ? 1 : 0;
       if (S.framework && dyn->rdof[k] > 0) return fail(c, MDGPU_E_ARG, "a framework species cannot rotate");
-      const double sc = H.half / S.mass;
-      for (int i = 0; i < 9; i++) S.gdrift[i] = sc * Gi[i];
       const bool rot = dyn->rdof[k] > 0;
       H.d_of_f += (S.framework ? 0 : 3 * sp.nmols) + dyn->rdof[k] * sp.nmols;
       if (rot && H.saxis < 0) {
@@ -768,6 +827,10 @@ extern "C" mdgpu_status mdgpu_md_init(mdgpu_ctx *c, const mdgpu_dynamics *dyn, c
    CK(cudaMemcpyAsync(D.pf.p, c->spec_pf.data(), c->spec_pf.size() * sizeof(double), cudaMemcpyHostToDevice, st));
    CK(cudaMemcpyAsync(D.spec.p, H.spec.data(), nsp * sizeof(MdSpec), cudaMemcpyHostToDevice, st));
    CK(cudaMemsetAsync(D.err.p, 0, sizeof(int), st));
+   {
+      const double th0[4] = {1.0, 0.0, 0.0, 0.0};   // s = 1, no momentum, H_0 not evaluated
+      CK(cudaMemcpyAsync(D.therm.p, th0, sizeof th0, cudaMemcpyHostToDevice, st));
+   }
    CK(cudaStreamSynchronize(st));
    H.ready = true;
    return MDGPU_OK;
@@ -812,6 +875,203 @@ static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap
    CK(cudaGetLastError());
    c->launches += 3;
    if (th) {
+      k_md_therm<<<1, 128, 0, st>>>(P, th, D.tpart.p + nbd, nbd, 1);
+      CK(cudaGetLastError());
+      c->launches += 1;
+   }
+   return MDGPU_OK;
+}
+
+// ---- constant pressure: the cell's part of do_step, on the host (its
+// state is nine numbers and its updates need the whole system's kinetic and
+// virial stress, reduced on the device and copied back each step).
+// Matrices row-major 3x3; the operation order of src/leapfrog.c and
+// src/algorith.c, built without contraction.
+
+// cofactors of h (mk_sigma, src/algorith.c:287-294)
+static void mk_sigma_h(const double *h, double *sg)
+{
+   for (int i = 0, j = 1, k = 2; i < 3; i++, j = (j + 1) % 3, k = (k + 1) % 3)
+      for (int l = 0, m = 1, n = 2; l < 3; l++, m = (m + 1) % 3, n = (n + 1) % 3)
+         sg[3 * i + l] = h[3 * j + m] * h[3 * k + n] - h[3 * k + m] * h[3 * j + n];
+}
+
+// src/algorith.c:296-306
+static double ke_cell_h(const double *hmom, double w)
+{
+   double s = 0;
+   for (int i = 0; i < 9; i++) s += hmom[i] * hmom[i];
+   return 0.5 / w * s;
+}
+
+static double trace_sqr_h(const double *a)
+{
+   double sum = 0.0;
+   for (int i = 0; i < 9; i++) sum += a[i] * a[i];
+   return sum;
+}
+
+// leapf_hmom (src/leapfrog.c:422-437): masked elements of h's momentum held
+// at zero
+static void leapf_hmom_h(double step, double *hmom, const double *sigma, double s, double pressure, int mask)
+{
+   const double r = 0.5 * step * s * pressure;
+   for (int i = 0; i < 9; i++) {
+      if (mask & 1)
+         hmom[i] = 0;
+      else
+         hmom[i] -= r * sigma[i];
+      mask >>= 1;
+   }
+}
+
+// gleap_cell (src/leapfrog.c:474-507); the thermostat momentum's changes
+// go to *dsmom
+static void gleap_cell_h(double step, double pmass, double s, double pressure, int mask, double *h, double *hmom,
+                         double *dsmom, bool therm, bool uniform)
+{
+   double sigma[9];
+   double vol = det3(h);
+   if (uniform) {
+      leapf_hmom_h(step, hmom, h, 3.0 * vol * s / trace_sqr_h(h), pressure, mask);
+   } else {
+      mk_sigma_h(h, sigma);
+      leapf_hmom_h(step, hmom, sigma, s, pressure, mask);
+   }
+   if (therm) *dsmom -= 0.5 * step * (ke_cell_h(hmom, pmass) + pressure * vol);
+   // leapf_h (src/leapfrog.c:441-449)
+   const double r = step * s / pmass;
+   for (int i = 0; i < 9; i++) h[i] += r * hmom[i];
+   vol = det3(h);
+   if (therm) *dsmom -= 0.5 * step * (ke_cell_h(hmom, pmass) + pressure * vol);
+   if (uniform) {
+      leapf_hmom_h(step, hmom, h, 3.0 * vol * s / trace_sqr_h(h), pressure, mask);
+   } else {
+      mk_sigma_h(h, sigma);
+      leapf_hmom_h(step, hmom, sigma, s, pressure, mask);
+   }
+}
+
+// update_hmom (src/leapfrog.c:515-535): stress_part is a stress times the
+// volume
+static void update_hmom_h(double step, double s, const double *h, const double *stress_part, double *hmom,
+                          bool uniform)
+{
+   double tmp[9];
+   if (uniform) {
+      const double f = step * s * (stress_part[0] + stress_part[4] + stress_part[8]) / trace_sqr_h(h);
+      for (int i = 0; i < 9; i++) tmp[i] = f * h[i];
+   } else {
+      const double vol = det3(h);
+      double sigma[9], prod[9];
+      mk_sigma_h(h, sigma);
+      for (int i = 0; i < 3; i++)
+         for (int j = 0; j < 3; j++)
+            prod[3 * i + j] = stress_part[3 * i] * sigma[j] + stress_part[3 * i + 1] * sigma[3 + j] +
+                              stress_part[3 * i + 2] * sigma[6 + j];
+      const double f = step * s / vol;
+      for (int i = 0; i < 9; i++) tmp[i] = f * prod[i];
+   }
+   for (int i = 0; i < 9; i++) hmom[i] = hmom[i] + tmp[i];
+}
+
+// Kinetic stress (stress_kin) of the current momenta: device block sums,
+// summed here in block order.
+static mdgpu_status ke_dyad_h(mdgpu_ctx *c, const MdStepParams &P, double *dyad)
+{
+   MdDev &D = c->md;
+   cudaStream_t st = c->stream;
+   const int nbd = (c->nmols + 127) / 128;
+   k_md_kedyad<<<nbd, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mom.p, D.therm.p, D.kdpart.p);
+   CK(cudaGetLastError());
+   c->launches += 1;
+   std::vector<double> &hp = c->mdh.kpart_h;
+   hp.resize(9 * (size_t)nbd);
+   CK(cudaMemcpyAsync(hp.data(), D.kdpart.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+   CK(cudaStreamSynchronize(st));
+   for (int k = 0; k < 9; k++) dyad[k] = 0.0;
+   for (int b = 0; b < nbd; b++)
+      for (int k = 0; k < 9; k++) dyad[k] += hp[9 * (size_t)b + k];
+   return MDGPU_OK;
+}
+
+// One step of do_step under constant pressure (and, when set, constant
+// temperature), src/accel.c:673-791 in order: thermostat half step, cell
+// half step (gleap_cell), kinetic-stress half kick of h's momentum, half
+// drift, forces with the molecular virial, two half kicks and H_0, the
+// virial-stress kick of h's momentum, the second kinetic-stress half kick,
+// half drift, cell half step, thermostat half step.  Launched directly
+// (h changes every step, and with it the cell grid and the k-vector list
+// the force path rebuilds on the host).
+static mdgpu_status md_baro_step(mdgpu_ctx *c, int cap)
+{
+   MdHost &H = c->mdh;
+   MdDev &D = c->md;
+   cudaStream_t st = c->stream;
+   const int N = c->nsites, M = c->nmols, nbm = (M + 255) / 256, nbd = (M + 127) / 128;
+   const bool uni = H.baro == 2, therm = H.therm;
+   const double dt = 2.0 * H.half;
+   double *th = D.therm.p;
+   MdStepParams P;
+   step_params(c, P);
+   double ts = 1.0;
+   if (therm) {
+      k_md_therm<<<1, 128, 0, st>>>(P, th, nullptr, 0, 0);
+      CK(cudaGetLastError());
+      c->launches += 1;
+      CK(cudaMemcpyAsync(&ts, th + TH_S, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+   }
+   double dsm_mid = 0.0, dsm_end = 0.0, dyad[9];
+   gleap_cell_h(0.5 * dt, H.pmass, ts, H.pressure, H.strain_mask, H.h, H.hmom, &dsm_mid, therm, uni);
+   step_params(c, P);
+   mdgpu_status s = ke_dyad_h(c, P, dyad);
+   if (s) return s;
+   update_hmom_h(0.5 * dt, ts, H.h, dyad, H.hmom, uni);
+   k_md_drift<<<nbd, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p, D.amom.p,
+                                   D.err.p, th, D.tpart.p);
+   k_md_sites<<<(N + 255) / 256, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.cofm.p,
+                                               D.quat.p, c->site.p);
+   CK(cudaGetLastError());
+   c->launches += 2;
+   if ((s = mdgpu_forces_device(c, H.h, c->site.p, D.cofm.p, c->force.p, c->small.p, c->small.p + 2)) != MDGPU_OK)
+      return s;
+   const int nbs = (N + 255) / 256;
+   k_md_virc<<<nbs, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.quat.p, c->force.p, D.vpart.p);
+   k_md_virc2<<<1, 256, 0, st>>>(D.vpart.p, nbs, D.virc.p);
+   const double vol = det3(H.h);
+   P.kecell = ke_cell_h(H.hmom, H.pmass);
+   P.pv = H.pressure * vol;
+   P.dsm_mid = dsm_mid;
+   std::memcpy(P.hmom, H.hmom, sizeof P.hmom);
+   k_md_kick<<<nbm, 256, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.mol_site0.p, D.pf.p, c->force.p,
+                                  D.quat.p, D.mom.p, D.amom.p, D.kpart.p, D.molf.p, D.molt.p, th);
+   k_md_record<<<1, 128, 0, st>>>(D.counter.p, cap, c->small.p, D.kpart.p, nbm, H.dist / vol, c->out.p,
+                                 D.energies.p, D.err.p, P, th, D.tpart.p, nbd);
+   CK(cudaGetLastError());
+   c->launches += 4;
+   // the virial stress of eval_forces (src/accel.c:573-611): force_calc's
+   // and ewald's upper triangle mirrored, the molecular correction
+   // subtracted, the distant pressure added on the diagonal
+   double sm[11], vc[9], S[9];
+   CK(cudaMemcpyAsync(sm, c->small.p, sizeof sm, cudaMemcpyDeviceToHost, st));
+   CK(cudaMemcpyAsync(vc, D.virc.p, sizeof vc, cudaMemcpyDeviceToHost, st));
+   CK(cudaStreamSynchronize(st));
+   for (int k = 0; k < 9; k++) S[k] = sm[2 + k];
+   for (int i = 0; i < 3; i++)
+      for (int j = i + 1; j < 3; j++) S[3 * j + i] = S[3 * i + j];
+   for (int k = 0; k < 9; k++) S[k] -= vc[k];
+   for (int i = 0; i < 3; i++) S[4 * i] += H.distp / vol;
+   update_hmom_h(dt, ts, H.h, S, H.hmom, uni);
+   if ((s = ke_dyad_h(c, P, dyad)) != MDGPU_OK) return s;
+   update_hmom_h(0.5 * dt, ts, H.h, dyad, H.hmom, uni);
+   k_md_drift<<<nbd, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p, D.amom.p,
+                                   D.err.p, th, D.tpart.p + nbd);
+   CK(cudaGetLastError());
+   c->launches += 1;
+   gleap_cell_h(0.5 * dt, H.pmass, ts, H.pressure, H.strain_mask, H.h, H.hmom, &dsm_end, therm, uni);
+   if (therm) {
+      P.dsm_end = dsm_end;
       k_md_therm<<<1, 128, 0, st>>>(P, th, D.tpart.p + nbd, nbd, 1);
       CK(cudaGetLastError());
       c->launches += 1;
@@ -882,6 +1142,11 @@ static mdgpu_status md_run_impl(mdgpu_ctx *c, int nsteps, double *energies, int 
    CK(c->small.ensure(16));
    const int nrec = records && nsteps >= first ? (nsteps - first) / interval + 1 : 0;
    int batch = 0;
+   if (H.baro) {
+      CK(D.vpart.ensure(9 * (size_t)((c->nsites + 255) / 256)));
+      CK(D.virc.ensure(9));
+      CK(D.kdpart.ensure(9 * (size_t)((c->nmols + 127) / 128)));
+   }
    if (nrec > 0) {
       // device batch of records: up to 256 MiB
       batch = (int)std::min<size_t>((size_t)nrec, std::max<size_t>(1, ((size_t)64 << 20) / (size_t)dsize));
@@ -893,7 +1158,7 @@ static mdgpu_status md_run_impl(mdgpu_ctx *c, int nsteps, double *energies, int 
    }
    CK(cudaMemsetAsync(D.counter.p, 0, sizeof(int), st));
    const double vol = det3(H.h);
-   const double dist_v = H.dist / vol, distp_v = H.distp / vol;
+   double dist_v = H.dist / vol, distp_v = H.distp / vol;
    int r = 0, r_done = 0;
    for (int i = 0; i < nsteps; i++) {
       const int k = i + 1;
@@ -903,12 +1168,21 @@ static mdgpu_status md_run_impl(mdgpu_ctx *c, int nsteps, double *energies, int 
       // captured step (a step whose record needs the virial correction also
       // runs directly)
       const bool virc = dump && (level & 8);
-      const bool replay = (i > 0 || H.warm_gen == c->gen) && !c->timing && !virc;
-      if (replay && (!H.graph || H.graph_gen != c->gen || H.graph_cap != cap)) {
+      const bool replay = (i > 0 || H.warm_gen == c->gen) && !c->timing && !virc && !H.baro;
+      if (H.baro) {
+         // constant pressure: every step direct, h and the tables change
+         if ((s = md_baro_step(c, cap)) != MDGPU_OK) return s;
+         step_params(c, P);
+         const double v = det3(H.h);
+         dist_v = H.dist / v;
+         distp_v = H.distp / v;
+         c->gen++;
+      } else if (replay && (!H.graph || H.graph_gen != c->gen || H.graph_cap != cap)) {
          if ((s = md_capture(c, P, cap, dist_v)) != MDGPU_OK) return s;
          H.graph_cap = cap;
       }
-      if (replay) {
+      if (H.baro) {
+      } else if (replay) {
          CK(cudaGraphLaunch(H.graph, st));
          c->launches += H.graph_launches;
       } else {
@@ -920,7 +1194,8 @@ static mdgpu_status md_run_impl(mdgpu_ctx *c, int nsteps, double *energies, int 
          k_md_dump<<<(M + 127) / 128, 128, 0, st>>>(P, DL, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p,
                                                     D.quat.p, D.amom.p, D.molf.p, D.molt.p, c->small.p,
                                                     D.virc.p, dist_v, distp_v,
-                                                    D.rec.p + (size_t)(r % batch) * dsize);
+                                                    D.rec.p + (size_t)(r % batch) * dsize,
+                                                    (H.therm || H.baro) ? D.therm.p : nullptr);
          CK(cudaGetLastError());
          c->launches += 1;
          r++;
@@ -1007,6 +1282,9 @@ extern "C" mdgpu_status mdgpu_md_set_thermostat(mdgpu_ctx *c, int enable, double
    MdHost &H = c->mdh;
    if (!enable) {
       H.therm = false;
+      const double v[4] = {1.0, 0.0, 0.0, 0.0};
+      CK(cudaMemcpyAsync(c->md.therm.p, v, sizeof v, cudaMemcpyHostToDevice, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
       c->gen++;
       return MDGPU_OK;
    }
@@ -1035,5 +1313,47 @@ extern "C" mdgpu_status mdgpu_md_get_thermostat(mdgpu_ctx *c, double *out)
    out[0] = v[0];
    out[1] = v[1];
    out[2] = v[2];
+   return MDGPU_OK;
+}
+
+extern "C" mdgpu_status mdgpu_md_set_barostat(mdgpu_ctx *c, int mode, double pressure, double pmass, int strain_mask,
+                                              const double *hmom)
+{
+   if (!c) return MDGPU_E_ARG;
+   if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
+   MdHost &H = c->mdh;
+   if (mode == 0) {
+      H.baro = 0;
+      std::memset(H.hmom, 0, sizeof H.hmom);
+      c->gen++;
+      return MDGPU_OK;
+   }
+   if (mode != 1 && mode != 2) return fail(c, MDGPU_E_ARG, "barostat: mode 1 (anisotropic) or 2 (uniform)");
+   if (!(pmass > 0.0) || !(pressure >= 0.0))
+      return fail(c, MDGPU_E_ARG, "barostat: the cell mass must be positive, the pressure not negative");
+   if (c->ctl.molpbc) return fail(c, MDGPU_E_UNSUPPORTED, "barostat with molecular cut-offs");
+   H.baro = mode;
+   H.pressure = pressure;
+   H.pmass = pmass;
+   H.strain_mask = strain_mask;
+   if (hmom) std::memcpy(H.hmom, hmom, sizeof H.hmom);
+   else std::memset(H.hmom, 0, sizeof H.hmom);
+   // H_0 is evaluated on the next step (with the thermostat's state kept)
+   double th[4];
+   CK(cudaMemcpyAsync(th, c->md.therm.p, sizeof th, cudaMemcpyDeviceToHost, c->stream));
+   CK(cudaStreamSynchronize(c->stream));
+   th[TH_H0SET] = 0.0;
+   CK(cudaMemcpyAsync(c->md.therm.p, th, sizeof th, cudaMemcpyHostToDevice, c->stream));
+   CK(cudaStreamSynchronize(c->stream));
+   c->gen++;
+   return MDGPU_OK;
+}
+
+extern "C" mdgpu_status mdgpu_md_get_barostat(mdgpu_ctx *c, double *h, double *hmom)
+{
+   if (!c) return MDGPU_E_ARG;
+   if (!c->mdh.ready) return fail(c, MDGPU_E_ARG, "mdgpu_md_init has not been called");
+   if (h) std::memcpy(h, c->mdh.h, 9 * sizeof(double));
+   if (hmom) std::memcpy(hmom, c->mdh.hmom, 9 * sizeof(double));
    return MDGPU_OK;
 }

@@ -228,7 +228,6 @@ struct AdjDev {
 struct MdSpec {
    double mass;
    double inertia[3], rinertia[3];   // principal moments and their inverses
-   double gdrift[9];                 // (dt/2 / mass) (h^T h)^-1, leapf_com's matrix
    int nsites, pf0;                  // sites per molecule, first principal-frame site
    int framework;                    // fixed framework: momentum zeroed after the kicks
 };
@@ -248,10 +247,15 @@ struct MdHost {
    int graph_cap = 0;                // record capacity it was captured with
    uint64_t warm_gen = 0;            // configuration of the last direct step
    // constant temperature (mdgpu_md_set_thermostat)
-   double ginv[9];                   // (h^T h)^-1
    int d_of_f = 0;                   // degrees of freedom as start_up counts them
    bool therm = false;
    double temp = 0, ttmass = 0, gkt = 0, ahalf = 0;
+   // constant pressure (mdgpu_md_set_barostat): mode 1 anisotropic, 2
+   // uniform dilation; h (above) and its momentum advance on the host
+   int baro = 0, strain_mask = 0;
+   double pressure = 0, pmass = 0;
+   double hmom[9] = {0};
+   std::vector<double> kpart_h;      // host copies of block sums
 };
 
 struct MdDev {
@@ -267,6 +271,7 @@ struct MdDev {
    DBuf<float> rec;                      // batch of dump records
    DBuf<double> therm;                   // s, its momentum, H_0, H_0 evaluated
    DBuf<double> tpart;                   // block sums of the thermostat momentum's increments
+   DBuf<double> kdpart;                  // block sums of the kinetic stress (constant pressure)
 };
 
 }  // namespace mdgpu

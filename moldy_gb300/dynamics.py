@@ -164,6 +164,22 @@ class MolecularDynamics:
         self.ff._check(self.L.mdgpu_md_set_thermostat(self.ff.ctx, int(enable), float(temp), float(ttmass),
                                                       float(ts), float(tsmom)))
 
+    def set_barostat(self, mode: int, pressure: float, pmass: float, strain_mask: int = 200,
+                     hmom: Optional[np.ndarray] = None) -> None:
+        """Constant pressure (mdgpu_md_set_barostat): the Parrinello-Rahman
+        cell dynamics of do_step, mode 1 anisotropic or 2 uniform (0 off),
+        pressure and cell mass W in program units, the reference's strain
+        mask."""
+        hm = None if hmom is None else np.ascontiguousarray(hmom, np.float64).reshape(9)
+        self.ff._check(self.L.mdgpu_md_set_barostat(self.ff.ctx, int(mode), float(pressure), float(pmass),
+                                                    int(strain_mask), _dp(hm) if hm is not None else None))
+
+    def cell(self):
+        """(h, its momentum) now, [3, 3] each."""
+        h, hm = np.zeros(9), np.zeros(9)
+        self.ff._check(self.L.mdgpu_md_get_barostat(self.ff.ctx, _dp(h), _dp(hm)))
+        return h.reshape(3, 3), hm.reshape(3, 3)
+
     def thermostat(self):
         """(ts, tsmom, H_0) after the last step."""
         out = np.zeros(3)

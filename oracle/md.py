@@ -40,7 +40,7 @@ def write_mdstate(path: str, sysm, dyn, state, nsteps: int) -> None:
 
 
 def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_out=None, restart_in=None,
-        const_temp=None):
+        const_temp=None, const_pressure=None):
     """(records [nsteps, 3] = (H_0, pe[0], pe[1]) per step, final MDState,
     seconds per step).  The reference prints its notes to stdout.
 
@@ -51,7 +51,10 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_ou
     state, read back by the reference's own reader, replaces `state`.
     const_temp = (T, Q): the reference's Nose-Poincare thermostat at T (K)
     with thermostat mass Q; the records are then [nsteps, 5] = (H_0, pe[0],
-    pe[1], ts, tsmom)."""
+    pe[1], ts, tsmom).  const_pressure = (mode, pressure, W, strain_mask):
+    the reference's Parrinello-Rahman cell dynamics (mode 1 anisotropic, 2
+    uniform); the records are then [nsteps, 23], h and its momentum
+    (row-major 3x3 each) after (H_0, pe[0], pe[1], ts, tsmom)."""
     from moldy_gb300.dynamics import MDState
     exe = os.path.join(REF, "moldy_ref_md_fast" if fast else "moldy_ref_md")
     if not os.path.exists(exe):
@@ -68,6 +71,8 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_ou
             env["MOLDY_REF_RESTART_IN"] = os.path.abspath(restart_in)
         if const_temp:
             env["MOLDY_REF_CONST_TEMP"] = "%.17g %.17g" % tuple(const_temp)
+        if const_pressure:
+            env["MOLDY_REF_CONST_PRESSURE"] = "%d %.17g %.17g %d" % tuple(const_pressure)
         subprocess.run(args, check=True, cwd=d, stdout=subprocess.DEVNULL, env=env)
         raw = np.fromfile(pout, "<f8")
         files = {}
@@ -76,7 +81,7 @@ def run(sysm, dyn, state, nsteps: int, fast: bool = False, dump=None, restart_ou
                 if fn not in ("in.mdstate", "out.bin"):
                     with open(os.path.join(d, fn), "rb") as fh:
                         files[fn] = fh.read()
-    w = 5 if const_temp else 3
+    w = 23 if const_pressure else 5 if const_temp else 3
     o = w * nsteps
     rec = raw[:o].reshape(nsteps, w)
     cm = raw[o:o + 3 * nm].reshape(nm, 3)

@@ -34,6 +34,12 @@
  *     and each step's record adds the thermostat variable and momentum
  *     (H_0, pe[0], pe[1], ts, tsmom).
  *
+ * Constant pressure (the Parrinello-Rahman cell dynamics of do_step,
+ * src/accel.c:686-704, 759-783):
+ *   MOLDY_REF_CONST_PRESSURE="mode P W mask"  const-pressure mode (1
+ *     anisotropic, 2 uniform) at pressure P with cell mass W and strain mask;
+ *     each step's record then adds h and its momentum (row-major 3x3 each).
+ *
  * Restart files (the reference's own writer and reader, src/restart.c):
  *   MOLDY_REF_RESTART_OUT=path  after the run, write_restart (native
  *     format, src/restart.c:435-548) saves the whole state to path;
@@ -224,13 +230,19 @@ int main(int argc, char **argv)
    clock_gettime(CLOCK_MONOTONIC, &t0);
    {
       const char *ct = getenv("MOLDY_REF_CONST_TEMP");
+      const char *cp = getenv("MOLDY_REF_CONST_PRESSURE");
       if (ct && sscanf(ct, "%lf %lf", &control.temp, &control.ttmass) == 2) control.const_temp = 1;
+      if (cp && sscanf(cp, "%d %lf %lf %d", &control.const_pressure, &control.pressure, &control.pmass,
+                       &control.strain_mask) != 4) control.const_pressure = 0;
    }
    for (control.istep = 1; control.istep <= nsteps; control.istep++) {
-      double rec[5];
-      do_step(&sys, species, site_info, potpar, msq, pe, dip, stress, &rh, 0, control.const_temp ? 0 : 1);
+      double rec[23];
+      const int ens = control.const_temp || control.const_pressure;
+      do_step(&sys, species, site_info, potpar, msq, pe, dip, stress, &rh, 0, ens ? 0 : 1);
       rec[0] = sys.H_0; rec[1] = pe[0]; rec[2] = pe[1]; rec[3] = sys.ts; rec[4] = sys.tsmom;
-      fwrite(rec, 8, control.const_temp ? 5 : 3, o);
+      memcpy(rec + 5, sys.h, 9 * sizeof(double));
+      memcpy(rec + 14, sys.hmom, 9 * sizeof(double));
+      fwrite(rec, 8, control.const_pressure ? 23 : ens ? 5 : 3, o);
    }
    clock_gettime(CLOCK_MONOTONIC, &t1);
    if (getenv("MOLDY_REF_RESTART_OUT")) {

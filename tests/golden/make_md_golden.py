@@ -20,6 +20,10 @@ The constant-temperature fixtures (md_nvt_*) hold runs of the reference's
 Nose-Poincare thermostat (const-temp 1): per step (H_0, pe[0], pe[1], ts,
 tsmom).
 
+The constant-pressure fixtures (md_npt_*) hold runs of the reference's
+Parrinello-Rahman cell dynamics (const-pressure 1 and 2, the second with the
+thermostat): per step (H_0, pe[0], pe[1], ts, tsmom, h[3][3], hmom[3][3]).
+
 The restart fixture (md_restart_water864) holds a restart file the
 reference's write_restart saved after 10 steps from the thermal start, the
 state those steps reached, and the reference's next 10 steps from that file
@@ -110,6 +114,21 @@ def main():
             st = thermal_state(sysm, dyn, 300.0, seed)
             rec, fin, sec = md.run(sysm, dyn, st, 30, const_temp=(250.0, 1.0e4))
             save(name, sysm, dyn, st, rec, fin, sec, 300.0, seed, nvt_temp=250.0, nvt_ttmass=1.0e4)
+    if only in (None, "md_npt"):
+        # constant pressure: the reference's Parrinello-Rahman cell dynamics
+        # (const-pressure 1 with its default strain mask 200, and 2, uniform
+        # dilation, under the thermostat too); pressure 0, cell mass 1e3 in
+        # program units
+        w = S.water(nside=6, seed=3)
+        for name, seed, mode, mask, nvt in (("md_npt_water864", 17, 1, 200, None),
+                                            ("md_npt_water864_uniform_nvt", 18, 2, 0, (250.0, 1.0e4))):
+            dyn = species_dynamics(w, 0.001)
+            st = thermal_state(w, dyn, 300.0, seed)
+            rec, fin, sec = md.run(w, dyn, st, 30, const_temp=nvt, const_pressure=(mode, 0.0, 1.0e3, mask))
+            extra = dict(npt_mode=mode, npt_pressure=0.0, npt_pmass=1.0e3, npt_mask=mask)
+            if nvt:
+                extra.update(nvt_temp=nvt[0], nvt_ttmass=nvt[1])
+            save(name, w, dyn, st, rec, fin, sec, 300.0, seed, **extra)
     if only in (None, "md_restart_water864"):
         # the reference's restart file after 10 steps (its own
         # write_restart) and its continuation read back from that file

@@ -139,6 +139,47 @@ def test_thermostat_follows_reference(name, prec, tol):
         assert np.max(np.abs(st.mom - st1.mom)) <= 1e-7 * np.max(np.abs(st1.mom))
 
 
+@pytest.mark.parametrize("name", ["md_npt_water864", "md_npt_water864_uniform_nvt"])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 2e-5)])
+def test_barostat_follows_reference(name, prec, tol):
+    """Constant pressure: the reference's own do_step under const-pressure
+    (the Parrinello-Rahman cell dynamics; anisotropic with its default strain
+    mask, and uniform dilation with the thermostat) and the GPU run from the
+    same state give the same potential energies every step, the same H_0,
+    cell h and its momentum at the end, and the same final state."""
+    from moldy_gb300 import ForceField
+    from moldy_gb300.dynamics import MolecularDynamics
+    sysm, dyn, st0, st1, z = _load(name)
+    rec = z["ref_rec"]
+    ff = ForceField(sysm, precision=prec)
+    try:
+        md = MolecularDynamics(ff, dyn, st0)
+        if "nvt_temp" in z:
+            md.set_thermostat(float(z["nvt_temp"]), float(z["nvt_ttmass"]))
+        md.set_barostat(int(z["npt_mode"]), float(z["npt_pressure"]), float(z["npt_pmass"]), int(z["npt_mask"]))
+        e = md.run(len(rec))
+        ts, tsmom, H0 = md.thermostat()
+        h, hmom = md.cell()
+        st = md.state()
+    finally:
+        ff.close()
+    scale = np.abs(e[:, 0]) + np.abs(e[:, 1]) + e[:, 2] + e[:, 3]
+    assert np.all(np.abs(e[:, 0] - rec[:, 1]) <= tol * scale), np.max(np.abs(e[:, 0] - rec[:, 1]) / scale)
+    assert np.all(np.abs(e[:, 1] - rec[:, 2]) <= tol * scale)
+    assert abs(H0 - rec[0, 0]) <= tol * scale[0], (H0, rec[0, 0])
+    h_ref, hm_ref = rec[-1, 5:14].reshape(3, 3), rec[-1, 14:23].reshape(3, 3)
+    h0 = np.asarray(sysm.h)
+    # the cell's change and its momentum, relative to their own size
+    assert np.max(np.abs((h - h0) - (h_ref - h0))) <= max(tol, 1e-6) * np.max(np.abs(h_ref - h0)) * 10 + 1e-13
+    assert np.max(np.abs(hmom - hm_ref)) <= max(tol, 1e-6) * np.max(np.abs(hm_ref)) * 10
+    assert np.all(np.tril(h, -1) == 0.0)
+    if "nvt_temp" in z:
+        assert abs(ts - rec[-1, 3]) <= tol * abs(rec[-1, 3] - 1.0) + 1e-12, (ts, rec[-1, 3])
+    d = st.c_of_m - st1.c_of_m
+    d -= np.round(d)
+    assert np.max(np.abs(d)) < (1e-9 if prec == "fp64" else 1e-6)
+
+
 def test_md_run_needs_init():
     from moldy_gb300 import ForceField, system
     from moldy_gb300._lib import MdgpuError
