@@ -1,6 +1,7 @@
-// Constant-energy rigid-molecule dynamics on the GPU: the step of do_step
-// (src/accel.c:626-827) without thermostat or barostat, all in FP64 and all
-// on the device, so a run of many steps moves no per-step data to the host.
+// Rigid-molecule dynamics on the GPU: the step of do_step (src/accel.c:626-827),
+// all in FP64 and, at constant volume, all on the device, so a run of many
+// steps moves no per-step data to the host.  The Nose-Poincare thermostat and
+// the Parrinello-Rahman cell are described with their kernels below.
 //
 // One step (the symplectic leapfrog of src/leapfrog.c):
 //   k_md_drift   half-step of the centres of mass (leapf_com,
@@ -9,8 +10,9 @@
 //                angular momenta (leapf_quat, src/leapfrog.c:246-392: the
 //                Dullweber-Leimkuhler-McLachlan rotational splitting,
 //                symmetric-top variant unless nosymmetric_rot)
-//   k_md_sites   site co-ordinates from centres of mass and quaternions
-//                (make_sites, src/algorith.c:169-215)
+//                the first half step also writes the site co-ordinates from
+//                the new centres of mass and quaternions (make_sites,
+//                src/algorith.c:169-215), one thread per molecule
 //   forces       the force path of this library (real space + k space)
 //   k_md_kick    molecular forces and principal-frame torques (mol_force,
 //                mol_torque, src/algorith.c:111-160), two half kicks of the
@@ -81,16 +83,65 @@ __device__ __forceinline__ void qconjmul(const double *p, const double *q, doubl
 // rot = (cos a, sin a along `axis`), a = 0.5 step rinertia amom[axis+1]
 // (make_rot, src/leapfrog.c:206-219), then amom <- rot^-1 amom rot,
 // quat <- quat rot (rot_substep, src/leapfrog.c:236-243).
+// The products of rot_substep with rot = (c, s along one axis): qmul's
+// terms with a zero factor left out (adding or subtracting a zero product
+// leaves every nonzero value unchanged, so the results are qmul's), the
+// remaining terms in qmul's order.  a = axis + 1.
+//   r = (c - s e_a) * q   (q_conj_mul of rot and q)
+__device__ __forceinline__ void qmul_conjrot_left(double c, double s, int a, const double *q, double *r)
+{
+   const double p0 = c, pa = -s;
+   const double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+   if (a == 1) {
+      r[0] = DS(DM(p0, q0), DM(pa, q1));
+      r[1] = DA(DM(pa, q0), DM(p0, q1));
+      r[2] = DS(DM(p0, q2), DM(pa, q3));
+      r[3] = DA(DM(pa, q2), DM(p0, q3));
+   } else if (a == 2) {
+      r[0] = DS(DM(p0, q0), DM(pa, q2));
+      r[1] = DA(DM(p0, q1), DM(pa, q3));
+      r[2] = DA(DM(pa, q0), DM(p0, q2));
+      r[3] = DS(DM(p0, q3), DM(pa, q1));
+   } else {
+      r[0] = DS(DM(p0, q0), DM(pa, q3));
+      r[1] = DS(DM(p0, q1), DM(pa, q2));
+      r[2] = DA(DM(pa, q1), DM(p0, q2));
+      r[3] = DA(DM(pa, q0), DM(p0, q3));
+   }
+}
+//   r = p * (c + s e_a)
+__device__ __forceinline__ void qmul_rot_right(const double *p, double c, double s, int a, double *r)
+{
+   const double p0 = p[0], p1 = p[1], p2 = p[2], p3 = p[3], q0 = c, qa = s;
+   if (a == 1) {
+      r[0] = DS(DM(p0, q0), DM(p1, qa));
+      r[1] = DA(DM(p1, q0), DM(p0, qa));
+      r[2] = DA(DM(p2, q0), DM(p3, qa));
+      r[3] = DS(DM(p3, q0), DM(p2, qa));
+   } else if (a == 2) {
+      r[0] = DS(DM(p0, q0), DM(p2, qa));
+      r[1] = DS(DM(p1, q0), DM(p3, qa));
+      r[2] = DA(DM(p2, q0), DM(p0, qa));
+      r[3] = DA(DM(p3, q0), DM(p1, qa));
+   } else {
+      r[0] = DS(DM(p0, q0), DM(p3, qa));
+      r[1] = DA(DM(p1, q0), DM(p2, qa));
+      r[2] = DS(DM(p2, q0), DM(p1, qa));
+      r[3] = DA(DM(p3, q0), DM(p0, qa));
+   }
+}
+
 __device__ __forceinline__ void rot_axis(double step, int axis, double rin, double *amom, double *quat)
 {
    const double angle = DM(DM(DM(0.5, step), rin), amom[axis + 1]);
    double sa, ca;
    sincos(angle, &sa, &ca);
-   double rot[4] = {ca, 0.0, 0.0, 0.0};
-   rot[axis + 1] = sa;
-   qconjmul(rot, amom, amom);
-   qmul(amom, rot, amom);
-   qmul(quat, rot, quat);
+   const int a = axis + 1;
+   double t[4];
+   qmul_conjrot_left(ca, sa, a, amom, t);
+   qmul_rot_right(t, ca, sa, a, amom);
+   qmul_rot_right(quat, ca, sa, a, t);
+   for (int k = 0; k < 4; k++) quat[k] = t[k];
 }
 
 // Rotation about the angular momentum by 0.5 step rinertia |L|
@@ -106,6 +157,67 @@ __device__ __forceinline__ void rot_amom(double step, double rin, const double *
    qmul(quat, rot, quat);
 }
 
+// Rotation matrix of a quaternion (q_to_rot, src/quaterns.c:129-160).
+__device__ __forceinline__ void q_to_rot(const double *q, double *r)
+{
+   const double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+   const double a01 = DM(DM(2.0, q0), q1), a02 = DM(DM(2.0, q0), q2), a03 = DM(DM(2.0, q0), q3);
+   const double a12 = DM(DM(2.0, q1), q2), a13 = DM(DM(2.0, q1), q3), a23 = DM(DM(2.0, q2), q3);
+   r[1] = DS(a12, a03);
+   r[2] = DA(a13, a02);
+   r[3] = DA(a12, a03);
+   r[5] = DS(a23, a01);
+   r[6] = DS(a13, a02);
+   r[7] = DA(a23, a01);
+   const double s0 = DM(q0, q0), s1 = DM(q1, q1), s2 = DM(q2, q2), s3 = DM(q3, q3);
+   r[0] = DS(DS(DA(s0, s1), s2), s3);
+   r[4] = DS(DA(DS(s0, s1), s2), s3);
+   r[8] = DA(DS(DS(s0, s1), s2), s3);
+}
+
+__device__ __forceinline__ void matvec(const double *m, double a0, double a1, double a2, double *o)
+{
+   o[0] = DA(DA(DM(m[0], a0), DM(m[1], a1)), DM(m[2], a2));
+   o[1] = DA(DA(DM(m[3], a0), DM(m[4], a1)), DM(m[5], a2));
+   o[2] = DA(DA(DM(m[6], a0), DM(m[7], a1)), DM(m[8], a2));
+}
+
+// Site co-ordinates of one molecule (make_sites, src/algorith.c:169-215):
+// site = R(q) p + h s, wrapped into the cell unless molecular cut-offs are
+// in use.  q null: a molecule without rotational freedom.
+__device__ __forceinline__ void mol_sites(const MdStepParams &P, const double *c_s, const double *q, int nsites,
+                                          const double *__restrict__ pf, int site0, double *__restrict__ site)
+{
+   const int N = P.nsites;
+   double c[3], R[9];
+   matvec(P.h, c_s[0], c_s[1], c_s[2], c);
+   if (q) q_to_rot(q, R);
+   for (int t = 0; t < nsites; t++) {
+      const double *p = pf + 3 * t;
+      double r[3];
+      if (q) {
+         matvec(R, p[0], p[1], p[2], r);
+      } else {
+         r[0] = p[0];
+         r[1] = p[1];
+         r[2] = p[2];
+      }
+      double x = DA(r[0], c[0]), y = DA(r[1], c[1]), z = DA(r[2], c[2]);
+      if (!P.molpbc) {
+         const double *hi = P.hinv, *h = P.h;
+         const double tx = floor(DA(DA(DA(DM(hi[0], x), DM(hi[1], y)), DM(hi[2], z)), 0.5));
+         const double ty = floor(DA(DA(DA(DM(hi[3], x), DM(hi[4], y)), DM(hi[5], z)), 0.5));
+         const double tz = floor(DA(DA(DA(DM(hi[6], x), DM(hi[7], y)), DM(hi[8], z)), 0.5));
+         x = DS(x, DA(DA(DM(h[0], tx), DM(h[1], ty)), DM(h[2], tz)));
+         y = DS(y, DA(DA(DM(h[3], tx), DM(h[4], ty)), DM(h[5], tz)));
+         z = DS(z, DA(DA(DM(h[6], tx), DM(h[7], ty)), DM(h[8], tz)));
+      }
+      site[site0 + t] = x;
+      site[N + site0 + t] = y;
+      site[2 * (size_t)N + site0 + t] = z;
+   }
+}
+
 // Half step of the co-ordinates (leapf_all_coords, src/accel.c:360-372).
 // Under the thermostat (therm non-null) the steps are scaled by its
 // variable s, and each block writes to tpart its share of the thermostat
@@ -117,7 +229,9 @@ __global__ void __launch_bounds__(128)
 k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restrict__ mol_spec,
            const int *__restrict__ mol_q, double *__restrict__ cofm, const double *__restrict__ mom,
            double *__restrict__ quat, double *__restrict__ amom, int *__restrict__ err,
-           const double *__restrict__ therm, double *__restrict__ tpart)
+           const double *__restrict__ therm, double *__restrict__ tpart,
+           const int *__restrict__ mol_site0 = nullptr, const double *__restrict__ pf = nullptr,
+           double *__restrict__ site = nullptr)
 {
    __shared__ double sh[128];
    const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -188,10 +302,17 @@ k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restric
    for (int k = 0; k < 4; k++) norm = DA(norm, DM(q[k], q[k]));
    norm = sqrt(norm);
    if (fabs(norm - 1.0) > QNORM_TOL) atomicOr(err, 2);
+   double qn[4];
    for (int k = 0; k < 4; k++) {
-      quat[4 * (size_t)qi + k] = q[k] / norm;
+      qn[k] = q[k] / norm;
+      quat[4 * (size_t)qi + k] = qn[k];
       amom[4 * (size_t)qi + k] = L[k];
    }
+   // the step's sites from the new centre of mass and orientation (the
+   // values stored above), when the force evaluation follows
+   if (site) mol_sites(P, c, qn, S.nsites, pf + 3 * (size_t)S.pf0, mol_site0[m], site);
+   } else if (site) {
+      mol_sites(P, c, nullptr, S.nsites, pf + 3 * (size_t)S.pf0, mol_site0[m], site);
    }
    }
    if (!therm) return;
@@ -203,70 +324,6 @@ k_md_drift(MdStepParams P, const MdSpec *__restrict__ spec, const int *__restric
       __syncthreads();
    }
    if (threadIdx.x == 0) tpart[blockIdx.x] = sh[0];
-}
-
-// Rotation matrix of a quaternion (q_to_rot, src/quaterns.c:129-160).
-__device__ __forceinline__ void q_to_rot(const double *q, double *r)
-{
-   const double q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
-   const double a01 = DM(DM(2.0, q0), q1), a02 = DM(DM(2.0, q0), q2), a03 = DM(DM(2.0, q0), q3);
-   const double a12 = DM(DM(2.0, q1), q2), a13 = DM(DM(2.0, q1), q3), a23 = DM(DM(2.0, q2), q3);
-   r[1] = DS(a12, a03);
-   r[2] = DA(a13, a02);
-   r[3] = DA(a12, a03);
-   r[5] = DS(a23, a01);
-   r[6] = DS(a13, a02);
-   r[7] = DA(a23, a01);
-   const double s0 = DM(q0, q0), s1 = DM(q1, q1), s2 = DM(q2, q2), s3 = DM(q3, q3);
-   r[0] = DS(DS(DA(s0, s1), s2), s3);
-   r[4] = DS(DA(DS(s0, s1), s2), s3);
-   r[8] = DA(DS(DS(s0, s1), s2), s3);
-}
-
-__device__ __forceinline__ void matvec(const double *m, double a0, double a1, double a2, double *o)
-{
-   o[0] = DA(DA(DM(m[0], a0), DM(m[1], a1)), DM(m[2], a2));
-   o[1] = DA(DA(DM(m[3], a0), DM(m[4], a1)), DM(m[5], a2));
-   o[2] = DA(DA(DM(m[6], a0), DM(m[7], a1)), DM(m[8], a2));
-}
-
-// One thread per site: site = R(q) p + h s (make_sites), wrapped into the
-// cell unless molecular cutoffs are in use.
-__global__ void k_md_sites(MdStepParams P, const int *__restrict__ site_mol, const int *__restrict__ site_pf,
-                           const double *__restrict__ pf, const int *__restrict__ mol_q,
-                           const double *__restrict__ cofm, const double *__restrict__ quat,
-                           double *__restrict__ site)
-{
-   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-   const int N = P.nsites;
-   if (i >= N) return;
-   const int m = site_mol[i];
-   double c[3], r[3];
-   matvec(P.h, cofm[3 * (size_t)m], cofm[3 * (size_t)m + 1], cofm[3 * (size_t)m + 2], c);
-   const double *p = pf + 3 * (size_t)site_pf[i];
-   const int qi = mol_q[m];
-   if (qi >= 0) {
-      double R[9];
-      q_to_rot(quat + 4 * (size_t)qi, R);
-      matvec(R, p[0], p[1], p[2], r);
-   } else {
-      r[0] = p[0];
-      r[1] = p[1];
-      r[2] = p[2];
-   }
-   double x = DA(r[0], c[0]), y = DA(r[1], c[1]), z = DA(r[2], c[2]);
-   if (!P.molpbc) {
-      const double *hi = P.hinv, *h = P.h;
-      const double tx = floor(DA(DA(DA(DM(hi[0], x), DM(hi[1], y)), DM(hi[2], z)), 0.5));
-      const double ty = floor(DA(DA(DA(DM(hi[3], x), DM(hi[4], y)), DM(hi[5], z)), 0.5));
-      const double tz = floor(DA(DA(DA(DM(hi[6], x), DM(hi[7], y)), DM(hi[8], z)), 0.5));
-      x = DS(x, DA(DA(DM(h[0], tx), DM(h[1], ty)), DM(h[2], tz)));
-      y = DS(y, DA(DA(DM(h[3], tx), DM(h[4], ty)), DM(h[5], tz)));
-      z = DS(z, DA(DA(DM(h[6], tx), DM(h[7], ty)), DM(h[8], tz)));
-   }
-   site[i] = x;
-   site[N + i] = y;
-   site[2 * N + i] = z;
 }
 
 // One thread per molecule: force and principal-frame torque from the site
@@ -849,12 +906,11 @@ static mdgpu_status md_enqueue_step(mdgpu_ctx *c, const MdStepParams &P, int cap
       k_md_therm<<<1, 128, 0, st>>>(P, th, nullptr, 0, 0);
       c->launches += 1;
    }
+   // half drift, and the sites of the force evaluation from its result
    k_md_drift<<<nbd, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p, D.amom.p,
-                                   D.err.p, th, D.tpart.p);
-   k_md_sites<<<(N + 255) / 256, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.cofm.p,
-                                               D.quat.p, c->site.p);
+                                   D.err.p, th, D.tpart.p, D.mol_site0.p, D.pf.p, c->site.p);
    CK(cudaGetLastError());
-   c->launches += 2;
+   c->launches += 1;
    mdgpu_status s = mdgpu_forces_device(c, H.h, c->site.p, D.cofm.p, c->force.p, c->small.p, c->small.p + 2);
    if (s) return s;
    if (virc) {
@@ -1028,12 +1084,11 @@ static mdgpu_status md_baro_step(mdgpu_ctx *c, int cap)
    mdgpu_status s = ke_dyad_h(c, P, dyad);
    if (s) return s;
    update_hmom_h(0.5 * dt, ts, H.h, dyad, H.hmom, uni);
+   // half drift, and the sites of the force evaluation from its result
    k_md_drift<<<nbd, 128, 0, st>>>(P, D.spec.p, D.mol_spec.p, D.mol_q.p, D.cofm.p, D.mom.p, D.quat.p, D.amom.p,
-                                   D.err.p, th, D.tpart.p);
-   k_md_sites<<<(N + 255) / 256, 256, 0, st>>>(P, D.site_mol.p, D.site_pf.p, D.pf.p, D.mol_q.p, D.cofm.p,
-                                               D.quat.p, c->site.p);
+                                   D.err.p, th, D.tpart.p, D.mol_site0.p, D.pf.p, c->site.p);
    CK(cudaGetLastError());
-   c->launches += 2;
+   c->launches += 1;
    if ((s = mdgpu_forces_device(c, H.h, c->site.p, D.cofm.p, c->force.p, c->small.p, c->small.p + 2)) != MDGPU_OK)
       return s;
    const int nbs = (N + 255) / 256;

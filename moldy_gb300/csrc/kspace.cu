@@ -407,6 +407,31 @@ k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__
 // Per-block energy/stress partials summed in a fixed order by one block
 // (any multiple of 32 threads up to 1024): thread t takes blocks t, t + T,
 // ..., then fixed-shape warp and cross-warp trees.
+// First level of the k-space energy/stress sum when there are many per-k
+// blocks: block b sums the contiguous slice b of the block records (fixed
+// order), so the single-block final sum below reads only gridDim.x
+// records (one SM's FP64 adds were the cost of a one-level sum).
+constexpr int KF_PARTS = 64;   // first-level blocks of the k-space energy/stress sum
+
+__global__ void __launch_bounds__(128) k_kfinal_part(const double *__restrict__ blk, int nblocks,
+                                                     double *__restrict__ blk2)
+{
+   __shared__ double sh[4][8];
+   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+   const int per = (nblocks + gridDim.x - 1) / gridDim.x;
+   const int b0 = blockIdx.x * per, b1 = min(nblocks, b0 + per);
+   double v[7] = {0, 0, 0, 0, 0, 0, 0};
+   for (int b = b0 + t; b < b1; b += blockDim.x)
+      for (int k = 0; k < 7; k++) v[k] += blk[b * 8 + k];
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1)
+      for (int k = 0; k < 7; k++) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+   if (lane == 0)
+      for (int k = 0; k < 7; k++) sh[w][k] = v[k];
+   __syncthreads();
+   if (t < 7) blk2[blockIdx.x * 8 + t] = ((sh[0][t] + sh[1][t]) + sh[2][t]) + sh[3][t];
+}
+
 __global__ void __launch_bounds__(1024) k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *out)
 {
    __shared__ double sh[32][8];
@@ -1084,7 +1109,14 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       k_kreduce<false><<<nbk, KR_K * KR_W, 0, st>>>(nk, sh.chunks, nullptr, d.part64.p, d.kz64.p, d.coeff.p,
                                             d.coeff2.p, nullptr, d.kdat64.p, d.blk.p);
    }
-   k_kfinal<<<1, 512, 0, st>>>(d.blk.p, nbk, out);
+   if (nbk > 4 * KF_PARTS) {
+      CK(d.blk2.ensure(8 * (size_t)KF_PARTS));
+      k_kfinal_part<<<KF_PARTS, 128, 0, st>>>(d.blk.p, nbk, d.blk2.p);
+      k_kfinal<<<1, 512, 0, st>>>(d.blk2.p, KF_PARTS, out);
+      c->launches += 1;
+   } else {
+      k_kfinal<<<1, 512, 0, st>>>(d.blk.p, nbk, out);
+   }
    CK(cudaGetLastError());
    if (tc) {
       sh.splits = ks_force_tc_splits(Nk);

@@ -180,6 +180,7 @@ struct KsDev {
    DBuf<double2> part64;
    DBuf<double> fpart;     // [splits][3][N] force partials
    DBuf<double> blk;       // per-block energy/stress partials
+   DBuf<double> blk2;      // their first-level sums
    // framework molecule: framework-charge channel, its structure factor,
    // negated framework coefficients, its sites' records held compactly
    DBuf<int> fslot, sortedc;
