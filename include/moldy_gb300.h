@@ -27,7 +27,8 @@ typedef enum {
    MDGPU_OK = 0,
    MDGPU_E_ARG = 1,          /* invalid argument or call order                   */
    MDGPU_E_CUDA = 2,         /* a CUDA runtime call failed                       */
-   MDGPU_E_UNSUPPORTED = 3,  /* option outside the implemented path (frameworks,
+   MDGPU_E_UNSUPPORTED = 3,  /* option outside the implemented path (a framework
+                                species listed before another species,
                                 non-upper-triangular h)                          */
    MDGPU_E_CUTOFF = 4,       /* neighbour cells beyond one image: the reference's
                                 FATAL CUTOFF (src/force.c:203-206)               */
@@ -50,7 +51,7 @@ typedef enum {
 typedef struct {
    int nsites;                  /* sites per molecule                         */
    int nmols;                   /* molecules of this species                  */
-   int framework;               /* nonzero: framework species (unsupported)   */
+   int framework;               /* nonzero: framework species (last, 1 mol.)  */
    const int *site_id;          /* [nsites] site identifiers (1..max_id-1)    */
    const double *p_f_sites;     /* [nsites][3] principal-frame co-ordinates   */
 } mdgpu_species;
@@ -223,7 +224,9 @@ mdgpu_status mdgpu_ewald_kspace_noalloc(const double *h, int nsites, const doubl
  * and its gradient sum_i 2 weight (F_i - f_ref_i) . dF_i/dtheta comes from
  * Hessian-vector products through the real-space pairs (their link-cell walk
  * recomputed, no stored pair list) and the k-space sum.  Both calls run the
- * forward evaluation first, in the context's precision.  Limits: max_id <=
+ * forward evaluation first, in the context's precision.  A framework
+ * molecule is handled as the forward path handles it: no framework-framework
+ * terms, its net charge in the sheet term.  Limits: max_id <=
  * MDGPU_ADJ_MAX_ID; in strict-cutoff mode no molecule may be larger than the
  * cutoff (MDGPU_E_UNSUPPORTED otherwise). */
 #define MDGPU_NPOTP 8

@@ -27,6 +27,16 @@
 // forward's structure-factor kernel with the weights in place of the
 // charges.  The self and sheet terms are added on the host
 // (ewald_self_sheet_grad).
+//
+// With a framework molecule (sites fw0.. N-1) the forward leaves out the
+// framework-framework part: E_k = sum_k c (|S|^2 - |S_f|^2)/2 and
+// G = sum_k c ((C Ts - S Tc) - (C_f Ts_f - S_f Tc_f)), S = S_n + S_f and
+// T = T_n + T_f split into the non-framework (n) and framework (f) sites.
+// A non-framework site's dE/dq and dG/dq keep the forms above with the
+// whole S and T; a framework site's take S_n and T_n in their place.  Both
+// are linear in (A, B, P, Q), so every site is first given the whole-sum
+// form and the framework sites then a second pass with the framework's
+// coefficients negated, as the forward corrects the framework forces.
 #include <cstring>
 
 #include "mdgpu_internal.h"
@@ -119,57 +129,102 @@ __global__ void k_adj_channels(int N, int mixed, const int4 *__restrict__ ph32, 
    }
 }
 
+// The framework sites' residual weights in the compacted order of the
+// forward's framework records (site fw0 + i at row i; fslot[i] its slot).
+__global__ void k_adj_fw_res(int nf, const int *__restrict__ fslot, int mixed, const float4 *__restrict__ res32,
+                             const double4 *__restrict__ res64, float4 *__restrict__ resc32,
+                             double4 *__restrict__ resc64)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= nf) return;
+   const int p = fslot[i];
+   if (mixed)
+      resc32[i] = res32[p];
+   else
+      resc64[i] = res64[p];
+}
+
+// gq[comp][fw0 + r] += sum over splits of part[split][comp][r], r < nf
+__global__ void k_adj_gsum_fw(int nf, int N, int fw0, int nsplit, const double *__restrict__ part,
+                              double *__restrict__ gq)
+{
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= 2 * nf) return;
+   double s = 0.0;
+   for (int k = 0; k < nsplit; k++) s += part[(size_t)k * 2 * nf + i];
+   const int comp = i / nf, r = i - comp * nf;
+   gq[(size_t)comp * N + fw0 + r] += s;
+}
+
 // Per k: structure factors summed over chunks in FP64 (fixed order), the
-// alpha derivatives, and the per-k coefficients of the per-site pass.
+// alpha derivatives, and the per-k coefficients of the per-site pass.  The
+// weighted partials pv hold the x, y, z planes; with a framework (fw) p and
+// pv hold the non-framework sites' sums, pf and pv's planes 3..5 the
+// framework's, and kdf receives the framework coefficients negated.
 template <bool MIXED>
 __global__ void __launch_bounds__(256)
-k_adj_kreduce(int nk, int nchunks, int loss, const float2 *__restrict__ p32, const float2 *__restrict__ pv32,
-              const double2 *__restrict__ p64, const double2 *__restrict__ pv64,
+k_adj_kreduce(int nk, int nchunks, int loss, int fw, const float2 *__restrict__ p32,
+              const float2 *__restrict__ pf32, const float2 *__restrict__ pv32, const double2 *__restrict__ p64,
+              const double2 *__restrict__ pf64, const double2 *__restrict__ pv64,
               const double *__restrict__ kvec /*[3][nk]*/, const double *__restrict__ coeff, double alpha,
-              float4 *__restrict__ kd32, float *__restrict__ kz32, double4 *__restrict__ kd64,
-              double *__restrict__ blk)
+              float4 *__restrict__ kd32, float4 *__restrict__ kdf32, float *__restrict__ kz32,
+              double4 *__restrict__ kd64, double4 *__restrict__ kdf64, double *__restrict__ blk)
 {
    __shared__ double sh[256];
    const int k = blockIdx.x * blockDim.x + threadIdx.x;
    double ea = 0.0, la = 0.0;
    if (k < nk) {
-      double S[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+      // channel 0: S; 1..3: the weighted x, y, z sums; 4..7 the same over
+      // the framework sites
+      double S[8][2] = {};
       const size_t plane = (size_t)nchunks * nk;
       const int nch = loss ? 4 : 1;
-      for (int ch = 0; ch < nch; ch++)
-         for (int c = 0; c < nchunks; c++) {
-            const size_t o = (size_t)c * nk + k;
-            double x, y;
-            if (MIXED) {
-               const float2 v = ch == 0 ? p32[o] : pv32[(ch - 1) * plane + o];
-               x = v.x;
-               y = v.y;
-            } else {
-               const double2 v = ch == 0 ? p64[o] : pv64[(ch - 1) * plane + o];
-               x = v.x;
-               y = v.y;
+      for (int g = 0; g < (fw ? 2 : 1); g++)
+         for (int ch = 0; ch < nch; ch++)
+            for (int c = 0; c < nchunks; c++) {
+               const size_t o = (size_t)c * nk + k;
+               const size_t ov = ch > 0 ? (size_t)(3 * g + ch - 1) * plane + o : 0;
+               double x, y;
+               if (MIXED) {
+                  const float2 v = ch > 0 ? pv32[ov] : g ? pf32[o] : p32[o];
+                  x = v.x;
+                  y = v.y;
+               } else {
+                  const double2 v = ch > 0 ? pv64[ov] : g ? pf64[o] : p64[o];
+                  x = v.x;
+                  y = v.y;
+               }
+               S[4 * g + ch][0] += x;
+               S[4 * g + ch][1] += y;
             }
-            S[ch][0] += x;
-            S[ch][1] += y;
-         }
       const double kx = kvec[k], ky = kvec[nk + k], kz = kvec[2 * nk + k];
       const double cf = coeff[k];
       const double dcf = cf * (kx * kx + ky * ky + kz * kz) / (2.0 * alpha * alpha * alpha);
-      const double C = S[0][0], Sn = S[0][1];
-      ea = 0.5 * dcf * (C * C + Sn * Sn);
-      double P = 0.0, Q = 0.0;
+      const double Cn = S[0][0], Sn = S[0][1], Cf = S[4][0], Sf = S[4][1];
+      const double C = Cn + Cf, Sv = Sn + Sf;
+      // |S|^2 - |S_f|^2 without the cancellation
+      ea = 0.5 * dcf * (Cn * (Cn + Cf + Cf) + Sn * (Sn + Sf + Sf));
+      double P = 0.0, Q = 0.0, Pf = 0.0, Qf = 0.0;
       if (loss) {
-         const double Tc = kx * S[1][0] + ky * S[2][0] + kz * S[3][0];
-         const double Ts = kx * S[1][1] + ky * S[2][1] + kz * S[3][1];
-         la = dcf * (C * Ts - Sn * Tc);
+         const double Tcn = kx * S[1][0] + ky * S[2][0] + kz * S[3][0];
+         const double Tsn = kx * S[1][1] + ky * S[2][1] + kz * S[3][1];
+         const double Tcf = kx * S[5][0] + ky * S[6][0] + kz * S[7][0];
+         const double Tsf = kx * S[5][1] + ky * S[6][1] + kz * S[7][1];
+         const double Tc = Tcn + Tcf, Ts = Tsn + Tsf;
+         // (C Ts - S Tc) - (C_f Ts_f - S_f Tc_f)
+         la = dcf * (Cn * Ts + Cf * Tsn - Sn * Tc - Sf * Tcn);
          P = cf * Tc;
          Q = cf * Ts;
+         Pf = -cf * Tcf;
+         Qf = -cf * Tsf;
       }
       if (MIXED) {
-         kd32[k] = make_float4((float)(cf * C), (float)(cf * Sn), (float)P, (float)Q);
+         kd32[k] = make_float4((float)(cf * C), (float)(cf * Sv), (float)P, (float)Q);
+         if (fw) kdf32[k] = make_float4((float)(-cf * Cf), (float)(-cf * Sf), (float)Pf, (float)Qf);
          kz32[k] = (float)kz;
       } else {
-         kd64[k] = make_double4(cf * C, cf * Sn, P, Q);
+         kd64[k] = make_double4(cf * C, cf * Sv, P, Q);
+         if (fw) kdf64[k] = make_double4(-cf * Cf, -cf * Sf, Pf, Qf);
       }
    }
    ea = block_sum256(ea, sh);
@@ -192,7 +247,9 @@ __global__ void k_adj_kfinal(const double *__restrict__ blk, int nblocks, double
 constexpr int AD_ITEMS = 64;     // k-vector items per shared-memory tile
 constexpr int AD_THREADS = 128;
 
-// Per site (slot), over the items of one split: dE/dq and dG/dq partials.
+// Per site (slot), over the items of one split: dE/dq and dG/dq partials,
+// written to row sorted[i] of the split's [2][N] block (row i when sorted
+// is null: the framework sites' compacted records).
 // Mixed form: the forward's phases (32-bit fixed point, polynomial seeds,
 // exact per-site tables exp(2 pi i t s_z)), FP32 terms summed in short
 // plain runs and Kahan-compensated across runs.
@@ -278,7 +335,7 @@ k_adj_site32(const int4 *__restrict__ item, const int *__restrict__ item_k0, con
    kahan(se, ce, pe);
    kahan(sl, cl, pl);
    if (live) {
-      const int oi = sorted[i];
+      const int oi = sorted ? sorted[i] : i;
       double *dst = gpart + (size_t)blockIdx.y * 2 * N;
       dst[oi] = (double)se - (double)ce;
       dst[N + oi] = (double)sl - (double)cl;
@@ -352,7 +409,7 @@ k_adj_site64(const int4 *__restrict__ item, const int *__restrict__ item_k0, con
       }
    }
    if (live) {
-      const int oi = sorted[i];
+      const int oi = sorted ? sorted[i] : i;
       double *dst = gpart + (size_t)blockIdx.y * 2 * N;
       dst[oi] = ge;
       dst[N + oi] = gl;
@@ -372,6 +429,11 @@ static mdgpu_status ks_adjoint(mdgpu_ctx *c, bool loss)
    cudaStream_t st = c->stream;
    const int N = c->nsites, nk = kl.nk, ni = kl.nitems;
    const bool mixed = c->prec == MDGPU_MIXED;
+   // framework sites fw0..N-1: the forward has split the charges of the
+   // per-slot records into the non-framework (ph) and framework (phf)
+   // channels and left the framework sites' records compacted
+   const int fw0 = c->fw_site0, nf = N - fw0;
+   const bool fw = nf > 0;
    if (nk == 0) {
       CK(cudaMemsetAsync(a.scal.p + 1, 0, 2 * sizeof(double), st));
       return MDGPU_OK;
@@ -380,40 +442,51 @@ static mdgpu_status ks_adjoint(mdgpu_ctx *c, bool loss)
    const KsShape sh = ks_shape(N, ni, 1, 1);
    const size_t plane = (size_t)sh.chunks * nk;
    if (loss) {
+      const int ngroups = fw ? 2 : 1;   // weighted channels of n (or all) sites, then f sites
       if (mixed) {
-         CK(a.phv32.ensure(3 * (size_t)N));
-         CK(a.partv32.ensure(3 * plane));
+         CK(a.phv32.ensure(3 * (size_t)ngroups * N));
+         CK(a.partv32.ensure(3 * (size_t)ngroups * plane));
       } else {
-         CK(a.phv64.ensure(3 * (size_t)N));
-         CK(a.partv64.ensure(3 * plane));
+         CK(a.phv64.ensure(3 * (size_t)ngroups * N));
+         CK(a.partv64.ensure(3 * (size_t)ngroups * plane));
       }
-      k_adj_channels<<<(N + 255) / 256, 256, 0, st>>>(N, mixed ? 1 : 0, d.ph32.p, a.res32.p, d.ph64b.p, a.res64.p,
-                                                      a.phv32.p, a.phv64.p);
       const dim3 g((ni + 127) / 128, sh.chunks);
-      for (int ch = 0; ch < 3; ch++) {
-         if (mixed)
-            k_sfac32<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, a.phv32.p + (size_t)ch * N, d.zp32.p, N,
-                                        sh.chunk, nk, a.partv32.p + ch * plane, &c->out.p->err);
-         else
-            k_sfac64<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, a.phv64.p + (size_t)ch * N, d.z64.p,
-                                        N, sh.chunk, nk, a.partv64.p + ch * plane);
+      for (int grp = 0; grp < ngroups; grp++) {
+         const size_t vo = (size_t)3 * grp * N;
+         k_adj_channels<<<(N + 255) / 256, 256, 0, st>>>(N, mixed ? 1 : 0, grp ? d.phf32.p : d.ph32.p, a.res32.p,
+                                                         grp ? d.phf64b.p : d.ph64b.p, a.res64.p,
+                                                         a.phv32.p + (mixed ? vo : 0),
+                                                         a.phv64.p + (mixed ? 0 : vo));
+         for (int ch = 0; ch < 3; ch++) {
+            const size_t po = (size_t)(3 * grp + ch) * plane;
+            if (mixed)
+               k_sfac32<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, a.phv32.p + vo + (size_t)ch * N, d.zp32.p,
+                                           N, sh.chunk, nk, a.partv32.p + po, &c->out.p->err);
+            else
+               k_sfac64<<<g, 128, 0, st>>>(d.item.p, d.item_k0.p, ni, d.ph64a.p, a.phv64.p + vo + (size_t)ch * N,
+                                           d.z64.p, N, sh.chunk, nk, a.partv64.p + po);
+         }
       }
       CK(cudaGetLastError());
-      c->launches += 4;
+      c->launches += 4 * ngroups;
    }
    const int nbk = (nk + 255) / 256;
    CK(a.blk.ensure(2 * (size_t)nbk));
    if (mixed) {
       CK(a.kadj32.ensure(nk));
       CK(a.kz32.ensure(nk));
-      k_adj_kreduce<true><<<nbk, 256, 0, st>>>(nk, sh.chunks, loss ? 1 : 0, d.part32.p, a.partv32.p, nullptr,
-                                               nullptr, d.kz64.p, d.coeff.p, c->ctl.alpha, a.kadj32.p, a.kz32.p,
-                                               nullptr, a.blk.p);
+      if (fw) CK(a.kadjf32.ensure(nk));
+      k_adj_kreduce<true><<<nbk, 256, 0, st>>>(nk, sh.chunks, loss ? 1 : 0, fw ? 1 : 0, d.part32.p,
+                                               fw ? d.partf32.p : nullptr, a.partv32.p, nullptr, nullptr,
+                                               nullptr, d.kz64.p, d.coeff.p, c->ctl.alpha, a.kadj32.p,
+                                               a.kadjf32.p, a.kz32.p, nullptr, nullptr, a.blk.p);
    } else {
       CK(a.kadj64.ensure(nk));
-      k_adj_kreduce<false><<<nbk, 256, 0, st>>>(nk, sh.chunks, loss ? 1 : 0, nullptr, nullptr, d.part64.p,
-                                                a.partv64.p, d.kz64.p, d.coeff.p, c->ctl.alpha, nullptr, nullptr,
-                                                a.kadj64.p, a.blk.p);
+      if (fw) CK(a.kadjf64.ensure(nk));
+      k_adj_kreduce<false><<<nbk, 256, 0, st>>>(nk, sh.chunks, loss ? 1 : 0, fw ? 1 : 0, nullptr, nullptr,
+                                                nullptr, d.part64.p, fw ? d.partf64.p : nullptr, a.partv64.p,
+                                                d.kz64.p, d.coeff.p, c->ctl.alpha, nullptr, nullptr, nullptr,
+                                                a.kadj64.p, a.kadjf64.p, a.blk.p);
    }
    k_adj_kfinal<<<1, 32, 0, st>>>(a.blk.p, nbk, a.scal.p);
    CK(a.gkpart.ensure((size_t)sh.splits * 2 * N));
@@ -429,13 +502,35 @@ static mdgpu_status ks_adjoint(mdgpu_ctx *c, bool loss)
    k_fsum<<<(2 * N + 255) / 256, 256, 0, st>>>(2 * N, sh.splits, a.gkpart.p, a.gq.p, 1);
    CK(cudaGetLastError());
    c->launches += 4;
+   if (fw) {
+      // the framework sites again, with the framework's coefficients negated
+      const KsShape shf = ks_shape(nf, ni, 1, 1);
+      CK(a.gkpartf.ensure((size_t)shf.splits * 2 * nf));
+      if (loss) {
+         if (mixed) CK(a.resc32.ensure(nf)); else CK(a.resc64.ensure(nf));
+         k_adj_fw_res<<<(nf + 255) / 256, 256, 0, st>>>(nf, d.fslot.p, mixed ? 1 : 0, a.res32.p, a.res64.p,
+                                                        a.resc32.p, a.resc64.p);
+         c->launches += 1;
+      }
+      const dim3 gf((nf + AD_THREADS - 1) / AD_THREADS, shf.splits);
+      if (mixed)
+         k_adj_site32<<<gf, AD_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, shf.per_split,
+                                                 a.kadjf32.p, a.kz32.p, d.phc32.p, d.zpc32.p, a.resc32.p,
+                                                 nullptr, nf, loss ? 1 : 0, a.gkpartf.p);
+      else
+         k_adj_site64<<<gf, AD_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy64.p, ni, nk, shf.per_split,
+                                                 a.kadjf64.p, d.kz64.p, d.pac64.p, d.pbc64.p, d.zc64.p,
+                                                 a.resc64.p, nullptr, nf, loss ? 1 : 0, a.gkpartf.p);
+      k_adj_gsum_fw<<<(2 * nf + 255) / 256, 256, 0, st>>>(nf, N, fw0, shf.splits, a.gkpartf.p, a.gq.p);
+      CK(cudaGetLastError());
+      c->launches += 2;
+   }
    return MDGPU_OK;
 }
 
 // Checks the adjoint's limits for the current system and control record.
 static mdgpu_status adjoint_supported(mdgpu_ctx *c)
 {
-   if (c->fw_mol >= 0) return fail(c, MDGPU_E_UNSUPPORTED, "adjoint: framework molecules are not supported");
    if (c->max_id > MDGPU_ADJ_MAX_ID)
       return fail(c, MDGPU_E_UNSUPPORTED, "adjoint: more than MDGPU_ADJ_MAX_ID site identifiers");
    if (pot_nparams(c->ptype) == 0)

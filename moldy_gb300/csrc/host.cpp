@@ -593,26 +593,37 @@ static double as_derfc(double x)
 
 // Gradient of the energy terms ewald() adds besides the k sum,
 // -self + sheet/V (src/ewald.c:367-433): with respect to each site charge
-// (added into g_chg[nsites]) and alpha (added into *g_alpha).  The
-// intramolecular part of the self energy is taken per molecule with its own
-// charges (the reference evaluates the first molecule of each species, whose
-// charges every molecule of the species shares).
+// (added into g_chg[nsites]) and alpha (added into *g_alpha).  The self
+// energy covers the species before the framework, if any
+// (src/ewald.c:372-397); its intramolecular part is taken per molecule with
+// its own charges (the reference evaluates the first molecule of each
+// species, whose charges every molecule of the species shares).  A
+// framework's net charge q_f adds pi q_f^2 / (2 alpha^2) to the sheet term
+// (src/ewald.c:405-413); a net system charge sq subtracts pi sq^2 / (2
+// alpha^2) (src/ewald.c:417-422).
 void ewald_self_sheet_grad(const std::vector<mdgpu_species> &spec, const std::vector<double> &spec_pf,
                            const std::vector<double> &chg, double alpha, double vol, double *g_chg,
                            double *g_alpha)
 {
    const double rpi = 1.0 / std::sqrt(PI);
-   double ga = 0.0, sq = 0.0;
-   size_t isite = 0, so = 0;
+   double ga = 0.0, sq = 0.0, qf = 0.0;
+   size_t isite = 0, so = 0, fw0 = chg.size();
+   bool in_fw = false;
    for (const auto &sp : spec) {
       const int ns = sp.nsites;
       const double *pf = spec_pf.data() + 3 * so;
+      in_fw = in_fw || sp.framework;
+      if (in_fw && fw0 == chg.size()) fw0 = isite;
       for (int m = 0; m < sp.nmols; m++) {
          const double *q = chg.data() + isite;
          for (int a = 0; a < ns; a++) {
+            sq += q[a];
+            if (in_fw) {
+               qf += q[a];
+               continue;
+            }
             g_chg[isite + a] -= 2.0 * alpha * rpi * q[a];
             ga -= rpi * q[a] * q[a];
-            sq += q[a];
             for (int b = a + 1; b < ns; b++) {
                const double *u = pf + 3 * a, *v = pf + 3 * b;
                const double r = std::sqrt((u[0] - v[0]) * (u[0] - v[0]) + (u[1] - v[1]) * (u[1] - v[1]) +
@@ -627,8 +638,13 @@ void ewald_self_sheet_grad(const std::vector<mdgpu_species> &spec, const std::ve
       }
       so += ns;
    }
+   if (in_fw) {   // sheet += pi q_f^2 / (2 alpha^2)
+      const double dq = PI * qf / (alpha * alpha * vol);
+      for (size_t i = fw0; i < isite; i++) g_chg[i] += dq;
+      ga -= PI * qf * qf / (alpha * alpha * alpha * vol);
+   }
    const double conv_q = (4.07497263794495e-14 * 1.0e-3 * 1.05482230112e-05) / 1.60217733e-19;
-   if (std::fabs(sq) * conv_q > 1.0e-5) {   // sheet = -pi (sum q)^2 / (2 alpha^2)
+   if (std::fabs(sq) * conv_q > 1.0e-5) {   // sheet -= pi (sum q)^2 / (2 alpha^2)
       const double dq = -PI * sq / (alpha * alpha * vol);
       for (size_t i = 0; i < isite; i++) g_chg[i] += dq;
       ga += PI * sq * sq / (alpha * alpha * alpha * vol);

@@ -98,10 +98,16 @@ double det3(const double *a);
 void inv3(const double *a, double *b);
 
 // ---- device buffers ----------------------------------------------------------
+// Owned by the context: freed by release() or when the context is deleted
+// (on its device: mdgpu_destroy selects it first).
 template <typename T>
 struct DBuf {
    T *p = nullptr;
    size_t n = 0;
+   DBuf() = default;
+   DBuf(const DBuf &) = delete;
+   DBuf &operator=(const DBuf &) = delete;
+   ~DBuf() { release(); }
    cudaError_t ensure(size_t want) {
       if (want <= n && p) return cudaSuccess;
       if (p) cudaFree(p);
@@ -215,11 +221,18 @@ struct AdjDev {
    DBuf<double> scal;      // loss, k-space dE/dalpha, dG/dalpha
    DBuf<double> lpart;     // per-block loss partials
    DBuf<int4> phv32;       // [3][N] mixed-form phases with weight q v_a
+                           // ([6][N] with a framework: its sites' weights after)
    DBuf<ulonglong2> phv64; // [3][N] (u_z, weight q v_a) for the FP64 form
    DBuf<float2> partv32;   // [3][chunks][nk] weighted structure-factor partials
+                           // ([6][chunks][nk] with a framework)
    DBuf<double2> partv64;
    DBuf<float4> kadj32;    // per k: A, B, P, Q
    DBuf<double4> kadj64;
+   DBuf<float4> kadjf32;   // per k: the framework sites' A, B, P, Q, negated
+   DBuf<double4> kadjf64;
+   DBuf<float4> resc32;    // the framework sites' residual weights, compacted
+   DBuf<double4> resc64;
+   DBuf<double> gkpartf;   // [splits][2][nf] framework correction partials
    DBuf<float> kz32;       // per k: k_z
    DBuf<double> gkpart;    // [splits][2][N] k-space charge-gradient partials
    DBuf<double> blk;       // per-block k-space dE/dalpha, dG/dalpha

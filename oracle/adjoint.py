@@ -13,8 +13,10 @@ oracle/port):
   with erfc by the A&S 7.1.26 polynomial (src/kernel.c:182-186) and the
   force factor (erfc(a r)/r + 2a/sqrt(pi) exp(-a^2 r^2))/r^2;
 * the k-space sum of ewald() (src/ewald.c:495-566) over the half sphere,
-  coeff_k = 8 pi/V exp(-k^2/4a^2)/k^2 (src/ewald.c:510);
-* the self and sheet terms (src/ewald.c:367-433).
+  coeff_k = 8 pi/V exp(-k^2/4a^2)/k^2 (src/ewald.c:510), without the
+  framework-framework part when a framework molecule is present;
+* the self and sheet terms (src/ewald.c:367-433), the charged-framework
+  sheet term included.
 
 Conventions (the GPU library's): the gradient entry [a, b, k] of the
 potential table is the derivative with respect to potpar[a*max_id + b][k] as
@@ -155,15 +157,34 @@ def kvectors(sysm) -> Tuple[np.ndarray, np.ndarray]:
     return kv, coeff
 
 
-def _self_sheet_grad(sysm, gq: np.ndarray) -> float:
-    """Adds d(-self + sheet/V)/dq_i into gq; returns d/dalpha."""
-    alpha = sysm.control.alpha
-    q = sysm.chg()
-    rpi = 1.0 / math.sqrt(math.pi)
-    ga = -rpi * float(np.sum(q * q))
-    gq -= 2.0 * alpha * rpi * q
+def _framework_mask(sysm) -> np.ndarray:
+    """True for the sites of the framework species (the last species, one
+    molecule; src/force.c:1215-1222)."""
+    m = np.zeros(sysm.nsites, bool)
     base = 0
     for sp in sysm.species:
+        n = sp.nsites * sp.nmols
+        m[base:base + n] = bool(sp.framework)
+        base += n
+    return m
+
+
+def _self_sheet_grad(sysm, gq: np.ndarray) -> float:
+    """Adds d(-self + sheet/V)/dq_i into gq; returns d/dalpha.  The self
+    energy covers the species before the framework (src/ewald.c:372-397); a
+    framework's net charge q_f adds pi q_f^2/(2 alpha^2) to the sheet term
+    (src/ewald.c:405-413), a net system charge sq subtracts pi sq^2/(2
+    alpha^2) (src/ewald.c:417-422)."""
+    alpha = sysm.control.alpha
+    q = sysm.chg()
+    fw = _framework_mask(sysm)
+    rpi = 1.0 / math.sqrt(math.pi)
+    ga = -rpi * float(np.sum(q[~fw] * q[~fw]))
+    gq[~fw] -= 2.0 * alpha * rpi * q[~fw]
+    base = 0
+    for sp in sysm.species:
+        if sp.framework:
+            break
         ns, pf = sp.nsites, np.asarray(sp.p_f_sites, np.float64)
         for a in range(ns):
             for b in range(a + 1, ns):
@@ -175,9 +196,13 @@ def _self_sheet_grad(sysm, gq: np.ndarray) -> float:
                 gq[ib] -= q[ia] * e
                 ga += float(np.sum(q[ia] * q[ib])) * float(_as_derfc(alpha * r))
         base += ns * sp.nmols
+    vol = sysm.volume()
+    if fw.any():
+        qf = float(np.sum(q[fw]))
+        gq[fw] += math.pi * qf / (alpha * alpha * vol)
+        ga -= math.pi * qf * qf / (alpha ** 3 * vol)
     sq = float(np.sum(q))
     if abs(sq) * CONV_Q > 1e-5:
-        vol = sysm.volume()
         gq += -math.pi * sq / (alpha * alpha * vol)
         ga += math.pi * sq * sq / (alpha ** 3 * vol)
     return ga
@@ -251,24 +276,34 @@ def gradients(sysm, f_ref=None, weight: float = 1.0) -> Tuple[float, Dict[str, n
             np.add.at(gq, j, np.where(inter, q[i] * uc, 0.0))
             parts[0] = float(np.sum(np.where(inter, q[i] * q[j] * duc, 0.0)))
 
-    # ---- reciprocal space
+    # ---- reciprocal space.  With a framework molecule the framework-
+    # framework part |S_f|^2 is left out (src/ewald.c:528-579): non-framework
+    # sites see the whole S(k), framework sites the non-framework part only.
     if ew:
         kv, cf = kvectors(sysm)
         ksq = np.sum(kv * kv, 1)
         dcf = cf * ksq / (2.0 * alpha ** 3)
+        fw = _framework_mask(sysm)
         ph = x.T @ kv.T                  # [N, nk]
         cs, sn = np.cos(ph), np.sin(ph)
         C, S = q @ cs, q @ sn
+        Cf, Sf = q[fw] @ cs[fw], q[fw] @ sn[fw]
         A, B = cf * C, cf * S
+        Af, Bf = cf * Cf, cf * Sf
         if loss:
             kvv = v.T @ kv.T             # k . v_i
             Tc, Ts = (q[:, None] * kvv * cs).sum(0), (q[:, None] * kvv * sn).sum(0)
+            Tcf = (q[fw, None] * kvv[fw] * cs[fw]).sum(0)
+            Tsf = (q[fw, None] * kvv[fw] * sn[fw]).sum(0)
             P, Q = cf * Tc, cf * Ts
+            Pf, Qf = cf * Tcf, cf * Tsf
             gq += cs @ Q - sn @ P + np.sum(kvv * (A * sn - B * cs), 1)
-            parts[1] = float(np.sum(dcf * (C * Ts - S * Tc)))
+            gq[fw] -= cs[fw] @ Qf - sn[fw] @ Pf + np.sum(kvv[fw] * (Af * sn[fw] - Bf * cs[fw]), 1)
+            parts[1] = float(np.sum(dcf * (C * Ts - S * Tc - (Cf * Tsf - Sf * Tcf))))
         else:
             gq += cs @ A + sn @ B
-            parts[1] = float(np.sum(0.5 * dcf * (C * C + S * S)))
+            gq[fw] -= cs[fw] @ Af + sn[fw] @ Bf
+            parts[1] = float(np.sum(0.5 * dcf * (C * C + S * S - Cf * Cf - Sf * Sf)))
             parts[2] = _self_sheet_grad(sysm, gq)
     ga = parts[0] + parts[1] + parts[2]
     return value, {"potpar": gp, "chg": gq, "alpha": ga, "alpha_parts": parts}

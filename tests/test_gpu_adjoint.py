@@ -13,7 +13,8 @@ from conftest import GOLDEN
 pytestmark = pytest.mark.gpu
 
 CASES = ["syn_water864_strict", "syn_water864_molpbc", "syn_water864_mcy", "ex_mgclh2o", "ex_quartz",
-         "syn_generic216", "syn_hiw216", "syn_morse216", "syn_argon500_strict", "syn_rocksalt512"]
+         "syn_generic216", "syn_hiw216", "syn_morse216", "syn_argon500_strict", "syn_rocksalt512", "ex_clay",
+         "syn_waterwall"]
 
 # FP64: the oracle's own rounding level.  Mixed: FP32 pair and k-space
 # arithmetic; the bar for the fitted gradients is 1e-4 relative.
@@ -27,7 +28,11 @@ ATOL = {"fp64": 1e-10, "mixed": 5e-6}
 
 
 def _load(name):
+    """A golden fixture, or syn_waterwall: 245 rigid waters over a neutral
+    checkerboard framework of 64 sites (charges +-0.4 e), built in place."""
     from moldy_gb300 import system
+    if name == "syn_waterwall":
+        return system.water_on_framework()
     return system.load_npz(os.path.join(GOLDEN, name + ".npz"))[0]
 
 
