@@ -938,6 +938,7 @@ mdgpu_status ks_prepare(mdgpu_ctx *c)
       CK(cudaMemcpyAsync(d.tc_item.p, kl.tc_item.data(), nt * sizeof(int4), cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(d.tc_k0.p, kl.tc_k0.data(), nt * sizeof(int4), cudaMemcpyHostToDevice, st));
       CK(cudaStreamSynchronize(st));
+      d.tc_ver++;
       c->kl_uploaded = true;
    }
    if (c->prec == MDGPU_MIXED && c->tc_sfac) {
@@ -1128,7 +1129,11 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    dim3 gf((Nk + 255) / 256, sh.splits);
    const int obase = compact ? -1 : 0;   // partial rows by slot of the charged list, or by site
    if (tc) {
-      ks_force_tc(st, Nk, d, (int)kl.tc_item.size(), c->rd.chg.p, slots, d.fpart.p, &out->err);
+      if (c->nsm <= 0) CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
+      const int nl = ks_force_tc(st, Nk, d, (int)kl.tc_item.size(), c->nsm, c->rd.chg.p, slots, d.fpart.p,
+                                 &out->err);
+      if (nl < 0) return fail(c, MDGPU_E_NOMEM, "device allocation failed (force-pass work ranges)");
+      c->launches += nl - 1;
    } else if (mixed)
       k_force32<<<gf, FT_THREADS, 0, st>>>(d.item.p, d.item_k0.p, d.item_kxy32.p, ni, nk, sh.per_split,
                                            d.kdat32.p, d.ph32.p, d.zp32.p, c->rd.chg.p, slots, Nk, obase,

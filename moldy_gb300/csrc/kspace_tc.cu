@@ -33,11 +33,12 @@
 // CTA roles (608 threads): warps 0-15 build the A operand of each 32-site
 // stage (one item row and 8 sites per thread) and, at the end, read the
 // accumulators back (a warp reaches tensor-memory lanes 32 (w % 4) ..);
-// warp 16 copies the chunk's site records once and streams each stage's z
-// tables (bulk copies, three in flight); warp 17 owns the tensor memory and
-// issues the Ar MMAs, warp 18 the Ai MMAs.  A operands are double-buffered,
-// z tables triple-buffered, on mbarriers; every wait is bounded and sets
-// bit 3 of the error word when it expires.
+// warp 16 streams each stage's z tables and its 32 site records (bulk
+// copies, three stages in flight); warp 17 owns the tensor memory and
+// issues the Ar MMAs, warp 18 the Ai MMAs.  A operands and z tables are
+// triple-buffered on mbarriers, so the A operand of a stage is built while
+// the MMAs of the two before it run; every wait is bounded and sets bit 3
+// of the error word when it expires.
 #include <atomic>
 #include <cmath>
 
@@ -48,21 +49,22 @@
 namespace mdgpu {
 
 constexpr int TC_KS = 32;                          // sites per stage (two MMA K-steps of 16)
-constexpr int TC_NSA = 2;                          // A-operand buffers
+constexpr int TC_NSA = 3;                          // A-operand buffers
 constexpr int TC_NSB = 3;                          // z-table buffers (bulk copies in flight)
 constexpr int TC_TERM = 128 * TC_KS * 2;           // one 128-row bf16 operand of a stage: 8 KB
 constexpr int TC_ABYTES = 6 * TC_TERM;             // Ar, Ai x (hi, mid, lo)
 constexpr int TC_BBYTES = 3 * TC_TERM;             // [Zr | Zi] x (hi, mid, lo)
 constexpr int TC_CHUNK = 1024;                     // sites per CTA (one partial per k)
-constexpr int TC_PBYTES = TC_CHUNK * 16;           // the chunk's site records (u_x, u_y, u_z, q)
-constexpr int TC_AOFF = TC_PBYTES, TC_BOFF = TC_AOFF + TC_NSA * TC_ABYTES;
-constexpr int TC_SMEM = TC_BOFF + TC_NSB * TC_BBYTES;
+constexpr int TC_PBYTES = TC_KS * 16;              // a stage's site records (u_x, u_y, u_z, q)
+constexpr int TC_AOFF = 0, TC_BOFF = TC_AOFF + TC_NSA * TC_ABYTES, TC_POFF = TC_BOFF + TC_NSB * TC_BBYTES;
+constexpr int TC_SMEM = TC_POFF + TC_NSB * TC_PBYTES;
 constexpr int TC_LBO = 16 * 128;                   // 8-column groups of a 128-row operand
 constexpr int TC_ERR = 8;                          // error-word bit: a stage wait expired
 constexpr int TC_AW = 16;                          // operand / read-back warps
 constexpr int TC_THREADS = 32 * (TC_AW + 3);       // and a bulk-copy warp, two MMA warps
 
-static_assert(TC_AOFF % 1024 == 0 && TC_BOFF % 1024 == 0, "operand buffers stay aligned");
+static_assert(TC_AOFF % 1024 == 0 && TC_BOFF % 1024 == 0 && TC_POFF % 16 == 0, "operand buffers stay aligned");
+static_assert(TC_SMEM <= 227 * 1024, "one CTA's shared memory");
 static_assert(TC_CHUNK % TC_KS == 0, "chunks hold whole stages");
 static_assert(KT == 4 * KI && KT <= 64, "an item is four KI runs, Zr and Zi fit 128 rows");
 
@@ -119,7 +121,7 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
 {
    using namespace tc;
    extern __shared__ __align__(1024) unsigned char sm[];
-   __shared__ __align__(8) uint64_t full_p, full_b[TC_NSB], empty_b[TC_NSB], full_a[TC_NSA], empty_a[TC_NSA], accf;
+   __shared__ __align__(8) uint64_t full_b[TC_NSB], empty_b[TC_NSB], full_a[TC_NSA], empty_a[TC_NSA], accf;
    __shared__ unsigned int tmem_s;
    __shared__ int abort_s;
    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -129,7 +131,6 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
    const int ncols = (item[tile * 128].w + 15) & ~15;   // the tile's largest count, rounded up
    if (ncols == 0 || nst <= 0) return;                  // (uniform over the CTA)
    if (tid == 0) {
-      bar_init(&full_p, 1);
       for (int s = 0; s < TC_NSB; s++) {
          bar_init(&full_b[s], 1);
          bar_init(&empty_b[s], 2);   // released by both MMA issuers
@@ -150,10 +151,8 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
    const unsigned int tmem = tmem_s;
 
    if (w == TC_AW) {
-      // ---- bulk copies: the chunk's site records once, each stage's z tables
+      // ---- bulk copies: each stage's z tables and site records
       if (lane == 0) {
-         bar_expect_tx(&full_p, (unsigned int)nst * TC_KS * 16);
-         bulk_load(sm, ph + s0, (unsigned int)nst * TC_KS * 16, &full_p);
          int issued = 0;
          for (int st = 0; st < nst; st++) {
             const int s = st % TC_NSB;
@@ -162,13 +161,13 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
                break;
             }
             if (tc_aborted(&abort_s)) break;
-            bar_expect_tx(&full_b[s], TC_BBYTES);
+            bar_expect_tx(&full_b[s], TC_BBYTES + TC_PBYTES);
             bulk_load(sm + TC_BOFF + s * TC_BBYTES, ztab + (size_t)(s0 / TC_KS + st) * (TC_BBYTES / 16), TC_BBYTES,
                       &full_b[s]);
+            bulk_load(sm + TC_POFF + s * TC_PBYTES, ph + s0 + st * TC_KS, TC_PBYTES, &full_b[s]);
             issued = st + 1;
          }
          // copies still in flight complete before the CTA's shared memory goes
-         bar_wait(&full_p, 0);
          for (int st = issued > TC_NSB ? issued - TC_NSB : 0; st < issued; st++)
             bar_wait(&full_b[st % TC_NSB], (unsigned int)(st / TC_NSB) & 1u);
       }
@@ -208,16 +207,16 @@ k_sfac_tc(const int4 *__restrict__ item, const int4 *__restrict__ item_k0, const
       const int m = tid & 127, qq = tid >> 7;
       const int4 hd = item[tile * 128 + m];
       const unsigned int H = (unsigned int)hd.x, K = (unsigned int)hd.y, L = (unsigned int)hd.z;
-      if (!bar_wait(&full_p, 0)) tc_abort(&abort_s, err);
       for (int st = 0; st < nst; st++) {
-         const int s = st % TC_NSA;
+         const int s = st % TC_NSA, sb = st % TC_NSB;
          if (tc_aborted(&abort_s)) break;
-         if (st >= TC_NSA && !bar_wait(&empty_a[s], (unsigned int)(st / TC_NSA - 1) & 1u)) {
+         if ((st >= TC_NSA && !bar_wait(&empty_a[s], (unsigned int)(st / TC_NSA - 1) & 1u)) ||
+             !bar_wait(&full_b[sb], (unsigned int)(st / TC_NSB) & 1u)) {
             tc_abort(&abort_s, err);
             break;
          }
          unsigned char *A = sm + TC_AOFF + s * TC_ABYTES;
-         const int4 *P = reinterpret_cast<const int4 *>(sm) + st * TC_KS + 8 * qq;
+         const int4 *P = reinterpret_cast<const int4 *>(sm + TC_POFF + sb * TC_PBYTES) + 8 * qq;
          unsigned int hr[4], mr[4], lr[4], hi[4], mi[4], li[4];
 #pragma unroll
          for (int jp = 0; jp < 4; jp++) {
@@ -345,10 +344,10 @@ constexpr int FTC_BBYTES = 3 * FTC_BTERM;          // 12 KB
 constexpr int FTC_EG = 4;                          // epilogue warps per tensor-memory lane quarter
 constexpr int FTC_IPW = FTC_NI / FTC_EG;           // items of a tile per epilogue warp
 constexpr int FTC_EW = 4 * FTC_EG;                 // epilogue warps
-constexpr int FTC_SMEM = FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + FTC_EG * 128 * 3 * 4 + FTC_EW * FTC_IPW * 32;
+constexpr int FTC_SMEM = FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + 2 * FTC_EG * 128 * 3 * 4 + FTC_EW * FTC_IPW * 32;
 constexpr int FTC_THREADS = 32 * (FTC_EW + 4);     // epilogue warps, two bulk-copy warps, two MMA warps
 static_assert(FTC_IPW % 4 == 0, "an epilogue warp reads its items' columns 16 at a time");
-constexpr int FTC_SPLITS = 2;                      // item-tile ranges per site tile (grid.y)
+constexpr int FTC_SPLITS = 2;                      // force slots per site (two CTAs at most per site tile)
 constexpr int FTC_ERR = 16;                        // error-word bit: a force-pass wait expired
 
 // Site tiles' z tables as the A operand: [tile][term][column group 16][row
@@ -463,29 +462,75 @@ __device__ __forceinline__ void kahan_add_tc(float &s, float &c, float x)
    s = t;
 }
 
-// Grid: (site tiles of 128, FTC_SPLITS ranges of item tiles).
+// Work ranges of the persistent force pass.  Unit u is (site tile u / ntl,
+// item tile u % ntl); CTA c takes units ustart[c] .. ustart[c + 1] - 1, a
+// contiguous run over the site tiles.  The runs split the units' weights
+// (an item tile's K-steps plus one for its epilogue) evenly over G CTAs,
+// with G <= the number of site tiles (or G = twice that, each CTA then half
+// a tile), so no run lies strictly inside a site tile and a tile is shared
+// by two CTAs at most.  One block; pre (after ustart[G]) holds the prefix
+// weights of the item tiles.
+__global__ void k_ftc_ranges(const int4 *__restrict__ item, int ntl, int nsite_tiles, int G, int *__restrict__ ustart)
+{
+   int *pre = ustart + G + 1;
+   if (threadIdx.x == 0) {
+      int sum = 0;
+      pre[0] = 0;
+      for (int t = 0; t < ntl; t++) {
+         sum += 2 * ((item[t * FTC_NI].w + 15) >> 4) + 1;
+         pre[t + 1] = sum;
+      }
+   }
+   __syncthreads();
+   const long long wt = pre[ntl], wall = wt * nsite_tiles;
+   for (int c = threadIdx.x; c <= G; c += blockDim.x) {
+      const long long target = (long long)c * wall / G;
+      const long long tile = target / wt, rem = target - tile * wt;
+      int lo = 0, hi = ntl;   // the first item tile whose prefix weight reaches rem
+      while (lo < hi) {
+         const int mid = (lo + hi) >> 1;
+         if (pre[mid] >= rem)
+            hi = mid;
+         else
+            lo = mid + 1;
+      }
+      ustart[c] = (int)(tile * ntl + lo);
+   }
+}
+
+// Persistent: one CTA per work range (k_ftc_ranges).  Per site tile of the
+// range the CTA loads its z tables once (after the MMAs of the previous tile
+// have completed) and runs its item tiles as before; the epilogue writes the
+// tile's forces into slot 0 of fpart, or slot 1 when the range starts inside
+// the tile (and zeros into slot 1 when the range covers the whole tile).
 __global__ void __launch_bounds__(FTC_THREADS, 1)
 k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int nitems,
            const int4 *__restrict__ ph, const uint4 *__restrict__ zsite, const uint4 *__restrict__ utab,
-           const double *__restrict__ chg, const int *__restrict__ slots, int n, double *__restrict__ fpart,
-           int *__restrict__ err)
+           const double *__restrict__ chg, const int *__restrict__ slots, int n, const int *__restrict__ ustart,
+           double *__restrict__ fpart, int *__restrict__ err)
 {
    using namespace tc;
    extern __shared__ __align__(1024) unsigned char sm[];
-   __shared__ __align__(8) uint64_t full_a, full_b[2][FTC_NSB], empty_b[2][FTC_NSB], acc_full[2], acc_empty[2], done[2];
+   __shared__ __align__(8) uint64_t full_a, a_free, full_b[2][FTC_NSB], empty_b[2][FTC_NSB], acc_full[2],
+       acc_empty[2], done[2];
    __shared__ unsigned int tmem_s;
    __shared__ int abort_s;
    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-   const int tile = blockIdx.x;
-   const int ntiles = nitems / FTC_NI;
-   const int per = (ntiles + gridDim.y - 1) / gridDim.y;
-   const int nt0 = blockIdx.y * per, nt1 = min(ntiles, nt0 + per);
+   const int ntl = nitems / FTC_NI;   // item tiles per site tile
+   const int u0 = ustart[blockIdx.x], u1 = ustart[blockIdx.x + 1];
+   if (u1 <= u0) return;              // an empty range (uniform)
+   const int T0 = u0 / ntl, T1 = (u1 - 1) / ntl;
+   // the range's units of site tile T: ua(T) .. ue(T) - 1; local index u - u0
+   auto ua = [&](int T) { return max(u0, T * ntl); };
+   auto ue = [&](int T) { return min(u1, (T + 1) * ntl); };
    unsigned char *A = sm, *Bs = sm + FTC_ABYTES;
-   float *red = reinterpret_cast<float *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES);   // [FTC_EG][128][3]
+   // [2][FTC_EG][128][3]: per epilogue group, a site tile's force sums (by tile parity)
+   float *red = reinterpret_cast<float *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES);
    // per epilogue warp: its items' (h, k, l0, count) and force coefficients
-   int4 *sitem = reinterpret_cast<int4 *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + FTC_EG * 128 * 3 * 4);
+   int4 *sitem = reinterpret_cast<int4 *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + 2 * FTC_EG * 128 * 3 * 4);
    if (tid == 0) {
       bar_init(&full_a, 1);
+      bar_init(&a_free, 2);
       for (int p = 0; p < 2; p++)
          for (int s = 0; s < FTC_NSB; s++) {
             bar_init(&full_b[p][s], 1);
@@ -506,63 +551,87 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
    __syncthreads();
    fence_after_sync();
    const unsigned int tmem = tmem_s;
-   // K-steps of an item tile: ceil(longest count / 16) in each half of K
-   auto khalf = [&](int nt) { return (item[nt * FTC_NI].w + 15) >> 4; };
+   // K-steps of a unit's item tile: ceil(longest count / 16) in each half of K
+   auto khalf = [&](int u) { return (item[(u % ntl) * FTC_NI].w + 15) >> 4; };
 
    if (w == FTC_EW || w == FTC_EW + 1) {
       // ---- bulk copies: warp FTC_EW + p streams the coefficient rows of the
-      // item tiles j = p, p + 2, ... of this CTA's range into ring p
+      // range's units of local parity p into ring p; warp FTC_EW also loads
+      // each site tile's z tables
       const int p = w - FTC_EW;
       if (lane == 0) {
-         if (p == 0) {
-            bar_expect_tx(&full_a, FTC_ABYTES);
-            bulk_load(A, zsite + (size_t)tile * (FTC_ABYTES / 16), FTC_ABYTES, &full_a);
-         }
-         int g = 0;
+         int g = 0, na = 0;
          bool stop = false;
-         for (int nt = nt0 + p; nt < nt1 && !stop; nt += 2) {
-            const int kh = khalf(nt);
-            for (int q = 0; q < 2 * kh; q++) {
-               const int ks = q < kh ? q : 4 + q - kh;
-               const int s = g % FTC_NSB;
-               if (g >= FTC_NSB && !bar_wait(&empty_b[p][s], (unsigned int)(g / FTC_NSB - 1) & 1u)) {
+         for (int T = T0; T <= T1 && !stop; T++) {
+            if (p == 0) {
+               if (T > T0 && !bar_wait(&a_free, (unsigned int)(T - T0 - 1) & 1u)) {
                   tc_abort(&abort_s, err, FTC_ERR);
-                  stop = true;
                   break;
                }
-               if (tc_aborted(&abort_s)) {
-                  stop = true;
-                  break;
+               bar_expect_tx(&full_a, FTC_ABYTES);
+               bulk_load(A, zsite + (size_t)T * (FTC_ABYTES / 16), FTC_ABYTES, &full_a);
+               na++;
+            }
+            for (int u = ua(T); u < ue(T) && !stop; u++) {
+               if (((u - u0) & 1) != p) continue;
+               const int kh = khalf(u), nt = u % ntl;
+               for (int q = 0; q < 2 * kh; q++) {
+                  const int ks = q < kh ? q : 4 + q - kh;
+                  const int s = g % FTC_NSB;
+                  if (g >= FTC_NSB && !bar_wait(&empty_b[p][s], (unsigned int)(g / FTC_NSB - 1) & 1u)) {
+                     tc_abort(&abort_s, err, FTC_ERR);
+                     stop = true;
+                     break;
+                  }
+                  if (tc_aborted(&abort_s)) {
+                     stop = true;
+                     break;
+                  }
+                  bar_expect_tx(&full_b[p][s], FTC_BBYTES);
+                  bulk_load(Bs + (p * FTC_NSB + s) * FTC_BBYTES,
+                            utab + ((size_t)nt * 8 + ks) * (FTC_BBYTES / 16), FTC_BBYTES, &full_b[p][s]);
+                  g++;
                }
-               bar_expect_tx(&full_b[p][s], FTC_BBYTES);
-               bulk_load(Bs + (p * FTC_NSB + s) * FTC_BBYTES, utab + ((size_t)nt * 8 + ks) * (FTC_BBYTES / 16),
-                         FTC_BBYTES, &full_b[p][s]);
-               g++;
             }
          }
-         if (p == 0) bar_wait(&full_a, 0);
+         // copies still in flight complete before the CTA's shared memory goes
+         if (na > 0) bar_wait(&full_a, (unsigned int)(na - 1) & 1u);
          for (int q = g > FTC_NSB ? g - FTC_NSB : 0; q < g; q++)
             bar_wait(&full_b[p][q % FTC_NSB], (unsigned int)(q / FTC_NSB) & 1u);
       }
    } else if (w == FTC_EW + 2 || w == FTC_EW + 3) {
-      // ---- MMA issue: warp FTC_EW + 2 + p takes the item tiles j = p, p + 2,
-      // ... into tensor-memory buffer p (one issuing thread sustains half the
+      // ---- MMA issue: warp FTC_EW + 2 + p takes the units of local parity
+      // p into tensor-memory buffer p (one issuing thread sustains half the
       // tensor pipe's rate at N = 128; two keep it busy)
       const int p = w - FTC_EW - 2;
-      if (lane == 0) {
-         const unsigned int idn = idesc_bf16(128, 128, false);
-         const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
-         const unsigned int a0 = saddr(A), b0 = saddr(Bs + p * FTC_NSB * FTC_BBYTES);
-         bool ok = bar_wait(&full_a, 0);
-         if (!ok) tc_abort(&abort_s, err, FTC_ERR);
-         int g = 0;
-         for (int nt = nt0 + p, jj = 0; nt < nt1 && ok; nt += 2, jj++) {
-            if (jj >= 1 && !bar_wait(&acc_empty[p], (unsigned int)(jj - 1) & 1u)) {
+      const unsigned int idn = idesc_bf16(128, 128, false);
+      const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
+      const unsigned int a0 = saddr(A), b0 = saddr(Bs + p * FTC_NSB * FTC_BBYTES);
+      bool ok = true;
+      int g = 0, jj = 0;
+      for (int T = T0; T <= T1; T++) {
+         if (T > T0) {
+            // both issuers are past the previous site tile: its z tables go
+            // once their MMAs complete
+            __syncwarp();
+            asm volatile("bar.sync 1, 64;" : : : "memory");
+            if (lane == 0) mma_commit(&a_free);
+         }
+         if (lane != 0) continue;
+         if (ok && !bar_wait(&full_a, (unsigned int)(T - T0) & 1u)) {
+            tc_abort(&abort_s, err, FTC_ERR);
+            ok = false;
+         }
+         fence_after_sync();
+         for (int u = ua(T); u < ue(T); u++) {
+            if (((u - u0) & 1) != p) continue;
+            if (ok && (tc_aborted(&abort_s) ||
+                       (jj >= 1 && !bar_wait(&acc_empty[p], (unsigned int)(jj - 1) & 1u)))) {
                tc_abort(&abort_s, err, FTC_ERR);
-               break;
+               ok = false;
             }
             fence_after_sync();
-            const int kh = khalf(nt);
+            const int kh = ok ? khalf(u) : 0;
             for (int q = 0; q < 2 * kh; q++) {
                const int ks = q < kh ? q : 4 + q - kh;
                const int s = g % FTC_NSB;
@@ -582,93 +651,118 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
                mma_commit(&empty_b[p][s]);
                g++;
             }
-            if (ok) mma_commit(&acc_full[p]);
+            mma_commit(&acc_full[p]);
+            jj++;
          }
+      }
+      if (lane == 0) {
          mma_commit(&done[p]);
          bar_wait(&done[p], 0);   // every MMA complete before the tensor memory is released
       }
    } else {
-      // ---- epilogue: site row r, items ig * FTC_IPW .. of each item tile
+      // ---- epilogue: site row r of each site tile, items ig * FTC_IPW .. of
+      // each item tile
       const int r = 32 * (w & 3) + lane, ig = w >> 2;
-      const int i = tile * 128 + r;
-      const int4 v = i < n ? ph[i] : make_int4(0, 0, 0, 0);
-      const unsigned int ux = (unsigned int)v.x, uy = (unsigned int)v.y, uz = (unsigned int)v.z;
       const unsigned int trow = tmem + ((unsigned int)(32 * (w & 3)) << 16);
       int4 *wi = sitem + w * 2 * FTC_IPW;   // [FTC_IPW] items, then [FTC_IPW] coefficients
       const float4 *wc = reinterpret_cast<const float4 *>(wi + FTC_IPW);
-      float Fx = 0.f, Fy = 0.f, Fz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
-      for (int nt = nt0, j = 0; nt < nt1; nt++, j++) {
-         const int b = j & 1;
-         const int it0 = nt * FTC_NI + ig * FTC_IPW;
-         // this tile's item records, fetched while its MMAs run
-         __syncwarp();
-         if (lane < FTC_IPW)
-            wi[lane] = item[it0 + lane];
-         else if (lane < 2 * FTC_IPW)
-            reinterpret_cast<float4 *>(wi)[lane] = coef[it0 + lane - FTC_IPW];
-         __syncwarp();
-         const bool got = bar_wait(&acc_full[b], (unsigned int)(j >> 1) & 1u);
-         if (!__all_sync(0xffffffffu, got && !tc_aborted(&abort_s))) {
-            if (lane == 0) tc_abort(&abort_s, err, FTC_ERR);
-            break;
-         }
-         fence_after_sync();
-         float fx = 0.f, fy = 0.f, fz = 0.f;
-#pragma unroll 1
-         for (int grp = 0; grp < FTC_IPW / 4; grp++) {
-            float mv[16], cv[16];
-            const unsigned int col = (unsigned int)(b * 256 + 4 * FTC_IPW * ig + 16 * grp);
-            tmem_ld16(trow + col, mv);
-            tmem_ld16(trow + col + 128, cv);
-            tmem_wait2(mv, cv);
+      bool live = true;
+      for (int T = T0; T <= T1; T++) {
+         const int i = T * 128 + r;
+         const int4 v = i < n ? ph[i] : make_int4(0, 0, 0, 0);
+         const unsigned int ux = (unsigned int)v.x, uy = (unsigned int)v.y, uz = (unsigned int)v.z;
+         float Fx = 0.f, Fy = 0.f, Fz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
+         for (int u = ua(T); u < ue(T) && live; u++) {
+            const int j = u - u0, b = j & 1;
+            const int it0 = (u % ntl) * FTC_NI + ig * FTC_IPW;
+            // this unit's item records, fetched while its MMAs run
+            __syncwarp();
+            if (lane < FTC_IPW)
+               wi[lane] = item[it0 + lane];
+            else if (lane < 2 * FTC_IPW)
+               reinterpret_cast<float4 *>(wi)[lane] = coef[it0 + lane - FTC_IPW];
+            __syncwarp();
+            const bool got = !tc_aborted(&abort_s) && bar_wait(&acc_full[b], (unsigned int)(j >> 1) & 1u);
+            if (!__all_sync(0xffffffffu, got && !tc_aborted(&abort_s))) {
+               if (lane == 0) tc_abort(&abort_s, err, FTC_ERR);
+               live = false;
+               break;
+            }
+            fence_after_sync();
+            // the warp's accumulator columns (hh sums plus the rest) into
+            // registers, then the buffer goes back to its MMA warp at once:
+            // the next unit's MMAs into it overlap this unit's arithmetic
+            float wv[FTC_IPW / 4][16];
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-               const int4 hd = wi[4 * grp + e];
-               // padding items come last; a tile of padding only issues no
-               // MMAs, so its buffer holds an earlier tile's sums (uniform)
-               if (hd.w == 0) continue;
-               const float4 cf = wc[4 * grp + e];
-               float sn, cs;
-               sincos_poly((unsigned int)hd.x * ux + (unsigned int)hd.y * uy + (unsigned int)hd.z * uz, &sn, &cs);
-               const float w1r = mv[4 * e] + cv[4 * e], w1i = mv[4 * e + 1] + cv[4 * e + 1];
-               const float w2r = mv[4 * e + 2] + cv[4 * e + 2], w2i = mv[4 * e + 3] + cv[4 * e + 3];
-               const float f1 = fmaf(cs, w1i, sn * w1r), f2 = fmaf(cs, w2i, sn * w2r);
-               fx = fmaf(cf.x, f1, fx);
-               fy = fmaf(cf.y, f1, fy);
-               fz = fmaf(cf.z, f1, fmaf(cf.w, f2, fz));
+            for (int grp = 0; grp < FTC_IPW / 4; grp++) {
+               float mv[16], cv[16];
+               const unsigned int col = (unsigned int)(b * 256 + 4 * FTC_IPW * ig + 16 * grp);
+               tmem_ld16(trow + col, mv);
+               tmem_ld16(trow + col + 128, cv);
+               tmem_wait2(mv, cv);
+#pragma unroll
+               for (int c = 0; c < 16; c++) wv[grp][c] = mv[c] + cv[c];
+            }
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) bar_arrive(&acc_empty[b]);
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+            for (int grp = 0; grp < FTC_IPW / 4; grp++) {
+#pragma unroll
+               for (int e = 0; e < 4; e++) {
+                  const int4 hd = wi[4 * grp + e];
+                  // padding items come last; a tile of padding only issues no
+                  // MMAs, so its buffer holds an earlier unit's sums (uniform)
+                  if (hd.w == 0) continue;
+                  const float4 cf = wc[4 * grp + e];
+                  float sn, cs;
+                  sincos_poly((unsigned int)hd.x * ux + (unsigned int)hd.y * uy + (unsigned int)hd.z * uz, &sn,
+                              &cs);
+                  const float w1r = wv[grp][4 * e], w1i = wv[grp][4 * e + 1];
+                  const float w2r = wv[grp][4 * e + 2], w2i = wv[grp][4 * e + 3];
+                  const float f1 = fmaf(cs, w1i, sn * w1r), f2 = fmaf(cs, w2i, sn * w2r);
+                  fx = fmaf(cf.x, f1, fx);
+                  fy = fmaf(cf.y, f1, fy);
+                  fz = fmaf(cf.z, f1, fmaf(cf.w, f2, fz));
+               }
+            }
+            kahan_add_tc(Fx, Cx, fx);
+            kahan_add_tc(Fy, Cy, fy);
+            kahan_add_tc(Fz, Cz, fz);
+         }
+         float *rt = red + (size_t)(T & 1) * FTC_EG * 128 * 3;
+         float *rr = rt + ((size_t)ig * 128 + r) * 3;
+         rr[0] = Fx - Cx;
+         rr[1] = Fy - Cy;
+         rr[2] = Fz - Cz;
+         // the four groups' sums of this site tile, then its output slot
+         __syncwarp();
+         asm volatile("bar.sync 2, %0;" : : "n"(FTC_EW * 32) : "memory");
+         if (w < 4 && i < n && !tc_aborted(&abort_s)) {
+            const double q = chg[slots[i]];
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            for (int g = 0; g < FTC_EG; g++) {
+               const float *rg = rt + ((size_t)g * 128 + r) * 3;
+               sx += (double)rg[0];
+               sy += (double)rg[1];
+               sz += (double)rg[2];
+            }
+            double *dst = fpart + (u0 > T * ntl ? 3 * (size_t)n : 0);
+            dst[i] = q * sx;
+            dst[n + i] = q * sy;
+            dst[2 * (size_t)n + i] = q * sz;
+            if (u0 <= T * ntl && u1 >= (T + 1) * ntl) {
+               double *z = fpart + 3 * (size_t)n;
+               z[i] = 0.0;
+               z[n + i] = 0.0;
+               z[2 * (size_t)n + i] = 0.0;
             }
          }
-         fence_before_sync();
-         __syncwarp();
-         if (lane == 0) bar_arrive(&acc_empty[b]);
-         kahan_add_tc(Fx, Cx, fx);
-         kahan_add_tc(Fy, Cy, fy);
-         kahan_add_tc(Fz, Cz, fz);
       }
-      float *rr = red + ((size_t)ig * 128 + r) * 3;
-      rr[0] = Fx - Cx;
-      rr[1] = Fy - Cy;
-      rr[2] = Fz - Cz;
    }
    fence_before_sync();
    __syncthreads();
-   if (w < 4) {
-      const int r = 32 * w + lane, i = tile * 128 + r;
-      if (i < n && !tc_aborted(&abort_s)) {
-         const double q = chg[slots[i]];
-         double sx = 0.0, sy = 0.0, sz = 0.0;
-         for (int g = 0; g < FTC_EG; g++) {
-            const float *rg = red + ((size_t)g * 128 + r) * 3;
-            sx += (double)rg[0];
-            sy += (double)rg[1];
-            sz += (double)rg[2];
-         }
-         double *dst = fpart + (size_t)blockIdx.y * 3 * n;
-         dst[i] = q * sx;
-         dst[n + i] = q * sy;
-         dst[2 * (size_t)n + i] = q * sz;
-      }
-   }
    if (w == FTC_EW + 2) {
       __syncwarp();
       fence_after_sync();
@@ -697,13 +791,24 @@ void ks_coef_tc(cudaStream_t st, const KsDev &d, int nitems_padded, float dkz)
                                                       d.kdat32.p, dkz, d.utab.p, d.tc_coef.p);
 }
 
-int ks_force_tc(cudaStream_t st, int nsites, const KsDev &d, int nitems_padded, const double *chg,
+int ks_force_tc(cudaStream_t st, int nsites, KsDev &d, int nitems_padded, int nsm, const double *chg,
                 const int *slots, double *fpart, int *err)
 {
-   const int np128 = (nsites + 127) / 128 * 128;
-   k_force_tc<<<dim3(np128 / 128, FTC_SPLITS), FTC_THREADS, FTC_SMEM, st>>>(
-       d.tc_item.p, d.tc_coef.p, nitems_padded, d.ph32.p, d.zsite.p, d.utab.p, chg, slots, nsites, fpart, err);
-   return FTC_SPLITS;
+   const int T = (nsites + 127) / 128, ntl = nitems_padded / FTC_NI;
+   const int G = 2 * T <= nsm ? 2 * T : std::min(nsm, T);
+   int launches = 1;
+   if (d.tc_rkey[0] != T || d.tc_rkey[1] != ntl || d.tc_rkey[2] != G || d.tc_rver != d.tc_ver) {
+      if (d.tc_ustart.ensure((size_t)G + ntl + 2) != cudaSuccess) return -1;
+      k_ftc_ranges<<<1, 256, 0, st>>>(d.tc_item.p, ntl, T, G, d.tc_ustart.p);
+      d.tc_rkey[0] = T;
+      d.tc_rkey[1] = ntl;
+      d.tc_rkey[2] = G;
+      d.tc_rver = d.tc_ver;
+      launches++;
+   }
+   k_force_tc<<<G, FTC_THREADS, FTC_SMEM, st>>>(d.tc_item.p, d.tc_coef.p, nitems_padded, d.ph32.p, d.zsite.p,
+                                                d.utab.p, chg, slots, nsites, d.tc_ustart.p, fpart, err);
+   return launches;
 }
 
 size_t ks_tc_zsite_len(int nsites)

@@ -208,6 +208,10 @@ struct KsDev {
    DBuf<uint4> zsite;      // force pass: z tables as the A operand, per 128 sites
    DBuf<uint4> utab;       // force pass: per-item coefficient rows (B operand)
    DBuf<float4> tc_coef;   // per item: kx s1, ky s1, kz0 s1, dkz s2 (row scales s)
+   DBuf<int> tc_ustart;    // force pass: the CTAs' work ranges (k_ftc_ranges)
+   long long tc_ver = 0;   // uploads of tc_item so far
+   int tc_rkey[3] = {-1, -1, -1};   // (site tiles, item tiles, CTAs) of tc_ustart
+   long long tc_rver = -1;          // tc_ver of tc_ustart
 };
 
 // Buffers of the adjoint (parameter-gradient) passes.
@@ -292,6 +296,7 @@ struct MdDev {
 
 struct mdgpu_ctx {
    int device = 0;
+   int nsm = 0;        // multiprocessors of the device (read when first needed)
    cudaStream_t own_stream = nullptr, stream = nullptr;
    mdgpu_precision prec = MDGPU_MIXED;
    std::string err;
@@ -408,7 +413,7 @@ KsShape ks_shape(int N, int nitems, int ipt, int spt);
 void ks_tables_tc(cudaStream_t st, int nsites, const KsDev &d);
 int ks_sfac_tc(cudaStream_t st, int nsites, int nk, const KsDev &d, int ntiles, double qmax, int *err);
 void ks_coef_tc(cudaStream_t st, const KsDev &d, int nitems_padded, float dkz);
-int ks_force_tc(cudaStream_t st, int nsites, const KsDev &d, int nitems_padded, const double *chg,
+int ks_force_tc(cudaStream_t st, int nsites, KsDev &d, int nitems_padded, int nsm, const double *chg,
                 const int *slots, double *fpart, int *err);
 int ks_force_tc_splits(int nsites);
 cudaError_t ks_tc_init(int device);
