@@ -1051,7 +1051,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
       CK(d.zsite.ensure(ks_tc_zsite_len(Nk)));
       CK(d.utab.ensure(ks_tc_utab_len((int)kl.tc_item.size())));
       ks_tables_tc(st, Nk, d);
-      c->launches += 2;
+      c->launches += 1;
    }
    KsShape sh = mixed ? ks_shape(Nk, ni, 1, 2) : ks_shape(Nk, ni, 1, 1);
    if (nf > 0) {

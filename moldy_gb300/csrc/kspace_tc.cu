@@ -68,40 +68,6 @@ static_assert(TC_SMEM <= 227 * 1024, "one CTA's shared memory");
 static_assert(TC_CHUNK % TC_KS == 0, "chunks hold whole stages");
 static_assert(KT == 4 * KI && KT <= 64, "an item is four KI runs, Zr and Zi fit 128 rows");
 
-// z tables of the padded site list (np a multiple of TC_KS) as the MMA's B
-// operand, per 32-site stage: [term][column group (8 sites)][row group][8
-// rows][8 sites] bf16, rows 0..63 cos(2 pi t u_z) and 64..127 its sine.
-// One thread per (8 sites, row); also zeroes the site records past n so
-// padding sites have no charge.
-__global__ void k_ztab_tc(int n, int np, int4 *__restrict__ ph, uint4 *__restrict__ ztab)
-{
-   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-   if (idx >= (long long)(np / 8) * 128) return;
-   const int q8 = (int)(idx >> 7), row = (int)(idx & 127), t = row & 63;
-   float v[8];
-#pragma unroll
-   for (int s = 0; s < 8; s++) {
-      const int i = q8 * 8 + s;
-      const unsigned int uz = i < n ? (unsigned int)ph[i].z : 0u;
-      float sn, cs;
-      sincos_rev32((unsigned int)t * uz, &sn, &cs);
-      v[s] = row < 64 ? cs : sn;
-   }
-   unsigned int h[4], m[4], l[4];
-#pragma unroll
-   for (int j = 0; j < 4; j++) tc::split3(v[2 * j], v[2 * j + 1], h[j], m[j], l[j]);
-   constexpr int G = TC_KS / 8;   // column groups per stage
-   const size_t base = (size_t)(q8 / G) * (TC_BBYTES / 16) + (q8 % G) * (TC_LBO / 16) + (row >> 3) * 8 + (row & 7);
-   ztab[base] = make_uint4(h[0], h[1], h[2], h[3]);
-   ztab[base + TC_TERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
-   ztab[base + 2 * TC_TERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
-   if (row == 0)
-      for (int s = 0; s < 8; s++) {
-         const int i = q8 * 8 + s;
-         if (i >= n && i < np) ph[i] = make_int4(0, 0, 0, 0);
-      }
-}
-
 __device__ __forceinline__ void tc_abort(int *flag, int *err, int bit = TC_ERR)
 {
    *(volatile int *)flag = 1;
@@ -349,33 +315,6 @@ constexpr int FTC_THREADS = 32 * (FTC_EW + 4);     // epilogue warps, two bulk-c
 static_assert(FTC_IPW % 4 == 0, "an epilogue warp reads its items' columns 16 at a time");
 constexpr int FTC_SPLITS = 2;                      // force slots per site (two CTAs at most per site tile)
 constexpr int FTC_ERR = 16;                        // error-word bit: a force-pass wait expired
-
-// Site tiles' z tables as the A operand: [tile][term][column group 16][row
-// group 16][8 rows][8 t] bf16; column groups 0..7 hold cos(2 pi t u_z), t =
-// 0..63, 8..15 the sines.  One thread per (site, column group).
-__global__ void k_zsite_tc(int n, int np128, const int4 *__restrict__ ph, uint4 *__restrict__ zsite)
-{
-   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-   if (idx >= (long long)np128 * 16) return;
-   const int r = (int)(idx & 127), g = (int)((idx >> 7) & 15), tile = (int)(idx >> 11);
-   const int i = tile * 128 + r;
-   const unsigned int uz = i < n ? (unsigned int)ph[i].z : 0u;
-   const int t0 = 8 * (g & 7);
-   float v[8];
-#pragma unroll
-   for (int e = 0; e < 8; e++) {
-      float sn, cs;
-      sincos_rev32((unsigned int)(t0 + e) * uz, &sn, &cs);
-      v[e] = g < 8 ? cs : sn;
-   }
-   unsigned int h[4], m[4], l[4];
-#pragma unroll
-   for (int j = 0; j < 4; j++) tc::split3(v[2 * j], v[2 * j + 1], h[j], m[j], l[j]);
-   const size_t base = (size_t)tile * (FTC_ABYTES / 16) + g * 128 + (r >> 3) * 8 + (r & 7);
-   zsite[base] = make_uint4(h[0], h[1], h[2], h[3]);
-   zsite[base + FTC_ATERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
-   zsite[base + 2 * FTC_ATERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
-}
 
 // Coefficient rows of each item from the per-k (A, B, kz): one warp per
 // item.  Layout per (item tile, K-step of 16): [term][column group 2][row
@@ -772,16 +711,74 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
 
 int ks_force_tc_splits(int) { return FTC_SPLITS; }
 
+// Both z tables, cos and sin of 2 pi t u_z for t = 0..63, split into three
+// bf16 terms:
+//   ztab, the structure factor's B operand per 32-site stage (np sites, a
+//     multiple of TC_KS): [term][column group (8 sites)][row group][8 rows]
+//     [8 sites], rows 0..63 the cosines and 64..127 the sines;
+//   zsite, the force pass's A operand per 128-site tile: [term][column group
+//     16][row group 16][8 rows (sites)][8 t], column groups 0..7 the
+//     cosines, 8..15 the sines.
+// A block of 256 threads takes 32 sites (one stage, a quarter of a tile).
+// Each thread computes the values of one site and 8 t (each value once),
+// writes them to zsite and to shared memory, from where the block writes
+// ztab.  Also zeroes the site records past n (padding sites have no
+// charge).
+__global__ void __launch_bounds__(256) k_ztabs_tc(int n, int np, int4 *__restrict__ ph, uint4 *__restrict__ ztab,
+                                                  uint4 *__restrict__ zsite)
+{
+   __shared__ float sv[32][129];   // [site][t: cosines, then sines] (padded row)
+   const int tid = threadIdx.x, sl = tid >> 3, tg = tid & 7;
+   const int i = blockIdx.x * 32 + sl;   // site (the grid covers the 128-site tiles)
+   const unsigned int uz = i < n ? (unsigned int)ph[i].z : 0u;
+   float c[8], sn[8];
+#pragma unroll
+   for (int e = 0; e < 8; e++) sincos_rev32((unsigned int)(8 * tg + e) * uz, &sn[e], &c[e]);
+   unsigned int h[4], m[4], l[4];
+   const int tile = i >> 7, r = i & 127;
+   const size_t zb = (size_t)tile * (FTC_ABYTES / 16) + (r >> 3) * 8 + (r & 7);
+#pragma unroll
+   for (int j = 0; j < 4; j++) tc::split3(c[2 * j], c[2 * j + 1], h[j], m[j], l[j]);
+   zsite[zb + tg * 128] = make_uint4(h[0], h[1], h[2], h[3]);
+   zsite[zb + tg * 128 + FTC_ATERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
+   zsite[zb + tg * 128 + 2 * FTC_ATERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+   for (int j = 0; j < 4; j++) tc::split3(sn[2 * j], sn[2 * j + 1], h[j], m[j], l[j]);
+   zsite[zb + (8 + tg) * 128] = make_uint4(h[0], h[1], h[2], h[3]);
+   zsite[zb + (8 + tg) * 128 + FTC_ATERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
+   zsite[zb + (8 + tg) * 128 + 2 * FTC_ATERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
+#pragma unroll
+   for (int e = 0; e < 8; e++) {
+      sv[sl][8 * tg + e] = c[e];
+      sv[sl][64 + 8 * tg + e] = sn[e];
+   }
+   if (i >= n && i < np) ph[i] = make_int4(0, 0, 0, 0);
+   __syncthreads();
+   // B operand of the stage: (8 sites q8, row) per thread, two each
+   const int stage = blockIdx.x;
+   if (stage * TC_KS >= np) return;   // past the structure factor's padded sites (uniform)
+#pragma unroll
+   for (int k = 0; k < 2; k++) {
+      const int id = tid + 256 * k, q8 = id >> 7, row = id & 127;
+      float v[8];
+#pragma unroll
+      for (int e = 0; e < 8; e++) v[e] = sv[8 * q8 + e][row];
+#pragma unroll
+      for (int j = 0; j < 4; j++) tc::split3(v[2 * j], v[2 * j + 1], h[j], m[j], l[j]);
+      const size_t base = (size_t)stage * (TC_BBYTES / 16) + q8 * (TC_LBO / 16) + (row >> 3) * 8 + (row & 7);
+      ztab[base] = make_uint4(h[0], h[1], h[2], h[3]);
+      ztab[base + TC_TERM / 16] = make_uint4(m[0], m[1], m[2], m[3]);
+      ztab[base + 2 * TC_TERM / 16] = make_uint4(l[0], l[1], l[2], l[3]);
+   }
+}
+
 // Host side.  Per-site operand tables (after k_prep): the z tables as the
 // structure factor's B operand and as the force pass's A operand.
 void ks_tables_tc(cudaStream_t st, int nsites, const KsDev &d)
 {
    const int np = (nsites + TC_KS - 1) / TC_KS * TC_KS;
-   const long long nthr = (long long)(np / 8) * 128;
-   k_ztab_tc<<<(unsigned int)((nthr + 255) / 256), 256, 0, st>>>(nsites, np, d.ph32.p, d.ztab.p);
    const int np128 = (nsites + 127) / 128 * 128;
-   k_zsite_tc<<<(unsigned int)(((long long)np128 * 16 + 255) / 256), 256, 0, st>>>(nsites, np128, d.ph32.p,
-                                                                                    d.zsite.p);
+   k_ztabs_tc<<<np128 / 32, 256, 0, st>>>(nsites, np, d.ph32.p, d.ztab.p, d.zsite.p);
 }
 
 // The force pass's coefficient rows (after the per-k reduction).

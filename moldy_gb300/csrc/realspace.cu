@@ -44,6 +44,7 @@ struct RsParams {
    int ncols;             // stencil columns (k_pairs_col)
    double hinv[9];
    double h[9];
+   double rn[3];          // 1/nx, 1/ny, 1/nz
    double reloc[27][3];
    double cut2, cut100, alpha, norm;
    float cut2f, bandf, alphaf, normf;
@@ -229,7 +230,10 @@ __global__ void k_gather(RsParams P, const double *__restrict__ site, const doub
    if (pos64) pos64[p] = make_double4(x, y, z, q);
    if (pos32) {
       int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
-      double s0 = (double)cx / P.nx - 0.5, s1 = (double)cy / P.ny - 0.5, s2 = (double)cz / P.nz - 0.5;
+      // the cell's corner in fractional co-ordinates (reciprocals: the FP64
+      // pipe is the cost of this kernel; FP32 cell-relative co-ordinates
+      // need the corner only to FP64 rounding)
+      double s0 = (double)cx * P.rn[0] - 0.5, s1 = (double)cy * P.rn[1] - 0.5, s2 = (double)cz * P.rn[2] - 0.5;
       double ox = P.h[0] * s0 + P.h[1] * s1 + P.h[2] * s2;
       double oy = P.h[3] * s0 + P.h[4] * s1 + P.h[5] * s2;
       double oz = P.h[6] * s0 + P.h[7] * s1 + P.h[8] * s2;
@@ -1381,6 +1385,7 @@ static RsParams make_params(mdgpu_ctx *c)
    P.nmol_ent = c->nmols_nf;
    P.nent = c->ctl.molpbc ? c->nmols_nf + (c->nsites - c->fw_site0) : c->nsites;
    P.nx = g.nx; P.ny = g.ny; P.nz = g.nz; P.ncells = g.ncells;
+   P.rn[0] = 1.0 / g.nx; P.rn[1] = 1.0 / g.ny; P.rn[2] = 1.0 / g.nz;
    P.nfull = (int)g.full.size();
    P.ncols = (int)g.cols.size();
    P.max_id = c->max_id;
