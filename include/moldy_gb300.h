@@ -149,6 +149,9 @@ mdgpu_status mdgpu_forces_device(mdgpu_ctx *ctx, const double *h, const double *
  * asynchronous calls (binning range, too-close pairs are counted in info). */
 mdgpu_status mdgpu_synchronize(mdgpu_ctx *ctx);
 
+/* The record of the last evaluation.  The mixed form's pair kernel leaves
+ * the pair count (npairs) out of its loop; this call then counts it over the
+ * binned sites the evaluation left, waiting for the context's stream. */
 mdgpu_status mdgpu_get_info(mdgpu_ctx *ctx, mdgpu_info *info);
 
 /* Diagnostic phase timing.  While enabled, every evaluation records CUDA

@@ -655,6 +655,11 @@ mdgpu_status mdgpu_synchronize(mdgpu_ctx *c)
 mdgpu_status mdgpu_get_info(mdgpu_ctx *c, mdgpu_info *info)
 {
    if (!c || !info) return MDGPU_E_ARG;
+   if (c->npairs_pending) {
+      cudaSetDevice(c->device);
+      const mdgpu_status s = rs_count_pairs(c);
+      if (s != MDGPU_OK) return s;
+   }
    *info = c->info;
    info->launches = c->launches;
    return MDGPU_OK;

@@ -326,6 +326,7 @@ struct mdgpu_ctx {
    bool rs_valid = false, rs_uploaded = false;
    mdgpu::KList kl;
    bool kl_valid = false, kl_uploaded = false;
+   bool npairs_pending = false;   // the last real-space pass left the pair count to rs_count_pairs
 
    mdgpu::RsDev rd;
    mdgpu::KsDev kd;
@@ -388,6 +389,10 @@ mdgpu_status rs_adjoint(mdgpu_ctx *c, bool loss);
 // The pair kernel and its energy/virial reduction over the sites binned by
 // the last rs_launch, on c->stream (rs_launch without cells_only runs both).
 mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys, int64_t key_cap);
+// The reference's evaluated pair count of the last real-space pass into
+// c->info.npairs, when that pass left it out (the column walk); waits for
+// the context's stream.
+mdgpu_status rs_count_pairs(mdgpu_ctx *c);
 int pot_nparams(int ptype);     // parameters the potential type reads
 // Site-pair distance histogram of the sites binned by the last rs_launch:
 // full-list counts [max_id][max_id][nbins] into c->rd.rdf_counts (zeroed

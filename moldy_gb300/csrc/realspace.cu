@@ -784,6 +784,33 @@ __global__ void k_cls_split(RsParams P, const int *__restrict__ pre, const int *
    }
 }
 
+// The partner cells of a home cell (cx, cy, cz) in stencil column cd =
+// (dx, dy, dz0, len): cc, the link-cell index of the partner column's first
+// cell; ns (1 or 2) runs of consecutive cells za[s] .. zb[s] in that column,
+// with their periodic images ix, iy (-1, 0, 1) and iz[s].
+struct ColRuns {
+   int cc, ns, ix, iy;
+   int za[2], zb[2], iz[2];
+};
+__device__ __forceinline__ ColRuns col_runs(const RsParams &P, int cx, int cy, int cz, int4 cd)
+{
+   ColRuns r;
+   int bx = cx + cd.x, by = cy + cd.y;
+   r.ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
+   r.iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
+   bx -= r.ix * P.nx;
+   by -= r.iy * P.ny;
+   r.cc = P.nz * (by + P.ny * bx);
+   const int z0 = cz + cd.z, z1 = z0 + cd.w - 1;
+   r.ns = 1;
+   if (z1 < 0) { r.za[0] = z0 + P.nz; r.zb[0] = z1 + P.nz; r.iz[0] = -1; }
+   else if (z0 >= P.nz) { r.za[0] = z0 - P.nz; r.zb[0] = z1 - P.nz; r.iz[0] = 1; }
+   else if (z0 < 0) { r.za[0] = z0 + P.nz; r.zb[0] = P.nz - 1; r.iz[0] = -1; r.za[1] = 0; r.zb[1] = z1; r.iz[1] = 0; r.ns = 2; }
+   else if (z1 >= P.nz) { r.za[0] = z0; r.zb[0] = P.nz - 1; r.iz[0] = 0; r.za[1] = 0; r.zb[1] = z1 - P.nz; r.iz[1] = 1; r.ns = 2; }
+   else { r.za[0] = z0; r.zb[0] = z1; r.iz[0] = 0; }
+   return r;
+}
+
 // One warp per home slot of the class-major layout.  A pass gives each lane
 // COL_E columns (up to two slot runs each, of the home site's class); a warp
 // prefix sum lays the runs end to end; windows of COL_WIN candidates are
@@ -818,7 +845,6 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
    const int p = blockIdx.x * PAIR_WARPS + w;   // home slot (class-major)
    int *inc = s_inc[w], *jbr = s_jb[w], *infr = s_inf[w], *cand = s_cand[w];
    R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
-   int nall = 0;   // candidates of every class (the reference's evaluated pairs)
    if (p < N) {
       const int *csk = cs + (p < n0 ? 0 : P.ncells + 1);
       const int c = cellc[p];
@@ -843,31 +869,17 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
             if (col < P.ncols) {
                const int4 cd = __ldg(&cols[col]);
                const int ob = __ldg(&col_base[col]);
-               int bx = cx + cd.x, by = cy + cd.y;
-               const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
-               const int iy = by < 0 ? -1 : (by >= P.ny ? 1 : 0);
-               bx -= ix * P.nx;
-               by -= iy * P.ny;
-               const int cc = P.nz * (by + P.ny * bx);   // the partner column's first cell
-               const int z0 = cz + cd.z, z1 = z0 + cd.w - 1;
-               // at most two runs of consecutive cells, each with one z image
-               int za[2], zb[2], iz[2], ns = 1;
-               if (z1 < 0) { za[0] = z0 + P.nz; zb[0] = z1 + P.nz; iz[0] = -1; }
-               else if (z0 >= P.nz) { za[0] = z0 - P.nz; zb[0] = z1 - P.nz; iz[0] = 1; }
-               else if (z0 < 0) { za[0] = z0 + P.nz; zb[0] = P.nz - 1; iz[0] = -1; za[1] = 0; zb[1] = z1; iz[1] = 0; ns = 2; }
-               else if (z1 >= P.nz) { za[0] = z0; zb[0] = P.nz - 1; iz[0] = 0; za[1] = 0; zb[1] = z1 - P.nz; iz[1] = 1; ns = 2; }
-               else { za[0] = z0; zb[0] = z1; iz[0] = 0; }
+               const ColRuns cr = col_runs(P, cx, cy, cz, cd);
 #pragma unroll
                for (int s = 0; s < 2; s++) {
-                  if (s < ns) {
-                     const int a = __ldg(&csk[cc + za[s]]), b = __ldg(&csk[cc + zb[s] + 1]);
+                  if (s < cr.ns) {
+                     const int a = __ldg(&csk[cr.cc + cr.za[s]]), b = __ldg(&csk[cr.cc + cr.zb[s] + 1]);
                      inc[q0 + s] = b - a;
                      jbr[q0 + s] = a;
                      tot += b - a;
                      // offset-table index of a candidate in cell z: z + eb
-                     const int eb = ob - cd.z - cz + iz[s] * P.nz;
-                     infr[q0 + s] = (eb * 32) | (9 * (ix + 1) + 3 * (iy + 1) + (iz[s] + 1));
-                     nall += __ldg(&cell_start[cc + zb[s] + 1]) - __ldg(&cell_start[cc + za[s]]);
+                     const int eb = ob - cd.z - cz + cr.iz[s] * P.nz;
+                     infr[q0 + s] = (eb * 32) | (9 * (cr.ix + 1) + 3 * (cr.iy + 1) + (cr.iz[s] + 1));
                   }
                }
             }
@@ -961,7 +973,6 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
          force[oi] = (double)Fx;
          force[N + oi] = (double)Fy;
          force[2 * N + oi] = (double)Fz;
-         nall -= 1;   // the home site itself
       }
    }
    __shared__ R wred[7][PAIR_WARPS];
@@ -979,9 +990,38 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
       for (int q = 0; q < PAIR_WARPS; q++) s += (double)wred[threadIdx.x][q];
       part[blockIdx.x * 8 + threadIdx.x] = s;
    }
+}
+
+// The reference's evaluated pair count after a column-walk pass (which
+// leaves it out of the hot loop): per home slot the sites of every class in
+// the stencil's column runs, less the site itself, summed into
+// out->npairs2.  One thread per slot; run on demand (mdgpu_get_info).
+__global__ void __launch_bounds__(256)
+k_count_col(RsParams P, const int *__restrict__ cell_start, const int4 *__restrict__ cols,
+            const int *__restrict__ cellc, DevOut *out)
+{
+   __shared__ unsigned long long sh[8];
+   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   unsigned long long n = 0;
+   if (p < P.nsites) {
+      const int c = cellc[p];
+      const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
+      for (int col = 0; col < P.ncols; col++) {
+         const ColRuns cr = col_runs(P, cx, cy, cz, __ldg(&cols[col]));
+         for (int s = 0; s < cr.ns; s++)
+            n += (unsigned long long)(__ldg(&cell_start[cr.cc + cr.zb[s] + 1]) - __ldg(&cell_start[cr.cc + cr.za[s]]));
+      }
+      n -= 1;   // the home site itself
+   }
 #pragma unroll
-   for (int o = 16; o > 0; o >>= 1) nall += __shfl_down_sync(0xffffffffu, nall, o);
-   if (lane == 0 && nall) atomicAdd((unsigned long long *)&out->npairs2, (unsigned long long)nall);
+   for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = n;
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      unsigned long long t = 0;
+      for (int w = 0; w < 8; w++) t += sh[w];
+      if (t) atomicAdd((unsigned long long *)&out->npairs2, t);
+   }
 }
 
 // Pairs across the interaction classes that come closer than the too-close
@@ -1766,6 +1806,25 @@ static mdgpu_status rs_pairs_col(mdgpu_ctx *c, const RsParams &P, double *d_forc
 #undef CK
 }
 
+mdgpu_status rs_count_pairs(mdgpu_ctx *c)
+{
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
+   if (!c->npairs_pending) return MDGPU_OK;
+   const RsParams P = make_params(c);
+   cudaStream_t st = c->stream;
+   DevOut *out = c->out.p;
+   CK(cudaMemsetAsync(&out->npairs2, 0, sizeof(out->npairs2), st));
+   k_count_col<<<(c->nsites + 255) / 256, 256, 0, st>>>(P, c->rd.cell_start.p, c->rd.cols.p, c->rd.cellc.p, out);
+   CK(cudaGetLastError());
+   int64_t n2 = 0;
+   CK(cudaMemcpyAsync(&n2, &out->npairs2, sizeof(n2), cudaMemcpyDeviceToHost, st));
+   CK(cudaStreamSynchronize(st));
+   c->info.npairs = n2 / 2;
+   c->npairs_pending = false;
+   return MDGPU_OK;
+#undef CK
+}
+
 mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys, int64_t key_cap)
 {
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_check(c, e_, #x); } while (0)
@@ -1781,9 +1840,11 @@ mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys,
    const bool ew = c->ctl.alpha > 0.0;
    const int mode = d_keys ? 1 : 0;
    cudaError_t e;
+   c->npairs_pending = false;
    if (mode == 0 && mixed && col_walk_ok(c)) {
       const mdgpu_status s = rs_pairs_col(c, P, d_force, ew, smem);
       if (s != MDGPU_OK) return s;
+      c->npairs_pending = true;   // counted on demand (rs_count_pairs)
    } else {
    switch (c->ptype) {
    case 0: e = launch_pairs_pt<0>(P, c, ew, mixed, mode, d_force, out, d_keys, key_cap, smem); break;
