@@ -327,6 +327,7 @@ struct mdgpu_ctx {
    mdgpu::KList kl;
    bool kl_valid = false, kl_uploaded = false;
    bool npairs_pending = false;   // the last real-space pass left the pair count to rs_count_pairs
+   int rs_nblk = 0;               // blocks (energy/virial partials) of the last real-space pass
 
    mdgpu::RsDev rd;
    mdgpu::KsDev kd;

@@ -811,7 +811,10 @@ __device__ __forceinline__ ColRuns col_runs(const RsParams &P, int cx, int cy, i
    return r;
 }
 
-// One warp per home slot of the class-major layout.  A pass gives each lane
+// Each warp takes home slots of the class-major layout in turn (eight
+// blocks per SM, the grid's warps striding over the slots, so that the
+// block's set-up and energy reduction are paid once per block).  Per home
+// slot, a pass gives each lane
 // COL_E columns (up to two slot runs each, of the home site's class); a warp
 // prefix sum lays the runs end to end; windows of COL_WIN candidates are
 // decoded into shared memory (slot | run << 24) and dealt out 32 at a time.
@@ -842,10 +845,17 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
 
    const int N = P.nsites, n0 = pre[N];
    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-   const int p = blockIdx.x * PAIR_WARPS + w;   // home slot (class-major)
    int *inc = s_inc[w], *jbr = s_jb[w], *infr = s_inf[w], *cand = s_cand[w];
-   R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
-   if (p < N) {
+   // the lane's energy and virial over all its home sites (per-site sums
+   // added in: two levels of FP32), kept in shared memory, which the
+   // candidate loop's registers leave no room for
+   __shared__ R s_tot[7][PAIR_WARPS * 32];
+#pragma unroll
+   for (int k = 0; k < 7; k++) s_tot[k][threadIdx.x] = R(0);
+   // home slots (class-major) w + PAIR_WARPS blockIdx.x, then a whole grid's
+   // warps further on: a few resident blocks per SM take every site
+   for (int p = blockIdx.x * PAIR_WARPS + w; p < N; p += gridDim.x * PAIR_WARPS) {
+      R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
       const int *csk = cs + (p < n0 ? 0 : P.ncells + 1);
       const int c = cellc[p];
       const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
@@ -974,9 +984,18 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
          force[N + oi] = (double)Fy;
          force[2 * N + oi] = (double)Fz;
       }
+      s_tot[0][threadIdx.x] += pe;
+      s_tot[1][threadIdx.x] += v0;
+      s_tot[2][threadIdx.x] += v1;
+      s_tot[3][threadIdx.x] += v2;
+      s_tot[4][threadIdx.x] += v3;
+      s_tot[5][threadIdx.x] += v4;
+      s_tot[6][threadIdx.x] += v5;
    }
    __shared__ R wred[7][PAIR_WARPS];
-   R vv[7] = {pe, v0, v1, v2, v3, v4, v5};
+   R vv[7];
+#pragma unroll
+   for (int k = 0; k < 7; k++) vv[k] = s_tot[k][threadIdx.x];
 #pragma unroll
    for (int k = 0; k < 7; k++) {
       R s = vv[k];
@@ -1745,10 +1764,9 @@ static bool col_walk_ok(const mdgpu_ctx *c)
 }
 
 template <int PT, bool EW>
-static cudaError_t launch_col_t(const RsParams &P, mdgpu_ctx *c, double *force, size_t smem)
+static cudaError_t launch_col_t(const RsParams &P, mdgpu_ctx *c, double *force, size_t smem, int nb)
 {
    RsDev &d = c->rd;
-   const int nb = (P.nsites + PAIR_WARPS - 1) / PAIR_WARPS;
    auto kfn = k_pairs_col<PT, EW>;
    if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1781,14 +1799,20 @@ static mdgpu_status rs_pairs_col(mdgpu_ctx *c, const RsParams &P, double *d_forc
                                                     d.sortc.p, d.cellc.p);
    CK(cudaGetLastError());
    c->launches += 5;
+   // eight resident blocks per SM (the kernel's launch bounds), each warp
+   // looping over home sites: the per-block set-up and energy reduction once
+   // per block instead of once per four sites
+   if (c->nsm <= 0) CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
+   const int nb = std::min((N + PAIR_WARPS - 1) / PAIR_WARPS, 8 * c->nsm);
+   c->rs_nblk = nb;
    cudaError_t e;
    switch (c->ptype) {
-   case 0: e = ew ? launch_col_t<0, true>(P, c, d_force, smem) : launch_col_t<0, false>(P, c, d_force, smem); break;
-   case 1: e = ew ? launch_col_t<1, true>(P, c, d_force, smem) : launch_col_t<1, false>(P, c, d_force, smem); break;
-   case 2: e = ew ? launch_col_t<2, true>(P, c, d_force, smem) : launch_col_t<2, false>(P, c, d_force, smem); break;
-   case 3: e = ew ? launch_col_t<3, true>(P, c, d_force, smem) : launch_col_t<3, false>(P, c, d_force, smem); break;
-   case 4: e = ew ? launch_col_t<4, true>(P, c, d_force, smem) : launch_col_t<4, false>(P, c, d_force, smem); break;
-   case 6: e = ew ? launch_col_t<6, true>(P, c, d_force, smem) : launch_col_t<6, false>(P, c, d_force, smem); break;
+   case 0: e = ew ? launch_col_t<0, true>(P, c, d_force, smem, nb) : launch_col_t<0, false>(P, c, d_force, smem, nb); break;
+   case 1: e = ew ? launch_col_t<1, true>(P, c, d_force, smem, nb) : launch_col_t<1, false>(P, c, d_force, smem, nb); break;
+   case 2: e = ew ? launch_col_t<2, true>(P, c, d_force, smem, nb) : launch_col_t<2, false>(P, c, d_force, smem, nb); break;
+   case 3: e = ew ? launch_col_t<3, true>(P, c, d_force, smem, nb) : launch_col_t<3, false>(P, c, d_force, smem, nb); break;
+   case 4: e = ew ? launch_col_t<4, true>(P, c, d_force, smem, nb) : launch_col_t<4, false>(P, c, d_force, smem, nb); break;
+   case 6: e = ew ? launch_col_t<6, true>(P, c, d_force, smem, nb) : launch_col_t<6, false>(P, c, d_force, smem, nb); break;
    default: return fail(c, MDGPU_E_PTYPE, "KERNEL called with unknown potential type");
    }
    CK(e);
@@ -1841,6 +1865,7 @@ mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys,
    const int mode = d_keys ? 1 : 0;
    cudaError_t e;
    c->npairs_pending = false;
+   c->rs_nblk = (N + PAIR_WARPS - 1) / PAIR_WARPS;   // blocks of partial sums for the reduction
    if (mode == 0 && mixed && col_walk_ok(c)) {
       const mdgpu_status s = rs_pairs_col(c, P, d_force, ew, smem);
       if (s != MDGPU_OK) return s;
@@ -1860,7 +1885,7 @@ mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys,
    }
    if (mode == 0) {
       CK(d.part2.ensure(8 * RS_RED));
-      k_reduce_rs<<<RS_RED, 256, 0, st>>>(d.part.p, (N + PAIR_WARPS - 1) / PAIR_WARPS, d.part2.p);
+      k_reduce_rs<<<RS_RED, 256, 0, st>>>(d.part.p, c->rs_nblk, d.part2.p);
       k_reduce_rs2<<<1, 256, 0, st>>>(d.part2.p, RS_RED, out);
       CK(cudaGetLastError());
       c->launches += 2;
