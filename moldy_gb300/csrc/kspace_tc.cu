@@ -295,22 +295,26 @@ int ks_tc_chunks(int nsites)
 // accumulator, the rest into another): the k-space force on a site is a
 // near-cancelling sum over k, and two fp16 terms (2^-22 per operand, three
 // products) raised the force error of the fixtures to 1.1e-5.  A CTA holds
-// one 128-site tile's z tables (96 KB, loaded once) and streams the coefficient rows of 32 items (N =
-// 128) per tile of items, K-step by K-step (only the K-steps an item tile's
-// longest item needs); tensor memory holds two accumulator pairs, so the
-// epilogue of one item tile (16 warps, four per tensor-memory lane quarter,
-// 8 items each: the seed sine/cosine per item and site, the k-vector
-// weights, Kahan-compensated FP32 force sums) overlaps the MMAs of the next.
+// one 128-site tile's z tables (96 KB) at a time and streams the
+// coefficient rows of 32 items (N = 128) per tile of items, two K-steps per
+// stage (only the K-steps an item tile's longest item needs; one barrier
+// wait and one commit per 12 MMAs: at one K-step per stage the issuing
+// threads' waits cost a tenth of the pass); tensor memory holds two
+// accumulator pairs, so the epilogue of one item tile (16 warps, four per
+// tensor-memory lane quarter, 8 items each: the seed sine/cosine per item
+// and site, the k-vector weights, Kahan-compensated FP32 force sums)
+// overlaps the MMAs of the next.
 constexpr int FTC_NI = 32;                         // items per item tile (4 rows each: N = 128)
-constexpr int FTC_NSB = 4;                         // coefficient stages in flight per ring (two rings)
+constexpr int FTC_NSB = 2;                         // coefficient stages in flight per ring (two rings)
 constexpr int FTC_ATERM = 128 * 128 * 2;           // one term of a site tile's z tables: 32 KB
 constexpr int FTC_ABYTES = 3 * FTC_ATERM;          // 96 KB
 constexpr int FTC_BTERM = 128 * 16 * 2;            // one term of a coefficient stage: 4 KB
 constexpr int FTC_BBYTES = 3 * FTC_BTERM;          // 12 KB
+constexpr int FTC_SBYTES = 2 * FTC_BBYTES;         // a stage: two K-steps (24 KB), one wait and commit per 12 MMAs
 constexpr int FTC_EG = 4;                          // epilogue warps per tensor-memory lane quarter
 constexpr int FTC_IPW = FTC_NI / FTC_EG;           // items of a tile per epilogue warp
 constexpr int FTC_EW = 4 * FTC_EG;                 // epilogue warps
-constexpr int FTC_SMEM = FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + 2 * FTC_EG * 128 * 3 * 4 + FTC_EW * FTC_IPW * 32;
+constexpr int FTC_SMEM = FTC_ABYTES + 2 * FTC_NSB * FTC_SBYTES + 2 * FTC_EG * 128 * 3 * 4 + FTC_EW * FTC_IPW * 32;
 constexpr int FTC_THREADS = 32 * (FTC_EW + 4);     // epilogue warps, two bulk-copy warps, two MMA warps
 static_assert(FTC_IPW % 4 == 0, "an epilogue warp reads its items' columns 16 at a time");
 constexpr int FTC_SPLITS = 2;                      // force slots per site (two CTAs at most per site tile)
@@ -464,9 +468,9 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
    auto ue = [&](int T) { return min(u1, (T + 1) * ntl); };
    unsigned char *A = sm, *Bs = sm + FTC_ABYTES;
    // [2][FTC_EG][128][3]: per epilogue group, a site tile's force sums (by tile parity)
-   float *red = reinterpret_cast<float *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES);
+   float *red = reinterpret_cast<float *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_SBYTES);
    // per epilogue warp: its items' (h, k, l0, count) and force coefficients
-   int4 *sitem = reinterpret_cast<int4 *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_BBYTES + 2 * FTC_EG * 128 * 3 * 4);
+   int4 *sitem = reinterpret_cast<int4 *>(sm + FTC_ABYTES + 2 * FTC_NSB * FTC_SBYTES + 2 * FTC_EG * 128 * 3 * 4);
    if (tid == 0) {
       bar_init(&full_a, 1);
       bar_init(&a_free, 2);
@@ -514,8 +518,9 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
             for (int u = ua(T); u < ue(T) && !stop; u++) {
                if (((u - u0) & 1) != p) continue;
                const int kh = khalf(u), nt = u % ntl;
-               for (int q = 0; q < 2 * kh; q++) {
-                  const int ks = q < kh ? q : 4 + q - kh;
+               // stage sq: K-steps q = 2 sq, 2 sq + 1 (the unit's 2 kh K-steps
+               // are the kh lowest of each half of K)
+               for (int sq = 0; sq < kh; sq++) {
                   const int s = g % FTC_NSB;
                   if (g >= FTC_NSB && !bar_wait(&empty_b[p][s], (unsigned int)(g / FTC_NSB - 1) & 1u)) {
                      tc_abort(&abort_s, err, FTC_ERR);
@@ -526,9 +531,12 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
                      stop = true;
                      break;
                   }
-                  bar_expect_tx(&full_b[p][s], FTC_BBYTES);
-                  bulk_load(Bs + (p * FTC_NSB + s) * FTC_BBYTES,
-                            utab + ((size_t)nt * 8 + ks) * (FTC_BBYTES / 16), FTC_BBYTES, &full_b[p][s]);
+                  bar_expect_tx(&full_b[p][s], FTC_SBYTES);
+                  for (int h = 0; h < 2; h++) {
+                     const int q = 2 * sq + h, ks = q < kh ? q : 4 + q - kh;
+                     bulk_load(Bs + (p * FTC_NSB + s) * FTC_SBYTES + h * FTC_BBYTES,
+                               utab + ((size_t)nt * 8 + ks) * (FTC_BBYTES / 16), FTC_BBYTES, &full_b[p][s]);
+                  }
                   g++;
                }
             }
@@ -545,7 +553,7 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
       const int p = w - FTC_EW - 2;
       const unsigned int idn = idesc_bf16(128, 128, false);
       const int ta[6] = {0, 0, 1, 0, 2, 1}, tb[6] = {0, 1, 0, 2, 0, 1};
-      const unsigned int a0 = saddr(A), b0 = saddr(Bs + p * FTC_NSB * FTC_BBYTES);
+      const unsigned int a0 = saddr(A), b0 = saddr(Bs + p * FTC_NSB * FTC_SBYTES);
       bool ok = true;
       int g = 0, jj = 0;
       for (int T = T0; T <= T1; T++) {
@@ -571,8 +579,7 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
             }
             fence_after_sync();
             const int kh = ok ? khalf(u) : 0;
-            for (int q = 0; q < 2 * kh; q++) {
-               const int ks = q < kh ? q : 4 + q - kh;
+            for (int sq = 0; sq < kh; sq++) {
                const int s = g % FTC_NSB;
                if (!bar_wait(&full_b[p][s], (unsigned int)(g / FTC_NSB) & 1u)) {
                   tc_abort(&abort_s, err, FTC_ERR);
@@ -580,12 +587,16 @@ k_force_tc(const int4 *__restrict__ item, const float4 *__restrict__ coef, int n
                   break;
                }
                fence_after_sync();
-               const unsigned int bs = b0 + s * FTC_BBYTES;
 #pragma unroll
-               for (int t = 0; t < 6; t++) {
-                  const uint64_t ad = sdesc(a0 + ta[t] * FTC_ATERM + ks * 4096, 2048, 128);
-                  const uint64_t bd = sdesc(bs + tb[t] * FTC_BTERM, 2048, 128);
-                  mma_f16(tmem + p * 256 + (t == 0 ? 0 : 128), ad, bd, idn, q > 0 || t > 1);
+               for (int h = 0; h < 2; h++) {
+                  const int q = 2 * sq + h, ks = q < kh ? q : 4 + q - kh;
+                  const unsigned int bs = b0 + s * FTC_SBYTES + h * FTC_BBYTES;
+#pragma unroll
+                  for (int t = 0; t < 6; t++) {
+                     const uint64_t ad = sdesc(a0 + ta[t] * FTC_ATERM + ks * 4096, 2048, 128);
+                     const uint64_t bd = sdesc(bs + tb[t] * FTC_BTERM, 2048, 128);
+                     mma_f16(tmem + p * 256 + (t == 0 ? 0 : 128), ad, bd, idn, q > 0 || t > 1);
+                  }
                }
                mma_commit(&empty_b[p][s]);
                g++;
