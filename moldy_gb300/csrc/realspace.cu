@@ -708,6 +708,23 @@ __global__ void __launch_bounds__(256) k_reduce_rs(const double *__restrict__ pa
    if (t < 7) part2[blockIdx.x * 8 + t] = sh[t][0];
 }
 
+// One block over all the partials (few blocks: the column walk's grid of a
+// few blocks per SM): thread t takes blocks t, t + 256, ..., then the tree.
+__global__ void __launch_bounds__(256) k_reduce_rs1(const double *__restrict__ part, int nblocks, DevOut *out)
+{
+   __shared__ double sh[7][256];
+   const int t = threadIdx.x;
+   double s[7] = {0, 0, 0, 0, 0, 0, 0};
+   for (int b = t; b < nblocks; b += 256)
+      for (int k = 0; k < 7; k++) s[k] += part[b * 8 + k];
+   for (int k = 0; k < 7; k++) sh[k][t] = s[k];
+   tree7(sh, t);
+   if (t == 0) {
+      out->pe_rs = sh[0][0];
+      for (int k = 0; k < 6; k++) out->vir_rs[k] = sh[k + 1][0];
+   }
+}
+
 __global__ void __launch_bounds__(256) k_reduce_rs2(const double *__restrict__ part2, int n, DevOut *out)
 {
    __shared__ double sh[7][256];
@@ -738,9 +755,10 @@ __global__ void __launch_bounds__(256) k_reduce_rs2(const double *__restrict__ p
 // forces, energy and virial: each home site walks the sites of its own class
 // only (rigid water: O meets only O, H and M only H and M -- 37.5% of the
 // ordered pairs skipped).  The slots are re-laid class by class, each class
-// in link-cell order, with per-class cell starts.  The pair count still
-// counts every class (the reference's evaluated pairs), and pairs across the
-// classes closer than the too-close distance are reported by k_tooclose_x.
+// in link-cell order, with per-class cell starts.  The reference's evaluated
+// pair count (every class) is counted on demand by k_count_col, and pairs
+// across the classes closer than the too-close distance are reported by
+// k_tooclose_x.
 constexpr int COL_E = 3;                    // stencil columns per lane in one pass
 constexpr int COL_ROWS = 32 * COL_E * 2;    // slot runs per pass (two per column at most)
 constexpr int COL_WIN = 256;                // candidates decoded per window
@@ -1884,11 +1902,16 @@ mdgpu_status rs_pairs(mdgpu_ctx *c, double *d_force, unsigned long long *d_keys,
    c->launches += 1;
    }
    if (mode == 0) {
-      CK(d.part2.ensure(8 * RS_RED));
-      k_reduce_rs<<<RS_RED, 256, 0, st>>>(d.part.p, c->rs_nblk, d.part2.p);
-      k_reduce_rs2<<<1, 256, 0, st>>>(d.part2.p, RS_RED, out);
+      if (c->rs_nblk <= 8 * 256) {
+         k_reduce_rs1<<<1, 256, 0, st>>>(d.part.p, c->rs_nblk, out);
+         c->launches += 1;
+      } else {
+         CK(d.part2.ensure(8 * RS_RED));
+         k_reduce_rs<<<RS_RED, 256, 0, st>>>(d.part.p, c->rs_nblk, d.part2.p);
+         k_reduce_rs2<<<1, 256, 0, st>>>(d.part2.p, RS_RED, out);
+         c->launches += 2;
+      }
       CK(cudaGetLastError());
-      c->launches += 2;
    }
    phase_mark(c, MDGPU_PH_KPREP);
    return MDGPU_OK;
