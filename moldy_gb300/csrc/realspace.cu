@@ -387,7 +387,7 @@ __device__ __forceinline__ double block_sum_d(double v, double *sh)
    return s;   // valid in thread 0
 }
 
-constexpr int PAIR_WARPS = 4;   // warps per block (8k registers: a block fits beside a tensor-core CTA)
+constexpr int PAIR_WARPS = 4;   // warps per block
 
 // Per-warp shared rows of the stencil walk (32 WALK_E entries), and the
 // stencil's cell-offset vectors (global, read by entry).
@@ -762,6 +762,7 @@ __global__ void __launch_bounds__(256) k_reduce_rs2(const double *__restrict__ p
 constexpr int COL_E = 3;                    // stencil columns per lane in one pass
 constexpr int COL_ROWS = 32 * COL_E * 2;    // slot runs per pass (two per column at most)
 constexpr int COL_WIN = 256;                // candidates decoded per window
+constexpr int COL_CHUNK = 16;               // consecutive home slots a block takes at a time
 
 // per slot (link-cell order): 1 when its identifier is in class 0; the
 // entry after the last is 0 (so the exclusive scan ends with the class-0
@@ -870,9 +871,14 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
    __shared__ R s_tot[7][PAIR_WARPS * 32];
 #pragma unroll
    for (int k = 0; k < 7; k++) s_tot[k][threadIdx.x] = R(0);
-   // home slots (class-major) w + PAIR_WARPS blockIdx.x, then a whole grid's
-   // warps further on: a few resident blocks per SM take every site
-   for (int p = blockIdx.x * PAIR_WARPS + w; p < N; p += gridDim.x * PAIR_WARPS) {
+   // home slots (class-major) in chunks of COL_CHUNK consecutive slots, the
+   // grid's blocks taking the chunks in turn and the block's warps the
+   // chunk's slots in turn: a few resident blocks per SM take every site,
+   // neighbouring sites (shared candidates and column starts in L1) at
+   // about the same time
+   for (int it = 0, p = blockIdx.x * COL_CHUNK + w; p < N;
+        it++, p = ((it / (COL_CHUNK / PAIR_WARPS)) * gridDim.x + blockIdx.x) * COL_CHUNK +
+                  (it % (COL_CHUNK / PAIR_WARPS)) * PAIR_WARPS + w) {
       R fx = 0, fy = 0, fz = 0, pe = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
       const int *csk = cs + (p < n0 ? 0 : P.ncells + 1);
       const int c = cellc[p];
