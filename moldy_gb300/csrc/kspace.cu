@@ -404,19 +404,19 @@ k_kreduce(int nk, int nchunks, const float2 *__restrict__ p32, const double2 *__
    }
 }
 
-// Per-block energy/stress partials summed in a fixed order by one block
-// (any multiple of 32 threads up to 1024): thread t takes blocks t, t + T,
-// ..., then fixed-shape warp and cross-warp trees.
-// First level of the k-space energy/stress sum when there are many per-k
-// blocks: block b sums the contiguous slice b of the block records (fixed
-// order), so the single-block final sum below reads only gridDim.x
-// records (one SM's FP64 adds were the cost of a one-level sum).
+// The k-space energy/stress sum when there are many per-k blocks: block b
+// sums the contiguous slice b of the block records (fixed order), and the
+// block that finishes last (a counter, reset by it for the next evaluation)
+// sums the gridDim.x slice records in a fixed order into out (one SM's FP64
+// adds were the cost of a one-level sum).
 constexpr int KF_PARTS = 64;   // first-level blocks of the k-space energy/stress sum
 
 __global__ void __launch_bounds__(128) k_kfinal_part(const double *__restrict__ blk, int nblocks,
-                                                     double *__restrict__ blk2)
+                                                     double *__restrict__ blk2, unsigned int *__restrict__ count,
+                                                     DevOut *__restrict__ out)
 {
    __shared__ double sh[4][8];
+   __shared__ bool last;
    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
    const int per = (nblocks + gridDim.x - 1) / gridDim.x;
    const int b0 = blockIdx.x * per, b1 = min(nblocks, b0 + per);
@@ -429,9 +429,29 @@ __global__ void __launch_bounds__(128) k_kfinal_part(const double *__restrict__ 
    if (lane == 0)
       for (int k = 0; k < 7; k++) sh[w][k] = v[k];
    __syncthreads();
-   if (t < 7) blk2[blockIdx.x * 8 + t] = ((sh[0][t] + sh[1][t]) + sh[2][t]) + sh[3][t];
+   if (t < 7) {
+      blk2[blockIdx.x * 8 + t] = ((sh[0][t] + sh[1][t]) + sh[2][t]) + sh[3][t];
+      __threadfence();
+   }
+   __syncthreads();
+   if (t == 0) last = atomicAdd(count, 1u) == gridDim.x - 1;
+   __syncthreads();
+   if (!last) return;
+   __threadfence();
+   if (t < 7) {
+      double s = 0.0;
+      for (int b = 0; b < (int)gridDim.x; b++) s += __ldcg(&blk2[b * 8 + t]);
+      if (t == 0)
+         out->pe_k = s;
+      else
+         out->st_k[t - 1] = s;
+   }
+   if (t == 0) *count = 0u;
 }
 
+// Per-block energy/stress partials summed in a fixed order by one block
+// (any multiple of 32 threads up to 1024): thread t takes blocks t, t + T,
+// ..., then fixed-shape warp and cross-warp trees.
 __global__ void __launch_bounds__(1024) k_kfinal(const double *__restrict__ blk, int nblocks, DevOut *out)
 {
    __shared__ double sh[32][8];
@@ -948,6 +968,10 @@ mdgpu_status ks_prepare(mdgpu_ctx *c)
       CK(d.utab.ensure(ks_tc_utab_len((int)kl.tc_item.size())));
    }
    CK(d.ph32.ensure(N + 128));
+   if (!d.kcount.p) {   // k_kfinal_part's finished-block counter, zero between evaluations
+      CK(d.kcount.ensure(1));
+      CK(cudaMemsetAsync(d.kcount.p, 0, sizeof(unsigned int), st));
+   }
    CK(d.z32.ensure(N));
    CK(d.zp32.ensure((size_t)N * KI));
    CK(d.ph64a.ensure(N));
@@ -1112,9 +1136,7 @@ mdgpu_status ks_launch(mdgpu_ctx *c, const double *d_site, double *d_force, bool
    }
    if (nbk > 4 * KF_PARTS) {
       CK(d.blk2.ensure(8 * (size_t)KF_PARTS));
-      k_kfinal_part<<<KF_PARTS, 128, 0, st>>>(d.blk.p, nbk, d.blk2.p);
-      k_kfinal<<<1, 512, 0, st>>>(d.blk2.p, KF_PARTS, out);
-      c->launches += 1;
+      k_kfinal_part<<<KF_PARTS, 128, 0, st>>>(d.blk.p, nbk, d.blk2.p, d.kcount.p, out);
    } else {
       k_kfinal<<<1, 512, 0, st>>>(d.blk.p, nbk, out);
    }

@@ -187,6 +187,7 @@ struct KsDev {
    DBuf<double> fpart;     // [splits][3][N] force partials
    DBuf<double> blk;       // per-block energy/stress partials
    DBuf<double> blk2;      // their first-level sums
+   DBuf<unsigned int> kcount;   // k_kfinal_part: blocks finished (the last one sums the slices)
    // framework molecule: framework-charge channel, its structure factor,
    // negated framework coefficients, its sites' records held compactly
    DBuf<int> fslot, sortedc;

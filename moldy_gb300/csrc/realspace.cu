@@ -1070,9 +1070,9 @@ k_count_col(RsParams P, const int *__restrict__ cell_start, const int4 *__restri
 // Pairs across the interaction classes that come closer than the too-close
 // distance (the reference warns of every evaluated pair with r^2 < 0.25,
 // src/force.c:943-948, whatever its potential): such a pair lies in the
-// 27-cell neighbourhood (cells at least 0.5 A thick).  One thread per
-// class-0 slot (class-major layout) takes the class-1 sites of the
-// neighbourhood, 9 column runs of 3 cells, and forms r^2 in FP32 from the
+// 27-cell neighbourhood (cells at least 0.5 A thick).  For each class-0
+// slot (class-major layout) nine threads take the class-1 sites of the
+// neighbourhood, one column run of 3 cells each, and form r^2 in FP32 from the
 // cell-relative co-ordinates and the exact cell offset (hi + lo), re-made
 // in FP64 from the original co-ordinates with the reference's operation
 // order within 1e-3 A^2 of the threshold, as k_pairs decides.  Reported
@@ -1089,7 +1089,8 @@ k_tooclose_x(RsParams P, NbCols nb, const int *__restrict__ cs, const int *__res
              const float4 *__restrict__ posc, const int2 *__restrict__ tagc, const int *__restrict__ cellc,
              const int *__restrict__ sortc, const double *__restrict__ site, DevOut *out)
 {
-   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   const int p = t / 9, d = t - 9 * p;   // one column of the neighbourhood per thread
    const int N = P.nsites, n0 = pre[N];
    if (p >= n0) return;
    const int *cs1 = cs + P.ncells + 1;
@@ -1097,7 +1098,7 @@ k_tooclose_x(RsParams P, NbCols nb, const int *__restrict__ cs, const int *__res
    const int cx = c / (P.ny * P.nz), cy = (c / P.nz) % P.ny, cz = c % P.nz;
    const float4 xi = posc[p];
    const int moli = tagc[p].y, oi = sortc[p];
-   for (int d = 0; d < 9; d++) {
+   {
       const int dx = d / 3 - 1, dy = d % 3 - 1;
       int bx = cx + dx, by = cy + dy;
       const int ix = bx < 0 ? -1 : (bx >= P.nx ? 1 : 0);
@@ -1844,7 +1845,7 @@ static mdgpu_status rs_pairs_col(mdgpu_ctx *c, const RsParams &P, double *d_forc
    if (two) {
       NbCols nb;
       for (int k = 0; k < 9; k++) nb.col[k] = c->rs.nbcol[k];
-      k_tooclose_x<<<(N + 255) / 256, 256, 0, st>>>(P, nb, d.cs.p, d.cls_pre.p, d.cols.p, d.col_base.p, d.coff_hi.p,
+      k_tooclose_x<<<(9 * N + 255) / 256, 256, 0, st>>>(P, nb, d.cs.p, d.cls_pre.p, d.cols.p, d.col_base.p, d.coff_hi.p,
                                                     d.coff_lo.p, d.posc.p, d.tagc.p, d.cellc.p, d.sortc.p,
                                                     c->cur_site, c->out.p);
       CK(cudaGetLastError());
