@@ -36,9 +36,14 @@ constexpr double INERTIA_MIN = 1.0e-14;   // src/defs.h:298
 constexpr double AMOM_EPS = 8.0e-37;      // 8 * DBL_MIN as src/leapfrog.c:88-90 defines it
 constexpr double QNORM_TOL = 1.0e-4;      // TOLERANCE, src/leapfrog.c:78
 
-#define DM(a, b) __dmul_rn(a, b)
-#define DA(a, b) __dadd_rn(a, b)
-#define DS(a, b) __dsub_rn(a, b)
+// FP64 products and sums in the reference's operation order; the compiler
+// fuses a product into the following sum (FMA, one rounding instead of
+// two), as a build of the reference for a CPU with FMA does: these kernels
+// are bound by the FP64 pipe, and the fused form takes about a third fewer
+// of its instructions.
+#define DM(a, b) ((a) * (b))
+#define DA(a, b) ((a) + (b))
+#define DS(a, b) ((a) - (b))
 
 struct MdStepParams {
    int nmols, nsites, molpbc, nosym, saxis, o1, o2;
