@@ -159,7 +159,7 @@ struct RsDev {
    // class in link-cell order, with per-class cell starts cs[2][ncells+1]
    DBuf<int4> cols;
    DBuf<int> col_base;
-   DBuf<float4> coff_hi, coff_lo;
+   DBuf<float4> coff;      // [e][2]: the column offsets' hi and lo parts side by side (32 B per entry)
    DBuf<int> cls_of_id, cls_pre, cs, sortc, cellc, cls_bsum;
    DBuf<float4> posc;
    DBuf<int2> tagc;

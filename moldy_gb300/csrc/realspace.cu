@@ -803,6 +803,14 @@ __global__ void k_cls_split(RsParams P, const int *__restrict__ pre, const int *
    }
 }
 
+// A column offset's hi and lo parts (32 bytes, 32-byte aligned) in one load.
+__device__ __forceinline__ void ld_coff(const float4 *p, float4 &h, float4 &l)
+{
+   asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+       : "=f"(h.x), "=f"(h.y), "=f"(h.z), "=f"(h.w), "=f"(l.x), "=f"(l.y), "=f"(l.z), "=f"(l.w)
+       : "l"(p));
+}
+
 // The partner cells of a home cell (cx, cy, cz) in stencil column cd =
 // (dx, dy, dz0, len): cc, the link-cell index of the partner column's first
 // cell; ns (1 or 2) runs of consecutive cells za[s] .. zb[s] in that column,
@@ -845,8 +853,8 @@ template <int PT, bool EW>
 __global__ void __launch_bounds__(PAIR_WARPS * 32, 8)
 k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restrict__ cs,
             const int *__restrict__ pre, const int4 *__restrict__ cols, const int *__restrict__ col_base,
-            const float4 *__restrict__ coff_hi, const float4 *__restrict__ coff_lo,
-            const float4 *__restrict__ posc, const int2 *__restrict__ tagc, const int *__restrict__ cellc,
+            const float4 *__restrict__ coff, const float4 *__restrict__ posc, const int2 *__restrict__ tagc,
+            const int *__restrict__ cellc,
             const int *__restrict__ sortc, const double *__restrict__ site, const float *__restrict__ potg,
             double *__restrict__ force, double *__restrict__ part, DevOut *out)
 {
@@ -952,7 +960,8 @@ k_pairs_col(RsParams P, const int *__restrict__ cell_start, const int *__restric
                      const int2 tj = __ldg(&tagc[j]);
                      const int e = (tj.x >> 16) + (inf_q >> 5);
                      const float4 xj = __ldg(&posc[j]);
-                     const float4 h4 = __ldg(&coff_hi[e]), l4 = __ldg(&coff_lo[e]);
+                     float4 h4, l4;
+                     ld_coff(coff + 2 * e, h4, l4);
                      const R rx = (h4.x + (xj.x - xi.x)) + l4.x;
                      const R ry = (h4.y + (xj.y - xi.y)) + l4.y;
                      const R rz = (h4.z + (xj.z - xi.z)) + l4.z;
@@ -1085,8 +1094,8 @@ struct NbCols {
 __global__ void __launch_bounds__(256)
 k_tooclose_x(RsParams P, NbCols nb, const int *__restrict__ cs, const int *__restrict__ pre,
              const int4 *__restrict__ cols, const int *__restrict__ col_base,
-             const float4 *__restrict__ coff_hi, const float4 *__restrict__ coff_lo,
-             const float4 *__restrict__ posc, const int2 *__restrict__ tagc, const int *__restrict__ cellc,
+             const float4 *__restrict__ coff, const float4 *__restrict__ posc, const int2 *__restrict__ tagc,
+             const int *__restrict__ cellc,
              const int *__restrict__ sortc, const double *__restrict__ site, DevOut *out)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1122,7 +1131,8 @@ k_tooclose_x(RsParams P, NbCols nb, const int *__restrict__ cs, const int *__res
             if (tj.y == moli) continue;
             const int e = (tj.x >> 16) + iz[s] * P.nz + eb;
             const float4 xj = posc[j];
-            const float4 h4 = __ldg(&coff_hi[e]), l4 = __ldg(&coff_lo[e]);
+            float4 h4, l4;
+            ld_coff(coff + 2 * e, h4, l4);
             const float rx = (h4.x + (xj.x - xi.x)) + l4.x;
             const float ry = (h4.y + (xj.y - xi.y)) + l4.y;
             const float rz = (h4.z + (xj.z - xi.z)) + l4.z;
@@ -1581,12 +1591,15 @@ mdgpu_status rs_prepare(mdgpu_ctx *c)
       CK(cudaMemcpyAsync(d.off_lo.p, g.off_lo.data(), g.off_lo.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
       CK(d.cols.ensure(g.cols.size()));
       CK(d.col_base.ensure(g.col_base.size()));
-      CK(d.coff_hi.ensure(g.coff_hi.size()));
-      CK(d.coff_lo.ensure(g.coff_lo.size()));
+      std::vector<float4> coff(2 * g.coff_hi.size());
+      for (size_t e = 0; e < g.coff_hi.size(); e++) {
+         coff[2 * e] = g.coff_hi[e];
+         coff[2 * e + 1] = g.coff_lo[e];
+      }
+      CK(d.coff.ensure(coff.size()));
       CK(cudaMemcpyAsync(d.cols.p, g.cols.data(), g.cols.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(d.col_base.p, g.col_base.data(), g.col_base.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(d.coff_hi.p, g.coff_hi.data(), g.coff_hi.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(d.coff_lo.p, g.coff_lo.data(), g.coff_lo.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.coff.p, coff.data(), coff.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
       CK(d.cs.ensure(2 * ((size_t)g.ncells + 1)));
       CK(cudaStreamSynchronize(st));
       c->rs_uploaded = true;
@@ -1798,7 +1811,7 @@ static cudaError_t launch_col_t(const RsParams &P, mdgpu_ctx *c, double *force, 
       if (e != cudaSuccess) return e;
    }
    kfn<<<nb, PAIR_WARPS * 32, smem, c->stream>>>(P, d.cell_start.p, d.cs.p, d.cls_pre.p, d.cols.p, d.col_base.p,
-                                                 d.coff_hi.p, d.coff_lo.p, d.posc.p, d.tagc.p, d.cellc.p,
+                                                 d.coff.p, d.posc.p, d.tagc.p, d.cellc.p,
                                                  d.sortc.p, c->cur_site, d.pot32.p, force, d.part.p, c->out.p);
    return cudaGetLastError();
 }
@@ -1845,8 +1858,8 @@ static mdgpu_status rs_pairs_col(mdgpu_ctx *c, const RsParams &P, double *d_forc
    if (two) {
       NbCols nb;
       for (int k = 0; k < 9; k++) nb.col[k] = c->rs.nbcol[k];
-      k_tooclose_x<<<(9 * N + 255) / 256, 256, 0, st>>>(P, nb, d.cs.p, d.cls_pre.p, d.cols.p, d.col_base.p, d.coff_hi.p,
-                                                    d.coff_lo.p, d.posc.p, d.tagc.p, d.cellc.p, d.sortc.p,
+      k_tooclose_x<<<(9 * N + 255) / 256, 256, 0, st>>>(P, nb, d.cs.p, d.cls_pre.p, d.cols.p, d.col_base.p, d.coff.p,
+                                                    d.posc.p, d.tagc.p, d.cellc.p, d.sortc.p,
                                                     c->cur_site, c->out.p);
       CK(cudaGetLastError());
       c->launches += 1;
