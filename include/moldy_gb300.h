@@ -447,6 +447,20 @@ mdgpu_status mdgpu_tc_rate(int device, int n, int reps, int nacc, int issuers, i
  * charge 1, neighbour charge chgsq, Ewald alpha as given. */
 double mdgpu_poteval(const double *potpar, double r, int ptype, double chgsq, double alpha);
 
+/* The link-cell stencil for cell h (row-major) and the control values (host
+ * only, no device needed): grid = (nx, ny, nz); half[3 i ..] = the
+ * reference's half-space neighbour offsets (dx, dy, dz) in its order, the
+ * zero offset included (*nhalf of them, the NABORS count); cols[5 c ..] =
+ * the column walk's regrouping of the full stencil (the half-space offsets,
+ * their mirrors and zero) into runs of consecutive dz, (dx, dy, dz0, len,
+ * base) sorted by (dx, dy, dz0); coff[6 (base + t) ..] = the FP32 hi and lo
+ * parts of the cell offset h (dx/nx, dy/ny, (dz0 + t)/nz) of each run's
+ * t-th cell.  Any of half, cols, coff may be NULL; MDGPU_E_CAPACITY if a
+ * list exceeds cap entries; MDGPU_E_CUTOFF as for the force call.  No
+ * counterpart in the reference. */
+mdgpu_status mdgpu_stencil_columns(const double *h, const mdgpu_control *ctl, int *grid, int *half, int *nhalf,
+                                   int *cols, float *coff, int *ncols, int cap);
+
 /* The tensor-core work items of the k-list for cell h (row-major) and the
  * control values (host only, no device needed): runs of up to 64 l values of
  * one (h, k) column, largest count first, padded with empty runs to a

@@ -21,7 +21,7 @@ EXPORTS = ["mdgpu_create", "mdgpu_destroy", "mdgpu_last_error", "mdgpu_set_preci
            "mdgpu_set_stream", "mdgpu_get_stream", "mdgpu_set_system", "mdgpu_set_control",
            "mdgpu_force_calc", "mdgpu_ewald", "mdgpu_forces", "mdgpu_forces_device",
            "mdgpu_synchronize", "mdgpu_get_info", "mdgpu_pair_keys", "mdgpu_poteval",
-           "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak", "mdgpu_tc_probe", "mdgpu_tc_rate", "mdgpu_tc_items",
+           "mdgpu_set_phase_timing", "mdgpu_phase_times", "mdgpu_fma_peak", "mdgpu_tc_probe", "mdgpu_tc_rate", "mdgpu_tc_items", "mdgpu_stencil_columns",
            "mdgpu_ewald_kspace_noalloc", "mdgpu_set_params", "mdgpu_energy_grad",
            "mdgpu_fm_loss_grad", "mdgpu_md_init", "mdgpu_md_run", "mdgpu_md_get_state", "mdgpu_md_set_state",
            "mdgpu_md_set_thermostat", "mdgpu_md_get_thermostat", "mdgpu_md_set_barostat",
@@ -132,6 +132,8 @@ def load():
         "mdgpu_tc_probe": ([ip, vp, vp, vp, vp, ip, ip, vp], ip),
         "mdgpu_tc_rate": ([ip, ip, ip, ip, ip, ip, dp], ip),
         "mdgpu_tc_items": ([dp, C.POINTER(ControlDesc), vp, vp, ip, C.POINTER(ip), C.POINTER(ip)], ip),
+        "mdgpu_stencil_columns": ([dp, C.POINTER(ControlDesc), vp, vp, C.POINTER(ip), vp, vp, C.POINTER(ip), ip],
+                                  ip),
         "mdgpu_ewald_kspace_noalloc": ([dp, ip, vp, vp, C.c_double, C.c_double, vp, vp, vp, vp], ip),
         "mdgpu_set_params": ([vp, C.POINTER(Params)], ip),
         "mdgpu_md_init": ([vp, C.POINTER(Dynamics), dp, dp, dp, dp, dp], ip),

@@ -749,6 +749,38 @@ mdgpu_status mdgpu_tc_items(const double *h, const mdgpu_control *ctl, int *item
    return MDGPU_OK;
 }
 
+mdgpu_status mdgpu_stencil_columns(const double *h, const mdgpu_control *ctl, int *grid, int *half, int *nhalf,
+                                   int *cols, float *coff, int *ncols, int cap)
+{
+   if (!h || !ctl || !grid || !nhalf || !ncols || cap < 0) return MDGPU_E_ARG;
+   RsGeom g;
+   mdgpu_status s = build_rs_geom(h, *ctl, g);
+   if (s) return s;
+   grid[0] = g.nx;
+   grid[1] = g.ny;
+   grid[2] = g.nz;
+   *nhalf = g.n_half;
+   *ncols = (int)g.cols.size();
+   if (g.n_half > cap || (int)g.cols.size() > cap || (int)g.coff_hi.size() > cap) return MDGPU_E_CAPACITY;
+   if (half)
+      for (int i = 0; i < 3 * g.n_half; i++) half[i] = g.half[i];
+   for (size_t i = 0; i < g.cols.size(); i++)
+      if (cols) {
+         cols[5 * i] = g.cols[i].x;
+         cols[5 * i + 1] = g.cols[i].y;
+         cols[5 * i + 2] = g.cols[i].z;
+         cols[5 * i + 3] = g.cols[i].w;
+         cols[5 * i + 4] = g.col_base[i];
+      }
+   if (coff)
+      for (size_t e = 0; e < g.coff_hi.size(); e++) {
+         const float4 a = g.coff_hi[e], b = g.coff_lo[e];
+         const float v[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
+         for (int r = 0; r < 6; r++) coff[6 * e + r] = v[r];
+      }
+   return MDGPU_OK;
+}
+
 // ------------------------------------------------ reference signatures
 // The caller's globals and log functions (src/main.c:83-84,
 // src/output.c:131-190), bound if the executable defines them.
