@@ -299,7 +299,7 @@ int ks_tc_chunks(int nsites)
 // coefficient rows of 32 items (N = 128) per tile of items, two K-steps per
 // stage (only the K-steps an item tile's longest item needs; one barrier
 // wait and one commit per 12 MMAs: at one K-step per stage the issuing
-// threads' waits cost a tenth of the pass); tensor memory holds two
+// threads' waits cost 6 % of the pass); tensor memory holds two
 // accumulator pairs, so the epilogue of one item tile (16 warps, four per
 // tensor-memory lane quarter, 8 items each: the seed sine/cosine per item
 // and site, the k-vector weights, Kahan-compensated FP32 force sums)
