@@ -22,11 +22,11 @@
 // Precision.  Charges are scaled by a power of two to |q| < 1, and every
 // FP32 operand is split into three bf16 terms on fixed grids (tc.cuh): the
 // hi*hi products go to their own tensor-memory accumulators (D1, D2), where
-// their sums are exact (multiples of 2^-14 below 2^10: a partial of at most 1024 sites
+// their sums are exact (multiples of 2^-14 below 2^10: a 1024-site partial
 // of terms of magnitude < 1), so the accumulator's round-toward-zero never
 // acts on them; hm, mh, hl, lh and mm go to a second pair, 2^-8 smaller.
 // The terms left out and the splitting are within 2^-24 of each operand, as
-// for the FP32 path.  Each CTA sums 960 sites and writes one partial per k;
+// for the FP32 path.  Each CTA sums 1024 sites and writes one partial per k;
 // the partials are added in compensated FP32 and FP64 by the per-k
 // reduction.
 //
@@ -54,11 +54,7 @@ constexpr int TC_NSB = 3;                          // z-table buffers (bulk copi
 constexpr int TC_TERM = 128 * TC_KS * 2;           // one 128-row bf16 operand of a stage: 8 KB
 constexpr int TC_ABYTES = 6 * TC_TERM;             // Ar, Ai x (hi, mid, lo)
 constexpr int TC_BBYTES = 3 * TC_TERM;             // [Zr | Zi] x (hi, mid, lo)
-// Sites per CTA (one partial per k), at most 1024.  960: for 98,304 charged
-// sites and 13 item tiles, 1,339 CTAs fill 8.8 waves of one CTA per SM on
-// 152 SMs where 1024 left the ninth wave a fifth full (structure factor
-// 0.414 -> 0.400 ms).
-constexpr int TC_CHUNK = 960;
+constexpr int TC_CHUNK = 1024;                     // sites per CTA (one partial per k)
 constexpr int TC_PBYTES = TC_KS * 16;              // a stage's site records (u_x, u_y, u_z, q)
 constexpr int TC_AOFF = 0, TC_BOFF = TC_AOFF + TC_NSA * TC_ABYTES, TC_POFF = TC_BOFF + TC_NSB * TC_BBYTES;
 constexpr int TC_SMEM = TC_POFF + TC_NSB * TC_PBYTES;
@@ -69,7 +65,7 @@ constexpr int TC_THREADS = 32 * (TC_AW + 3);       // and a bulk-copy warp, two 
 
 static_assert(TC_AOFF % 1024 == 0 && TC_BOFF % 1024 == 0 && TC_POFF % 16 == 0, "operand buffers stay aligned");
 static_assert(TC_SMEM <= 227 * 1024, "one CTA's shared memory");
-static_assert(TC_CHUNK % TC_KS == 0 && TC_CHUNK <= 1024, "chunks hold whole stages, exact hh sums");
+static_assert(TC_CHUNK % TC_KS == 0, "chunks hold whole stages");
 static_assert(KT == 4 * KI && KT <= 64, "an item is four KI runs, Zr and Zi fit 128 rows");
 
 __device__ __forceinline__ void tc_abort(int *flag, int *err, int bit = TC_ERR)

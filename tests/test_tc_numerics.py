@@ -5,7 +5,7 @@ each grid reached by (v + C) - C with C = 1.5 2^(23 - bits)), so that
 
 * every term is exactly representable in bf16,
 * |v - hi - mid - lo| <= 2^-24 for |v| <= 1,
-* sums of hi*hi products of a chunk of up to 1024 sites are exact in FP32 in any
+* sums of hi*hi products of a 1024-site chunk are exact in FP32 in any
   order (the property that makes the tensor cores' truncating FP32
   accumulation harmless for the large accumulator).
 """
